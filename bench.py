@@ -1,0 +1,378 @@
+"""Benchmark: batched HMC on Bayesian logistic regression.
+
+Workload (the multi-chain HMC configuration): X 10,000 x 50 fp32 iid N(0,1),
+w ~ N(0,1)^50, b ~ N(0,1), y ~ Bernoulli(sigmoid(Xw + b)); priors N(0,1);
+4,096 independent chains started from N(0,1); 10 leapfrog steps of size
+0.005; FP32 state, FP64 accept ratio.  One "step" = one HMC iteration of all
+chains (10 leapfrog steps + Metropolis test each), i.e. one launch of the
+persistent HMC kernel.  Metric: chain-leapfrog-steps per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference-structured CPU restatement (one
+chain per inference, GEMV per leapfrog gradient, as edward/inferences/hmc.py
+runs it) on all host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_ROWS, N_FEAT, N_CHAINS, N_LEAP, STEP = 10_000, 50, 4096, 10, 0.005
+METRIC = "HMC leapfrog chain-steps/s (Bayesian logistic regression, batched chains)"
+UNIT = "chain-steps/s"
+CONFIG = {"workload": "hmc_logreg_N10000_D50_C4096_L10", "N": N_ROWS, "D": N_FEAT,
+          "chains": N_CHAINS, "leapfrog_steps": N_LEAP, "step_size": STEP,
+          "state_dtype": "fp32", "ratio_dtype": "fp64"}
+
+
+def make_data(seed=0):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((N_ROWS, N_FEAT)).astype(np.float32)
+    w = rng.standard_normal(N_FEAT)
+    b = rng.standard_normal()
+    p = 1.0 / (1.0 + np.exp(-(X.astype(np.float64) @ w + b)))
+    y = (rng.random(N_ROWS) < p).astype(np.float32)
+    z0 = rng.standard_normal((N_CHAINS, N_FEAT + 1)).astype(np.float32)
+    return X, y, z0
+
+
+# ------------------------------------------------------------------ CPU baseline
+
+def _cpu_worker(args):
+    chains, n_iter, seed = args
+    import numpy as np
+    from oracle.cpu_baseline import hmc_logreg_chain
+    X, y, z0 = make_data()
+    P = N_FEAT + 1
+    t0 = time.perf_counter()
+    for c in chains:
+        hmc_logreg_chain(X, y, z0[c], n_iter, STEP, N_LEAP, seed, c,
+                         np.zeros(P, np.float32), np.ones(P, np.float32))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s=10.0, procs=None):
+    """Reference-structured CPU HMC on all host cores (one process per core,
+    chains split across processes); returns a cpu_baseline dict."""
+    import multiprocessing as mp
+    ncores = len(os.sched_getaffinity(0))
+    procs = procs or ncores
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    ctx = mp.get_context("spawn")
+    # calibrate: one chain, 2 iterations
+    t = _cpu_worker(([0], 2, 1))
+    per_chain_iter = max(t / 2, 1e-4)
+    n_iter = 2
+    chains_per_proc = max(1, int(budget_s / (per_chain_iter * n_iter)))
+    chains_per_proc = min(chains_per_proc, N_CHAINS // procs if N_CHAINS >= procs else 1)
+    work = [(list(range(p * chains_per_proc, (p + 1) * chains_per_proc)), n_iter, 1)
+            for p in range(procs)]
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        pool.map(_cpu_worker, work)
+        wall = time.perf_counter() - t0
+    total = procs * chains_per_proc * n_iter * N_LEAP
+    return {"value": total / wall, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{procs * chains_per_proc} chains x {n_iter} HMC iterations x {N_LEAP} "
+                      f"leapfrog steps, one chain at a time per process (GEMV per gradient, "
+                      f"NumPy FP32, BLAS 1 thread/process), {wall:.1f} s wall"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cb = None
+    steps = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(budget_s=max(2.0, 20.0 / max(1, args.steps + args.warmup)))
+        if i >= args.warmup:
+            steps.append(r)
+        cb = r
+    val = statistics.median(s["value"] for s in steps)
+    cb = dict(cb)
+    cb["value"] = val
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * N_CHAINS * N_LEAP / val, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(CONFIG, l2_flush="n/a (CPU)"), "impl": "reference",
+            "cpu_baseline": cb,
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        else:
+            self.out = ""
+
+    def summary(self):
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxes.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxes),
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    # CPU baseline first (spawned pool before heavy GPU work), rank 0 at N=1 only
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(budget_s=args.cpu_budget)
+
+    import edward_gb300 as ed
+    from edward_gb300 import _lib
+    from edward_gb300.models import Bernoulli, Empirical, Normal
+
+    X, y, z0 = make_data()
+    T = args.warmup + args.steps
+    w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
+    b = Normal(loc=0.0, scale=1.0)
+    yrv = Bernoulli(logits=ed.dot(X, w) + b)
+    qw_init = np.zeros((T, N_CHAINS, N_FEAT), np.float32)
+    qb_init = np.zeros((T, N_CHAINS), np.float32)
+    qw_init[0] = z0[:, :N_FEAT]
+    qb_init[0] = z0[:, N_FEAT]
+    qw = Empirical(ed.Variable(qw_init, trainable=False), n_chains=N_CHAINS)
+    qb = Empirical(ed.Variable(qb_init, trainable=False), n_chains=N_CHAINS)
+    inf = ed.HMC({w: qw, b: qb}, data={yrv: y}, n_chains=N_CHAINS)
+    inf.initialize(step_size=STEP, n_steps=N_LEAP, n_print=0, chains_per_block=args.ct)
+    ct = inf._cfg.chains_per_block
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        inf.run_iterations(1)
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))               # L2 flush (256 MB write), outside the events
+            ev[i][0].record(stream)
+            inf.run_iterations(1)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if world > 1:
+        dist.barrier()
+    per_step = [a.elapsed_time(bb) for a, bb in ev]
+    t_ms = sum(per_step)
+    if world > 1:
+        tt = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    units = N_CHAINS * N_LEAP * args.steps
+    value = world * units / (t_ms / 1e3)
+
+    # accept-rate sanity (posterior moves, chains not stuck)
+    acc = float(inf._n_accept.sum().item()) / (N_CHAINS * T)
+
+    # end-to-end through the C ABI with host buffers (copies inside the timed region)
+    e2e = run_e2e(args, inf, X, y, z0, dev)
+
+    # roofline of the dominant kernel (the persistent HMC kernel is the only launch per step)
+    P = N_FEAT + 1
+    flops_per_launch = 4.0 * N_ROWS * P * N_CHAINS * N_LEAP
+    avg_launch_ms = statistics.mean(per_step)
+    achieved = flops_per_launch / (avg_launch_ms / 1e3) / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        bf16 = float(peaks["bf16_tflops"])
+        src = "MEASURED_PEAKS.json bf16_tflops"
+    except (OSError, KeyError, ValueError):
+        bf16 = 1900.0
+        src = "fallback 1.9 PFLOP/s bf16"
+    peak = bf16 / 2.0 / 3.0
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": read_traffic(),
+            "kernel": f"hmc_glm_kernel<{ct}>",
+            "peak_source": f"{src} {bf16:g} / 2 (TF32 rate) / 3 (3xTF32 passes), of measured",
+            "algorithmic_flops_per_launch": flops_per_launch}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": dict(CONFIG, parallelism=f"replicas{world}",
+                               l2_flush="256 MB write before each step, outside the timed events",
+                               chains_per_block=ct, accept_rate=round(acc, 4)),
+                "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
+                "cpu_baseline": cb, "clocks": clk.summary(),
+                "wall_s_timed_region": wall}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, inf, X, y, z0, dev):
+    """Same metric through edg_hmc_glm_run with host buffers: every step copies
+    X, y and the chain state (z, cached gradient and log joint) from pinned
+    host memory, runs one iteration, and copies the state and the kept
+    sample back."""
+    import ctypes
+    import torch
+    from edward_gb300 import _lib
+    P = N_FEAT + 1
+    h_X = torch.as_tensor(X).pin_memory()
+    h_y = torch.as_tensor(y).pin_memory()
+    h_z = torch.as_tensor(z0).pin_memory()
+    h_g = torch.zeros(N_CHAINS, P).pin_memory()
+    h_lj = torch.zeros(N_CHAINS, dtype=torch.float64).pin_memory()
+    h_out = torch.zeros(N_CHAINS, P).pin_memory()
+    d_X = torch.empty_like(h_X, device=dev)
+    d_y = torch.empty_like(h_y, device=dev)
+    d_z = torch.empty_like(h_z, device=dev)
+    d_g = torch.empty_like(h_g, device=dev)
+    d_lj = torch.empty_like(h_lj, device=dev)
+    d_s = torch.zeros(1, N_CHAINS, P, device=dev)
+    st = _lib.new_state(dev)
+    glm = _lib.EdgGLM()
+    glm.X, glm.y, glm.N, glm.D, glm.bias, glm.lik, glm.lik_scale = (
+        d_X.data_ptr(), d_y.data_ptr(), N_ROWS, N_FEAT, 1, 0, 1.0)
+    glm.prior_loc = inf._glm.prior_loc.data_ptr()
+    glm.prior_scale = inf._glm.prior_scale.data_ptr()
+    cfg = inf._cfg
+    stream = torch.cuda.current_stream()
+    sp = _lib.stream_ptr(stream)
+    state0 = _lib.new_state(dev)
+
+    def step(cache_valid):
+        d_X.copy_(h_X, non_blocking=True)
+        d_y.copy_(h_y, non_blocking=True)
+        d_z.copy_(h_z, non_blocking=True)
+        d_g.copy_(h_g, non_blocking=True)
+        d_lj.copy_(h_lj, non_blocking=True)
+        st.copy_(state0)
+        _lib.call("edg_hmc_glm_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
+                  _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid, None, _lib.ptr(st),
+                  _lib.ptr(d_s), 1, None, None, None, None, sp)
+        h_z.copy_(d_z, non_blocking=True)
+        h_g.copy_(d_g, non_blocking=True)
+        h_lj.copy_(d_lj, non_blocking=True)
+        h_out.copy_(d_s[0], non_blocking=True)
+        stream.synchronize()
+
+    step(0)  # builds the gradient cache for the host-held state
+    for _ in range(max(0, args.warmup - 1)):
+        step(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(1)
+    dt = time.perf_counter() - t0
+    h2d = h_X.numel() * 4 + h_y.numel() * 4 + h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8
+    d2h = h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8 + h_out.numel() * 4
+    return {"value": N_CHAINS * N_LEAP * args.steps / dt, "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "path": "edg_hmc_glm_run (C ABI) with pinned host buffers, wall clock"}
+
+
+def read_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (a line 'dram_bytes_per_launch: <int>'), else None."""
+    p = os.path.join(ROOT, "profiles", "hmc_glm_kernel_logreg_C4096.txt")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return int(float(line.split(":", 1)[1]))
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ct", type=int, default=0, help="chains per block (0 = autotune)")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

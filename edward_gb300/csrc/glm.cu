@@ -1,0 +1,1063 @@
+// GLM hot path on SIMT FP32: batched log joint + adjoint, the fused KLqp
+// step and the persistent multi-chain HMC kernel.
+//
+// Shared building block: glm_grad_eval<CT>() runs over a row range of X for
+// CT parameter vectors held in shared memory (Monte Carlo samples or HMC
+// chains).  Per row tile it does
+//   phase A  eta[r][c]  = X[r,:] . z_c            (2 rows x 4 vectors per thread)
+//   epilogue resid[r][c] = d log p(y_r | eta) / d eta, log-lik terms (Kahan)
+//   phase B  G[c][d]   += sum_r resid[r][c] X[r][d]  (4x4 register blocks)
+// with X tiles streamed global -> shared by cp.async, double buffered.
+// One pass over X yields the log-likelihood and its gradient for every
+// vector, so X is read once per evaluation instead of 2S times
+// (klqp.py:725-747 builds S separate GEMV graphs).
+#include <cstdio>
+#include <algorithm>
+
+#include "edg_common.cuh"
+
+namespace edg {
+
+constexpr int kThreads = 256;
+
+template <int CT>
+struct Tile {
+  static_assert(CT == 8 || CT == 16 || CT == 32, "chains per block must be 8, 16 or 32");
+  static constexpr int RT = 2048 / CT;  // rows per tile: RT * CT = 8 outputs per thread
+  static constexpr int CQ = CT / 4;     // chain quads
+};
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Shared-memory views used by glm_grad_eval.
+struct GradSmem {
+  float* Xs;      // [2][RT][PP]  X tiles (bias column = 1, padding = 0)
+  float* ys;      // [2][RT]
+  float* Rs;      // [RT][CT]     residuals of the current tile
+  float* Zt;      // [PP][CT]     parameter vectors, transposed
+  float* G;       // [CT][PP]     OUT: likelihood gradient (scaled)
+  float* Gpart;   // [4096]       row-group partials of G
+  double* llred;  // [RT/2][CT]   per-thread log-lik partials
+  double* ll;     // [CT]         OUT: log-likelihood (scaled)
+};
+
+template <int CT>
+__host__ __device__ constexpr size_t grad_smem_floats(int PP) {
+  return (size_t)2 * Tile<CT>::RT * PP + 2 * Tile<CT>::RT + (size_t)Tile<CT>::RT * CT +
+         (size_t)PP * CT + (size_t)CT * PP + 4096;
+}
+template <int CT>
+__host__ __device__ constexpr size_t grad_smem_doubles() {
+  return (size_t)(Tile<CT>::RT / 2) * CT + CT;
+}
+
+// Carves GradSmem from `base` (16-byte aligned); returns the first free byte.
+template <int CT>
+__device__ unsigned char* carve_grad(unsigned char* base, int PP, GradSmem& S) {
+  double* d = reinterpret_cast<double*>(base);
+  S.llred = d;
+  d += (Tile<CT>::RT / 2) * CT;
+  S.ll = d;
+  d += CT;
+  float* f = reinterpret_cast<float*>(d);
+  S.Xs = f;
+  f += 2 * Tile<CT>::RT * PP;
+  S.Rs = f;
+  f += Tile<CT>::RT * CT;
+  S.Zt = f;
+  f += PP * CT;
+  S.G = f;
+  f += CT * PP;
+  S.Gpart = f;
+  f += 4096;
+  S.ys = f;
+  f += 2 * Tile<CT>::RT;
+  return reinterpret_cast<unsigned char*>(f);
+}
+
+// Constant columns of both X buffers: bias column = 1 (if any), padding = 0.
+template <int CT>
+__device__ void init_x_pad(const GLMDev& m, const GradSmem& S) {
+  constexpr int RT = Tile<CT>::RT;
+  const int extra = m.PP - m.D;
+  for (int i = threadIdx.x; i < 2 * RT * extra; i += kThreads) {
+    const int row = i / extra, col = m.D + i % extra;
+    S.Xs[row * m.PP + col] = (m.bias && col == m.D) ? 1.0f : 0.0f;
+  }
+}
+
+template <int CT>
+__device__ __forceinline__ void issue_tile(const GLMDev& m, float* Xdst, float* ydst, int row0,
+                                           int row_end) {
+  constexpr int RT = Tile<CT>::RT;
+  const int nrows = min(RT, row_end - row0);
+  const int D = m.D, PP = m.PP;
+  const int total = RT * D;
+  const float* Xsrc = m.X + (size_t)row0 * D;
+  const int valid = nrows * D;
+  // incremental (r, d) walk: e = tid + k * kThreads
+  int r = threadIdx.x / D, d = threadIdx.x - (threadIdx.x / D) * D;
+  const int step_r = kThreads / D, step_d = kThreads - (kThreads / D) * D;
+  for (int e = threadIdx.x; e < total; e += kThreads) {
+    const bool ok = e < valid;
+    cp_async4(Xdst + r * PP + d, ok ? (const void*)(Xsrc + e) : (const void*)m.X, ok ? 4 : 0);
+    r += step_r;
+    d += step_d;
+    if (d >= D) {
+      d -= D;
+      ++r;
+    }
+  }
+  for (int i = threadIdx.x; i < RT; i += kThreads) {
+    const bool ok = i < nrows;
+    cp_async4(ydst + i, ok ? (const void*)(m.y + row0 + i) : (const void*)m.y, ok ? 4 : 0);
+  }
+}
+
+// Log-likelihood term and residual d/d eta for one (row, vector).
+__device__ __forceinline__ void lik_term(const GLMDev& m, float y, float eta, float& ll,
+                                         float& resid) {
+  if (m.lik == EDG_LIK_BERNOULLI) {
+    const float e = expf(-fabsf(eta));
+    const float s = 1.0f / (1.0f + e);
+    const float sig = eta >= 0.0f ? s : e * s;
+    ll = -(fmaxf(eta, 0.0f) - eta * y + log1pf(e));
+    resid = y - sig;
+  } else {
+    const float diff = y - eta;
+    ll = -0.5f * diff * diff * m.inv_lik_var - m.lik_norm;
+    resid = diff * m.inv_lik_var;
+  }
+}
+
+// Log-likelihood (and gradient) of CT vectors S.Zt over rows [row_begin, row_end).
+// All threads of the block must call it.  On return S.G / S.ll hold the
+// results (multiplied by dscale) and a __syncthreads() has been done.
+template <int CT>
+__device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const GradSmem& S,
+                              bool need_ll, bool need_grad, float dscale) {
+  constexpr int RT = Tile<CT>::RT, CQ = Tile<CT>::CQ;
+  const int tid = threadIdx.x;
+  const int PP = m.PP, P4 = PP / 4;
+  const int cq = tid % CQ, rp = tid / CQ;  // phase A: rows 2rp, 2rp+1; chains 4cq..4cq+3
+  // phase B: units of (chain quad, feature quad)
+  const int U = CQ * P4;
+  int H, nu, unit0, unit1, hgrp;
+  if (U <= kThreads) {
+    H = kThreads / U;
+    hgrp = tid / U;
+    unit0 = tid % U;
+    unit1 = -1;
+    nu = tid < U * H ? 1 : 0;
+  } else {
+    H = 1;
+    hgrp = 0;
+    unit0 = tid;
+    unit1 = tid + kThreads;
+    nu = (unit0 < U) + (unit1 < U);
+  }
+  float accB[2][16];
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int i = 0; i < 16; ++i) accB[k][i] = 0.0f;
+  Kahan kll[4];
+
+  const int ntiles = (row_end - row_begin + RT - 1) / RT;
+  if (ntiles > 0) issue_tile<CT>(m, S.Xs, S.ys, row_begin, row_end);
+  cp_async_commit();
+  for (int it = 0; it < ntiles; ++it) {
+    const int buf = it & 1;
+    if (it + 1 < ntiles)
+      issue_tile<CT>(m, S.Xs + (buf ^ 1) * RT * PP, S.ys + (buf ^ 1) * RT, row_begin + (it + 1) * RT,
+                     row_end);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const float* Xb = S.Xs + buf * RT * PP;
+    const float* yb = S.ys + buf * RT;
+    const int r0 = row_begin + it * RT;
+
+    // ---- phase A: eta = X z
+    float acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+    const float4* xr0 = reinterpret_cast<const float4*>(Xb + (2 * rp) * PP);
+    const float4* xr1 = reinterpret_cast<const float4*>(Xb + (2 * rp + 1) * PP);
+    const float4* zt = reinterpret_cast<const float4*>(S.Zt);
+    for (int dq = 0; dq < P4; ++dq) {
+      const float4 x0 = xr0[dq], x1 = xr1[dq];
+      const float4 z0 = zt[(4 * dq + 0) * CQ + cq];
+      const float4 z1 = zt[(4 * dq + 1) * CQ + cq];
+      const float4 z2 = zt[(4 * dq + 2) * CQ + cq];
+      const float4 z3 = zt[(4 * dq + 3) * CQ + cq];
+#define EDG_ROWFMA(A, XV)                                                  \
+  A[0] = fmaf(XV.x, z0.x, A[0]); A[1] = fmaf(XV.x, z0.y, A[1]);            \
+  A[2] = fmaf(XV.x, z0.z, A[2]); A[3] = fmaf(XV.x, z0.w, A[3]);            \
+  A[0] = fmaf(XV.y, z1.x, A[0]); A[1] = fmaf(XV.y, z1.y, A[1]);            \
+  A[2] = fmaf(XV.y, z1.z, A[2]); A[3] = fmaf(XV.y, z1.w, A[3]);            \
+  A[0] = fmaf(XV.z, z2.x, A[0]); A[1] = fmaf(XV.z, z2.y, A[1]);            \
+  A[2] = fmaf(XV.z, z2.z, A[2]); A[3] = fmaf(XV.z, z2.w, A[3]);            \
+  A[0] = fmaf(XV.w, z3.x, A[0]); A[1] = fmaf(XV.w, z3.y, A[1]);            \
+  A[2] = fmaf(XV.w, z3.z, A[2]); A[3] = fmaf(XV.w, z3.w, A[3]);
+      EDG_ROWFMA(acc[0], x0)
+      EDG_ROWFMA(acc[1], x1)
+#undef EDG_ROWFMA
+    }
+    // ---- epilogue: residuals and log-lik terms
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int lr = 2 * rp + i;
+      const bool valid = r0 + lr < row_end;
+      const float yv = yb[lr];
+      float res[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float ll, rs;
+        lik_term(m, yv, acc[i][j], ll, rs);
+        res[j] = valid ? rs * dscale : 0.0f;
+        if (need_ll && valid) kll[j].add(ll);
+      }
+      reinterpret_cast<float4*>(S.Rs + lr * CT)[cq] = make_float4(res[0], res[1], res[2], res[3]);
+    }
+    __syncthreads();
+    // ---- phase B: G += resid^T X
+    if (need_grad) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int u = k == 0 ? unit0 : unit1;
+        if (k >= nu) break;
+        const int cqb = u % CQ, dqb = u / CQ;
+        float* a = accB[k];
+        for (int r = hgrp; r < RT; r += H) {
+          const float4 rr = reinterpret_cast<const float4*>(S.Rs + r * CT)[cqb];
+          const float4 xx = reinterpret_cast<const float4*>(Xb + r * PP)[dqb];
+          const float rv[4] = {rr.x, rr.y, rr.z, rr.w};
+          const float xv[4] = {xx.x, xx.y, xx.z, xx.w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int dd = 0; dd < 4; ++dd) a[c * 4 + dd] = fmaf(rv[c], xv[dd], a[c * 4 + dd]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+
+  // ---- combine row groups of G
+  if (need_grad) {
+    float* dst = (U <= kThreads) ? S.Gpart + hgrp * CT * PP : S.G;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (k >= nu) break;
+      const int u = k == 0 ? unit0 : unit1;
+      const int cqb = u % CQ, dqb = u / CQ;
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int dd = 0; dd < 4; ++dd)
+          dst[(4 * cqb + c) * PP + 4 * dqb + dd] = accB[k][c * 4 + dd];
+    }
+    __syncthreads();
+    if (U <= kThreads) {
+      for (int idx = tid; idx < CT * PP; idx += kThreads) {
+        float s = 0.0f;
+        for (int h = 0; h < H; ++h) s += S.Gpart[h * CT * PP + idx];
+        S.G[idx] = s;
+      }
+    }
+  }
+  // ---- FP64 reduction of the log-lik partials
+  if (need_ll) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) S.llred[rp * CT + 4 * cq + j] = kll[j].value();
+    __syncthreads();
+    if (tid < CT) {
+      double s = 0.0;
+      for (int q = 0; q < RT / 2; ++q) s += S.llred[q * CT + tid];
+      S.ll[tid] = s * (double)dscale;
+    }
+  }
+  __syncthreads();
+}
+
+// Zt[d][c] = z[c][d] for a [CT][PP] block.
+template <int CT>
+__device__ __forceinline__ void transpose_into(const float* Z, float* Zt, int PP) {
+  for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+    const int c = idx / PP, d = idx - c * PP;
+    Zt[d * CT + c] = Z[idx];
+  }
+}
+
+// ============================================================ batched grad
+template <int CT>
+__global__ void __launch_bounds__(kThreads) glm_partial_kernel(GLMDev m, const float* __restrict__ Z,
+                                                               int B, int chunk, float dscale,
+                                                               float* __restrict__ ws_g,
+                                                               double* __restrict__ ws_ll, int Bpad,
+                                                               int need_grad) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  GradSmem S;
+  carve_grad<CT>(smem, m.PP, S);
+  const int chunk_id = blockIdx.x, tile = blockIdx.y;
+  const int b0 = tile * CT;
+  init_x_pad<CT>(m, S);
+  for (int idx = threadIdx.x; idx < CT * m.PP; idx += kThreads) {
+    const int c = idx / m.PP, d = idx - c * m.PP;
+    const int b = b0 + c;
+    S.Zt[d * CT + c] = (b < B && d < m.P) ? Z[(size_t)b * m.P + d] : 0.0f;
+  }
+  __syncthreads();
+  const int rb = chunk_id * chunk, re = min(m.N, rb + chunk);
+  glm_grad_eval<CT>(m, rb, re, S, true, need_grad != 0, dscale);
+  for (int idx = threadIdx.x; idx < CT * m.PP; idx += kThreads) {
+    const int c = idx / m.PP;
+    if (b0 + c < B && need_grad)
+      ws_g[((size_t)chunk_id * Bpad + b0) * m.PP + idx] = S.G[idx];
+  }
+  if (threadIdx.x < CT && b0 + threadIdx.x < B)
+    ws_ll[(size_t)chunk_id * Bpad + b0 + threadIdx.x] = S.ll[threadIdx.x];
+}
+
+__global__ void glm_reduce_kernel(GLMDev m, const float* __restrict__ Z, int B, int nchunks,
+                                  const float* __restrict__ ws_g, const double* __restrict__ ws_ll,
+                                  int Bpad, int include_prior, double* lp_out, float* grad_out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int P = m.P, PP = m.PP;
+  if (grad_out && i < (int64_t)B * P) {
+    const int b = (int)(i / P), d = (int)(i % P);
+    float s = 0.0f;
+    for (int k = 0; k < nchunks; ++k) s += ws_g[((size_t)k * Bpad + b) * PP + d];
+    if (include_prior) {
+      const float sc = m.prior_scale[d];
+      s += -(Z[i] - m.prior_loc[d]) / (sc * sc);
+    }
+    grad_out[i] = s;
+  }
+  if (lp_out && i < B) {
+    double s = 0.0;
+    for (int k = 0; k < nchunks; ++k) s += ws_ll[(size_t)k * Bpad + i];
+    if (include_prior) {
+      for (int d = 0; d < P; ++d) {
+        const float sc = m.prior_scale[d];
+        const float zz = (Z[(size_t)i * P + d] - m.prior_loc[d]) / sc;
+        s += (double)(-0.5f * zz * zz - logf(sc)) - kHalfLog2Pi;
+      }
+    }
+    lp_out[i] = s;
+  }
+}
+
+// ============================================================ KLqp step
+struct KlqpArgs {
+  int method, S, Spad, nblocks, chunk;
+  float dscale;
+  const float* kl_scaling;
+  const float* latent_scale;
+  uint64_t seed;
+  edg_opt_t opt;
+  float* mu;
+  float* rho;
+  float* slots;
+  edg_state_t* state;
+  const float* eps_ovr;
+  float* grad_out;
+  int apply;
+  float* ws_g;     // [nblocks][Spad][PP]
+  double* ws_ll;   // [nblocks][Spad]
+};
+
+__device__ __forceinline__ float eps_value(const KlqpArgs& a, uint32_t iter, int s, int d, int P) {
+  return a.eps_ovr ? a.eps_ovr[(size_t)s * P + d] : philox_normal(a.seed, 0u, iter, (uint32_t)s, (uint32_t)d);
+}
+
+__device__ float opt_lr(const edg_opt_t& o, int64_t step) {
+  if (o.decay_steps <= 0) return o.lr0;
+  float p = (float)step / (float)o.decay_steps;
+  if (o.staircase) p = floorf(p);
+  return o.lr0 * powf(o.decay_rate, p);
+}
+
+// One optimizer apply for parameter index i of n (slots: two arrays of n).
+__device__ float opt_apply(const edg_opt_t& o, float p, float g, float* s0, float* s1, float lr,
+                           float b1p, float b2p) {
+  switch (o.optimizer) {
+    case EDG_OPT_ADAM: {
+      const float lr_t = lr * sqrtf(1.0f - b2p) / (1.0f - b1p);
+      const float m = o.beta1 * *s0 + (1.0f - o.beta1) * g;
+      const float v = o.beta2 * *s1 + (1.0f - o.beta2) * g * g;
+      *s0 = m;
+      *s1 = v;
+      return p - lr_t * m / (sqrtf(v) + o.epsilon);
+    }
+    case EDG_OPT_SGD:
+      return p - lr * g;
+    case EDG_OPT_MOMENTUM: {
+      const float acc = o.momentum * *s0 + g;
+      *s0 = acc;
+      return p - lr * acc;
+    }
+    case EDG_OPT_ADAGRAD: {
+      const float acc = *s0 + g * g;
+      *s0 = acc;
+      return p - lr * g * rsqrtf(acc);
+    }
+    case EDG_OPT_RMSPROP: {
+      const float ms = o.rho * *s0 + (1.0f - o.rho) * g * g;
+      const float mom = o.momentum * *s1 + lr * g / sqrtf(ms + o.epsilon);
+      *s0 = ms;
+      *s1 = mom;
+      return p - mom;
+    }
+    default: {  // EDG_OPT_ADADELTA
+      const float acc = o.rho * *s0 + (1.0f - o.rho) * g * g;
+      const float upd = sqrtf(*s1 + o.epsilon) / sqrtf(acc + o.epsilon) * g;
+      *s0 = acc;
+      *s1 = o.rho * *s1 + (1.0f - o.rho) * upd * upd;
+      return p - lr * upd;
+    }
+  }
+}
+
+template <int CT>
+__global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  GradSmem S;
+  unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
+  float* sig = reinterpret_cast<float*>(rest);  // [PP]
+  __shared__ bool s_last;
+  const int P = m.P, PP = m.PP;
+  const int64_t t = *(volatile int64_t*)&a.state->t;
+  const uint32_t iter = (uint32_t)t;
+  for (int d = threadIdx.x; d < PP; d += kThreads) sig[d] = d < P ? softplusf(a.rho[d]) : 0.0f;
+  init_x_pad<CT>(m, S);
+  __syncthreads();
+  const int rb = blockIdx.x * a.chunk, re = min(m.N, rb + a.chunk);
+  const bool need_grad = a.method != EDG_KLQP_SCORE;
+  for (int s0 = 0; s0 < a.S; s0 += CT) {
+    for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+      const int c = idx / PP, d = idx - c * PP;
+      const int s = s0 + c;
+      float zv = 0.0f;
+      if (s < a.S && d < P) zv = a.mu[d] + sig[d] * eps_value(a, iter, s, d, P);
+      S.Zt[d * CT + c] = zv;
+    }
+    __syncthreads();
+    glm_grad_eval<CT>(m, rb, re, S, true, need_grad, a.dscale);
+    for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+      const int c = idx / PP;
+      if (s0 + c < a.S && need_grad)
+        a.ws_g[((size_t)blockIdx.x * a.Spad + s0) * PP + idx] = S.G[idx];
+    }
+    if (threadIdx.x < CT && s0 + threadIdx.x < a.S)
+      a.ws_ll[(size_t)blockIdx.x * a.Spad + s0 + threadIdx.x] = S.ll[threadIdx.x];
+    __syncthreads();
+  }
+  // ---- last block finishes the step
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(&a.state->done, 1u);
+    s_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // per-sample totals (FP64 log-lik; FP32 gradient, summed in block order)
+  double* llS = S.llred;                 // [S]  (reuse; S <= RT/2*CT)
+  float* gS = S.Xs;                      // [S][PP] gradient per sample
+  for (int s = threadIdx.x; s < a.S; s += kThreads) {
+    double v = 0.0;
+    for (int b = 0; b < a.nblocks; ++b) v += ((volatile double*)a.ws_ll)[(size_t)b * a.Spad + s];
+    llS[s] = v;
+  }
+  if (need_grad) {
+    for (int idx = threadIdx.x; idx < a.S * PP; idx += kThreads) {
+      float v = 0.0f;
+      for (int b = 0; b < a.nblocks; ++b)
+        v += ((volatile float*)a.ws_g)[(size_t)b * a.Spad * PP + idx];
+      gS[idx] = v;
+    }
+  }
+  __syncthreads();
+  // score / reparam need per-sample log p(z_s) - log q(z_s)
+  double* lsig = llS + a.S;  // [S] learning signal / prior-q terms
+  if (a.method != EDG_KLQP_REPARAM_KL) {
+    for (int s = threadIdx.x; s < a.S; s += kThreads) {
+      double acc = 0.0;
+      for (int d = 0; d < P; ++d) {
+        const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
+        const float e = eps_value(a, iter, s, d, P);
+        const float zv = a.mu[d] + sig[d] * e;
+        const float ps = m.prior_scale[d];
+        const float zp = (zv - m.prior_loc[d]) / ps;
+        const float zq = (zv - a.mu[d]) / sig[d];
+        const float lp = -0.5f * zp * zp - logf(ps);
+        const float lq = -0.5f * zq * zq - logf(sig[d]);
+        acc += (double)(lsc * (lp - lq));  // the 0.5 log 2pi terms cancel
+      }
+      lsig[s] = acc;
+    }
+    __syncthreads();
+  }
+  // ---- loss
+  if (threadIdx.x == 0) {
+    double mean_ll = 0.0;
+    for (int s = 0; s < a.S; ++s) mean_ll += llS[s];
+    mean_ll /= a.S;
+    double loss;
+    if (a.method == EDG_KLQP_REPARAM_KL) {
+      double kl = 0.0;
+      for (int d = 0; d < P; ++d) {
+        const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
+        const double sp = m.prior_scale[d], sq = sig[d];
+        const double dm = ((double)a.mu[d] - m.prior_loc[d]) / sp;
+        const double ratio = (sq / sp) * (sq / sp);
+        kl += ks * (0.5 * dm * dm + 0.5 * (ratio - 1.0 - log(ratio)));
+      }
+      loss = -(mean_ll - kl);
+      a.state->aux[0] = mean_ll;
+      a.state->aux[1] = kl;
+    } else {
+      double ms = 0.0;
+      for (int s = 0; s < a.S; ++s) ms += lsig[s];
+      ms /= a.S;
+      loss = -(mean_ll + ms);
+      a.state->aux[0] = mean_ll;
+      a.state->aux[1] = ms;
+    }
+    a.state->loss = loss;
+    if (!isfinite(loss)) atomicAdd(&a.state->nonfinite, 1u);
+  }
+  __syncthreads();  // the loss reads mu/rho before the apply below overwrites them
+  // ---- gradients w.r.t. (mu, rho) and the optimizer apply
+  const float lr = opt_lr(a.opt, a.state->global_step);
+  const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
+  const float invS = 1.0f / (float)a.S;
+  for (int d = threadIdx.x; d < P; d += kThreads) {
+    const float mu = a.mu[d], rho = a.rho[d], sg = sig[d];
+    const float ps = m.prior_scale[d], pl = m.prior_loc[d];
+    const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
+    float gmu = 0.0f, gsig = 0.0f;
+    if (a.method == EDG_KLQP_REPARAM_KL) {
+      float sg_mu = 0.0f, sg_sig = 0.0f;
+      for (int s = 0; s < a.S; ++s) {
+        const float e = eps_value(a, iter, s, d, P);
+        const float g = gS[s * PP + d];
+        sg_mu += g;
+        sg_sig += g * e;
+      }
+      const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
+      gmu = -sg_mu * invS + ks * (mu - pl) / (ps * ps);
+      gsig = -sg_sig * invS + ks * (sg / (ps * ps) - 1.0f / sg);
+    } else if (a.method == EDG_KLQP_REPARAM) {
+      float acc_mu = 0.0f, acc_sig = 0.0f;
+      for (int s = 0; s < a.S; ++s) {
+        const float e = eps_value(a, iter, s, d, P);
+        const float zv = mu + sg * e;
+        const float dfdz = gS[s * PP + d] - lsc * (zv - pl) / (ps * ps) + lsc * (zv - mu) / (sg * sg);
+        const float dlq_dmu = (zv - mu) / (sg * sg);
+        const float dlq_dsig = -1.0f / sg + (zv - mu) * (zv - mu) / (sg * sg * sg);
+        acc_mu += dfdz - lsc * dlq_dmu;
+        acc_sig += dfdz * e - lsc * dlq_dsig;
+      }
+      gmu = -acc_mu * invS;
+      gsig = -acc_sig * invS;
+    } else {
+      float acc_mu = 0.0f, acc_sig = 0.0f;
+      for (int s = 0; s < a.S; ++s) {
+        const float e = eps_value(a, iter, s, d, P);
+        const float zv = mu + sg * e;
+        const float w = (float)(llS[s] + lsig[s]);
+        acc_mu += lsc * (zv - mu) / (sg * sg) * w;
+        acc_sig += lsc * (-1.0f / sg + (zv - mu) * (zv - mu) / (sg * sg * sg)) * w;
+      }
+      gmu = -acc_mu * invS;
+      gsig = -acc_sig * invS;
+    }
+    const float grho = gsig * sigmoidf(rho);
+    if (!isfinite(gmu) || !isfinite(grho)) atomicAdd(&a.state->nonfinite, 1u);
+    if (a.grad_out) {
+      a.grad_out[d] = gmu;
+      a.grad_out[P + d] = grho;
+    }
+    if (a.apply) {
+      const int n = 2 * P;
+      a.mu[d] = opt_apply(a.opt, mu, gmu, a.slots + d, a.slots + n + d, lr, b1p, b2p);
+      a.rho[d] = opt_apply(a.opt, rho, grho, a.slots + P + d, a.slots + n + P + d, lr, b1p, b2p);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (a.apply) {
+      a.state->t = t + 1;
+      a.state->global_step += 1;
+      a.state->beta1_power = b1p * a.opt.beta1;
+      a.state->beta2_power = b2p * a.opt.beta2;
+    }
+    a.state->done = 0;
+    __threadfence();
+  }
+}
+
+// ============================================================ HMC
+struct HmcArgs {
+  int C, n_iter, n_steps, cache_valid;
+  float step_size;
+  uint64_t seed;
+  float* z;
+  float* grad;
+  double* lj;
+  int32_t* n_accept;
+  edg_state_t* state;
+  float* samples;
+  int64_t T_cap;
+  double* moments;
+  const float* r_ovr;
+  const double* u_ovr;
+  double* ratio_out;
+};
+
+// Adds the Normal prior to a likelihood gradient block and returns nothing;
+// G[c][d] += -(z - loc) / scale^2 for d < P.
+template <int CT>
+__device__ __forceinline__ void add_prior_grad(const GLMDev& m, const float* Z, float* G) {
+  for (int idx = threadIdx.x; idx < CT * m.PP; idx += kThreads) {
+    const int d = idx % m.PP;
+    if (d < m.P) {
+      const float sc = m.prior_scale[d];
+      G[idx] += -(Z[idx] - m.prior_loc[d]) / (sc * sc);
+    }
+  }
+}
+
+// FP64 prior log density of chain c (called by one thread per chain).
+__device__ __forceinline__ double prior_lp(const GLMDev& m, const float* zc) {
+  double s = 0.0;
+  for (int d = 0; d < m.P; ++d) {
+    const float sc = m.prior_scale[d];
+    const float zz = (zc[d] - m.prior_loc[d]) / sc;
+    s += (double)(-0.5f * zz * zz - logf(sc)) - kHalfLog2Pi;
+  }
+  return s;
+}
+
+template <int CT>
+__host__ __device__ constexpr size_t hmc_smem_bytes(int PP) {
+  return grad_smem_doubles<CT>() * 8 + grad_smem_floats<CT>(PP) * 4 +
+         (size_t)4 * CT * PP * 4 /* Z0 G0 Z R (G is S.G) */ + (size_t)3 * CT * 8 + CT * 4;
+}
+
+template <int CT>
+__global__ void __launch_bounds__(kThreads) hmc_glm_kernel(GLMDev m, HmcArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  GradSmem S;
+  unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
+  const int PP = m.PP, P = m.P;
+  float* Z0 = reinterpret_cast<float*>(rest);
+  float* G0 = Z0 + CT * PP;
+  float* Z = G0 + CT * PP;
+  float* R = Z + CT * PP;
+  double* lj0 = reinterpret_cast<double*>(R + CT * PP);
+  double* kin0 = lj0 + CT;
+  double* ljn = kin0 + CT;
+  int* acc = reinterpret_cast<int*>(ljn + CT);
+  float* G = S.G;
+  __shared__ bool s_last;
+
+  const int cbase = blockIdx.x * CT;
+  const int nc = min(CT, a.C - cbase);
+  const int64_t t0 = *(volatile int64_t*)&a.state->t;
+  const float eps = a.step_size, half = 0.5f * a.step_size;
+
+  init_x_pad<CT>(m, S);
+  for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+    const int c = idx / PP, d = idx - c * PP;
+    const bool ok = c < nc && d < P;
+    const size_t g = (size_t)(cbase + c) * P + d;
+    Z0[idx] = ok ? a.z[g] : 0.0f;
+    G0[idx] = (ok && a.cache_valid) ? a.grad[g] : 0.0f;
+  }
+  if (threadIdx.x < CT) lj0[threadIdx.x] = (a.cache_valid && threadIdx.x < nc) ? a.lj[cbase + threadIdx.x] : 0.0;
+  __syncthreads();
+  if (!a.cache_valid) {
+    transpose_into<CT>(Z0, S.Zt, PP);
+    __syncthreads();
+    glm_grad_eval<CT>(m, 0, m.N, S, true, true, 1.0f);
+    add_prior_grad<CT>(m, Z0, G);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) G0[idx] = G[idx];
+    if (threadIdx.x < CT) lj0[threadIdx.x] = S.ll[threadIdx.x] + prior_lp(m, Z0 + threadIdx.x * PP);
+    __syncthreads();
+  }
+
+  for (int it = 0; it < a.n_iter; ++it) {
+    const int64_t t = t0 + it;
+    const uint32_t iter = (uint32_t)t;
+    // momentum draw; working copies
+    for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+      const int c = idx / PP, d = idx - c * PP;
+      float r = 0.0f;
+      if (c < nc && d < P) {
+        r = a.r_ovr ? a.r_ovr[((size_t)it * a.C + cbase + c) * P + d]
+                    : philox_normal(a.seed, 1u, iter, (uint32_t)(cbase + c), (uint32_t)d);
+      }
+      R[idx] = r;
+      Z[idx] = Z0[idx];
+      G[idx] = G0[idx];
+    }
+    __syncthreads();
+    if (threadIdx.x < CT) {
+      double k = 0.0;
+      const float* rc = R + threadIdx.x * PP;
+      for (int d = 0; d < P; ++d) k += (double)rc[d] * (double)rc[d];
+      kin0[threadIdx.x] = k;
+    }
+    __syncthreads();
+    // leapfrog (hmc.py:195-210): r += h g; z += eps r; g = grad(z); r += h g
+    for (int l = 0; l < a.n_steps; ++l) {
+      for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+        const float r = R[idx] + half * G[idx];
+        const float zz = Z[idx] + eps * r;
+        R[idx] = r;
+        Z[idx] = zz;
+        const int c = idx / PP, d = idx - c * PP;
+        S.Zt[d * CT + c] = zz;
+      }
+      __syncthreads();
+      const bool last = (l == a.n_steps - 1);
+      glm_grad_eval<CT>(m, 0, m.N, S, last, true, 1.0f);
+      for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+        const int d = idx % PP;
+        float g = G[idx];
+        if (d < P) {
+          const float sc = m.prior_scale[d];
+          g += -(Z[idx] - m.prior_loc[d]) / (sc * sc);
+        }
+        G[idx] = g;
+        R[idx] += half * g;
+      }
+      __syncthreads();
+    }
+    // Metropolis test in FP64 (hmc.py:100-109)
+    if (threadIdx.x < CT) {
+      const int c = threadIdx.x;
+      int accept = 0;
+      if (c < nc) {
+        double lj_new;
+        if (a.n_steps > 0) {
+          lj_new = S.ll[c] + prior_lp(m, Z + c * PP);
+        } else {
+          lj_new = lj0[c];
+        }
+        double k = 0.0;
+        const float* rc = R + c * PP;
+        for (int d = 0; d < P; ++d) k += (double)rc[d] * (double)rc[d];
+        const double ratio = 0.5 * kin0[c] - 0.5 * k + lj_new - lj0[c];
+        const double u = a.u_ovr ? a.u_ovr[(size_t)it * a.C + cbase + c]
+                                 : u01d(philox_at(a.seed, 2u, iter, (uint32_t)(cbase + c), 0u).x);
+        accept = log(u) < ratio ? 1 : 0;
+        if (accept) lj0[c] = lj_new;
+        if (a.n_accept) a.n_accept[cbase + c] += accept;
+        if (a.ratio_out) a.ratio_out[(size_t)it * a.C + cbase + c] = ratio;
+      }
+      acc[c] = accept;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+      const int c = idx / PP, d = idx - c * PP;
+      if (acc[c]) {
+        Z0[idx] = Z[idx];
+        G0[idx] = G[idx];
+      }
+      if (c < nc && d < P) {
+        const float v = acc[c] ? Z[idx] : Z0[idx];
+        if (a.samples && t < a.T_cap) a.samples[((size_t)t * a.C + cbase + c) * P + d] = v;
+        if (a.moments) {
+          const size_t g = (size_t)(cbase + c) * P + d;
+          a.moments[g] += (double)v;
+          a.moments[(size_t)a.C * P + g] += (double)v * (double)v;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // write back state and cache
+  for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
+    const int c = idx / PP, d = idx - c * PP;
+    if (c < nc && d < P) {
+      const size_t g = (size_t)(cbase + c) * P + d;
+      a.z[g] = Z0[idx];
+      a.grad[g] = G0[idx];
+    }
+  }
+  if (threadIdx.x < nc) a.lj[cbase + threadIdx.x] = lj0[threadIdx.x];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(&a.state->done, 1u);
+    s_last = (prev == gridDim.x - 1);
+    if (s_last) {
+      a.state->t = t0 + a.n_iter;
+      a.state->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------------ host helpers
+static int max_smem_optin() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+static int sm_count() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v > 0 ? v : 1;
+}
+
+template <int CT>
+static size_t grad_smem_bytes(int PP) {
+  return grad_smem_doubles<CT>() * 8 + grad_smem_floats<CT>(PP) * 4;
+}
+
+static int pick_ct(int B) { return B <= 8 ? 8 : (B <= 16 ? 16 : 32); }
+
+struct GradPlan {
+  int CT, ntiles, nchunks, chunk, Bpad;
+  size_t ws_g_bytes, ws_ll_bytes;
+};
+
+static GradPlan plan_grad(const GLMDev& m, int B) {
+  GradPlan p;
+  p.CT = pick_ct(B);
+  p.ntiles = (B + p.CT - 1) / p.CT;
+  p.Bpad = p.ntiles * p.CT;
+  const int RT = 2048 / p.CT;
+  const int max_chunks = (m.N + RT - 1) / RT;
+  int want = std::max(1, (2 * sm_count()) / p.ntiles);
+  p.nchunks = std::min(max_chunks, want);
+  p.chunk = (m.N + p.nchunks - 1) / p.nchunks;
+  p.chunk = round_up(p.chunk, RT);
+  p.nchunks = (m.N + p.chunk - 1) / p.chunk;
+  p.ws_g_bytes = (size_t)p.nchunks * p.Bpad * m.PP * sizeof(float);
+  p.ws_ll_bytes = (size_t)p.nchunks * p.Bpad * sizeof(double);
+  return p;
+}
+
+template <int CT>
+static int launch_partial(const GLMDev& m, const float* Z, int B, const GradPlan& p, float dscale,
+                          float* wg, double* wl, int need_grad, cudaStream_t st) {
+  const size_t sm = grad_smem_bytes<CT>(m.PP);
+  EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED,
+              "P=%d needs %zu bytes of shared memory", m.P, sm);
+  cudaFuncSetAttribute(glm_partial_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid(p.nchunks, p.ntiles);
+  glm_partial_kernel<CT><<<grid, kThreads, sm, st>>>(m, Z, B, p.chunk, dscale, wg, wl, p.Bpad,
+                                                     need_grad);
+  return check_launch("glm_partial_kernel");
+}
+
+}  // namespace edg
+
+using namespace edg;
+
+extern "C" size_t edg_glm_logjoint_grad_workspace_bytes(const edg_glm_t* model, int32_t B) {
+  GLMDev m;
+  if (make_glm(model, &m) != EDG_OK || B <= 0) return 0;
+  const GradPlan p = plan_grad(m, B);
+  return round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+}
+
+extern "C" int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int32_t B,
+                                     int32_t include_prior, float data_scale, double* lp_out,
+                                     float* grad_out, void* workspace, size_t workspace_bytes,
+                                     void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(Z, EDG_E_NULL, "Z is NULL");
+  EDG_REQUIRE(B > 0, EDG_E_SHAPE, "B must be positive (got %d)", B);
+  if (!lp_out && !grad_out) return EDG_OK;
+  const GradPlan p = plan_grad(m, B);
+  const size_t need = round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+  EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
+              "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
+  float* wg = reinterpret_cast<float*>(workspace);
+  double* wl = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) +
+                                         round_up((int)p.ws_g_bytes, 256));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int ng = grad_out ? 1 : 0;
+  switch (p.CT) {
+    case 8: rc = launch_partial<8>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+    case 16: rc = launch_partial<16>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+    default: rc = launch_partial<32>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+  }
+  if (rc) return rc;
+  const int64_t n = std::max<int64_t>((int64_t)B * m.P, B);
+  glm_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      m, Z, B, p.nchunks, wg, wl, p.Bpad, include_prior, lp_out, grad_out);
+  return check_launch("glm_reduce_kernel");
+}
+
+// ---------------------------------------------------------------- KLqp
+struct KlqpPlan {
+  int CT, Spad, nblocks, chunk;
+  size_t ws_g, ws_ll;
+};
+
+static KlqpPlan plan_klqp(const GLMDev& m, int S) {
+  KlqpPlan p;
+  p.CT = pick_ct(S);
+  p.Spad = round_up(S, p.CT);
+  const int RT = 2048 / p.CT;
+  const int ntiles = (m.N + RT - 1) / RT;
+  const int sm = sm_count();
+  const int tiles_per_block = std::max(1, (ntiles + sm - 1) / sm);
+  p.chunk = tiles_per_block * RT;
+  p.nblocks = (m.N + p.chunk - 1) / p.chunk;
+  p.ws_g = (size_t)p.nblocks * p.Spad * m.PP * sizeof(float);
+  p.ws_ll = (size_t)p.nblocks * p.Spad * sizeof(double);
+  return p;
+}
+
+extern "C" size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg_klqp_t* cfg) {
+  GLMDev m;
+  if (!cfg || make_glm(model, &m) != EDG_OK || cfg->n_samples <= 0) return 0;
+  const KlqpPlan p = plan_klqp(m, cfg->n_samples);
+  return round_up((int)p.ws_g, 256) + p.ws_ll;
+}
+
+template <int CT>
+static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
+  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4;
+  EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED, "P=%d too large for KLqp kernel", m.P);
+  EDG_REQUIRE(a.S * 2 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
+  EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,
+              "n_samples too large");
+  cudaFuncSetAttribute(klqp_glm_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  klqp_glm_kernel<CT><<<a.nblocks, kThreads, sm, st>>>(m, a);
+  return check_launch("klqp_glm_kernel");
+}
+
+extern "C" int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg,
+                                 const edg_opt_t* opt, float* mu, float* rho, float* opt_slots,
+                                 edg_state_t* state, const float* eps_override, float* grad_out,
+                                 int32_t apply, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(cfg && opt, EDG_E_NULL, "cfg and opt must not be NULL");
+  EDG_REQUIRE(mu && rho && state, EDG_E_NULL, "mu, rho and state must not be NULL");
+  EDG_REQUIRE(!apply || opt_slots, EDG_E_NULL, "opt_slots must not be NULL when apply = 1");
+  EDG_REQUIRE(cfg->n_samples > 0, EDG_E_VALUE, "n_samples should be greater than zero: %d",
+              cfg->n_samples);
+  EDG_REQUIRE(cfg->method >= 0 && cfg->method <= 2, EDG_E_VALUE, "unknown KLqp method %d",
+              cfg->method);
+  EDG_REQUIRE(opt->optimizer >= 0 && opt->optimizer <= 5, EDG_E_VALUE, "unknown optimizer %d",
+              opt->optimizer);
+  const KlqpPlan p = plan_klqp(m, cfg->n_samples);
+  const size_t need = round_up((int)p.ws_g, 256) + p.ws_ll;
+  EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
+              "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
+  KlqpArgs a;
+  a.method = cfg->method;
+  a.S = cfg->n_samples;
+  a.Spad = p.Spad;
+  a.nblocks = p.nblocks;
+  a.chunk = p.chunk;
+  a.dscale = cfg->data_scale;
+  a.kl_scaling = cfg->kl_scaling;
+  a.latent_scale = cfg->latent_scale;
+  a.seed = cfg->seed;
+  a.opt = *opt;
+  a.mu = mu;
+  a.rho = rho;
+  a.slots = opt_slots;
+  a.state = state;
+  a.eps_ovr = eps_override;
+  a.grad_out = grad_out;
+  a.apply = apply;
+  a.ws_g = reinterpret_cast<float*>(workspace);
+  a.ws_ll = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) + round_up((int)p.ws_g, 256));
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (p.CT) {
+    case 8: return launch_klqp<8>(m, a, st);
+    case 16: return launch_klqp<16>(m, a, st);
+    default: return launch_klqp<32>(m, a, st);
+  }
+}
+
+// ---------------------------------------------------------------- HMC
+template <int CT>
+static int launch_hmc(const GLMDev& m, const HmcArgs& a, cudaStream_t st) {
+  const size_t sm = hmc_smem_bytes<CT>(m.PP);
+  EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED,
+              "P=%d needs %zu bytes of shared memory for %d chains per block", m.P, sm, CT);
+  cudaFuncSetAttribute(hmc_glm_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int nblocks = (a.C + CT - 1) / CT;
+  hmc_glm_kernel<CT><<<nblocks, kThreads, sm, st>>>(m, a);
+  return check_launch("hmc_glm_kernel");
+}
+
+extern "C" int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C,
+                               int32_t n_iter, float* z, float* grad, double* lj,
+                               int32_t cache_valid, int32_t* n_accept, edg_state_t* state,
+                               float* samples, int64_t T_cap, double* moments,
+                               const float* r_override, const double* u_override,
+                               double* ratio_out, void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(cfg, EDG_E_NULL, "cfg is NULL");
+  EDG_REQUIRE(z && grad && lj && state, EDG_E_NULL, "z, grad, lj and state must not be NULL");
+  EDG_REQUIRE(C > 0, EDG_E_SHAPE, "C must be positive (got %d)", C);
+  EDG_REQUIRE(n_iter >= 0, EDG_E_SHAPE, "n_iter must be >= 0");
+  EDG_REQUIRE(cfg->n_steps >= 0, EDG_E_VALUE, "n_steps must be >= 0");
+  EDG_REQUIRE(!samples || T_cap > 0, EDG_E_SHAPE, "T_cap must be positive when samples is given");
+  if (n_iter == 0 && cache_valid) return EDG_OK;
+  HmcArgs a;
+  a.C = C;
+  a.n_iter = n_iter;
+  a.n_steps = cfg->n_steps;
+  a.cache_valid = cache_valid;
+  a.step_size = cfg->step_size;
+  a.seed = cfg->seed;
+  a.z = z;
+  a.grad = grad;
+  a.lj = lj;
+  a.n_accept = n_accept;
+  a.state = state;
+  a.samples = samples;
+  a.T_cap = T_cap;
+  a.moments = moments;
+  a.r_ovr = r_override;
+  a.u_ovr = u_override;
+  a.ratio_out = ratio_out;
+  int ct = cfg->chains_per_block;
+  if (ct == 0) ct = 32;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (ct) {
+    case 8: return launch_hmc<8>(m, a, st);
+    case 16: return launch_hmc<16>(m, a, st);
+    case 32: return launch_hmc<32>(m, a, st);
+    default: return fail(EDG_E_VALUE, "chains_per_block must be 0, 8, 16 or 32 (got %d)", ct);
+  }
+}

@@ -1,0 +1,149 @@
+"""Hamiltonian Monte Carlo (``edward/inferences/hmc.py``).
+
+Per iteration and chain (``hmc.py:61-130,195-210``): momentum r0 ~ N(0, I);
+``n_steps`` leapfrog steps (half kick, drift, gradient, half kick); FP64 log
+acceptance ratio 0.5|r0|^2 - 0.5|r|^2 + L(z) - L(z0); accept if
+log u < ratio; the kept state goes to ``Empirical.params[t]``.  All chains
+and all ``n_iter`` iterations of one ``update``/``run`` chunk run in one
+persistent kernel launch; the log joint and its gradient at the current
+state are carried between iterations instead of being recomputed.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib, autotune
+from ..compile import compile_glm
+from ..ops import GLMDevice
+from ..util import next_seed
+from .monte_carlo import MonteCarlo
+
+
+class HMC(MonteCarlo):
+    def initialize(self, step_size=0.25, n_steps=2, chains_per_block=0, *args, **kwargs):
+        """``step_size`` / ``n_steps`` as in ``hmc.py:45-59``;
+        ``chains_per_block`` 0 = autotuned."""
+        self.step_size = step_size
+        self.n_steps = n_steps
+        self._cpb = chains_per_block
+        return super().initialize(*args, **kwargs)
+
+    def _validate(self):
+        if not self.auto_transform:
+            raise ValueError("This implementation of HMC requires that all "
+                             "variables have unconstrained support. Please "
+                             "initialize with auto_transform=True to ensure "
+                             "this. (if your variables already have unconstrained "
+                             "support then doing this is a no-op).")
+        for z, qz in self.latent_vars.items():
+            if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
+                raise NotImplementedError(
+                    f"auto_transform of support '{z.support}' for this model family")
+        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        C = self.n_chains or 1
+        for qz in self.latent_vars.values():
+            if (qz.n_chains or 1) != C:
+                raise ValueError("every Empirical must hold the same number of chains")
+
+    def build_update(self):
+        spec = self._spec
+        self._glm = GLMDevice(spec, self._device)
+        C = self.n_chains or 1
+        self.C = C
+        T = self.n_iter
+        P = spec.P
+        dev = self._device
+        self._samples = torch.zeros(T, C, P, dtype=torch.float32, device=dev)
+        for blk in spec.blocks:
+            qz = self.latent_vars[blk.rv]
+            var = qz.params_var
+            src = var.value.to(dev).reshape(qz.n, C, blk.size)[:T]
+            self._samples[:, :, blk.offset:blk.offset + blk.size] = src
+            view = self._samples[:, :, blk.offset:blk.offset + blk.size]
+            shape = (T, C) + tuple(blk.shape) if qz.n_chains else (T,) + tuple(blk.shape)
+            var._value = view.view(shape)
+            var.shape = tuple(shape)
+            qz.n = T
+        self._z = self._samples[0].clone()
+        self._g = torch.zeros(C, P, dtype=torch.float32, device=dev)
+        self._lj = torch.zeros(C, dtype=torch.float64, device=dev)
+        self._cache_valid = 0
+        self._n_accept = torch.zeros(C, dtype=torch.int32, device=dev)
+        cfg = _lib.EdgHMC()
+        cfg.step_size = float(self.step_size)
+        cfg.n_steps = int(self.n_steps)
+        cfg.seed = next_seed()
+        cfg.chains_per_block = int(self._cpb)
+        self._cfg = cfg
+        if cfg.chains_per_block == 0:
+            cfg.chains_per_block = self._autotune()
+        self.train = self.update
+        return self.train
+
+    def _autotune(self):
+        C, P = self.C, self._spec.P
+        z = self._z.clone()
+        g = torch.zeros_like(self._g)
+        lj = torch.zeros_like(self._lj)
+        st = _lib.new_state(self._device)
+        cands = [8, 16, 32] if C > 8 else [8]
+
+        def run(ct):
+            cfg = _lib.EdgHMC()
+            cfg.step_size, cfg.n_steps, cfg.seed = self._cfg.step_size, self._cfg.n_steps, 1
+            cfg.chains_per_block = ct
+            _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(cfg), C, 1,
+                      _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st),
+                      None, 0, None, None, None, None, _lib.stream_ptr())
+
+        key = f"N{self._spec.N}_D{self._spec.D}_b{int(self._spec.bias)}_C{C}_L{self.n_steps}"
+        return autotune.choose("hmc_glm", key, cands, run)
+
+    def _launch(self, n_iter, r_override=None, u_override=None, ratio_out=None):
+        _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C, int(n_iter),
+                  _lib.ptr(self._z), _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
+                  _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
+                  self._samples.shape[0], None, _lib.ptr(r_override), _lib.ptr(u_override),
+                  _lib.ptr(ratio_out), _lib.stream_ptr())
+        self._cache_valid = 1
+
+    def update(self, feed_dict=None):
+        """One HMC iteration for every chain; returns ``{'t', 'accept_rate'}``
+        (``monte_carlo.py:111-150``), accept_rate = n_accept / t averaged over chains."""
+        if feed_dict:
+            raise NotImplementedError("feed_dict is not supported for this model family")
+        self._launch(1)
+        t = self.t
+        acc = float(self._n_accept.sum().item()) / (max(t, 1) * self.C)
+        return {"t": t, "accept_rate": acc}
+
+    def _run_loop(self):
+        chunk = self.n_print if self.n_print else self.n_iter
+        done = 0
+        while done < self.n_iter:
+            k = min(chunk, self.n_iter - done)
+            self._launch(k)
+            done += k
+            t = self.t
+            acc = float(self._n_accept.sum().item()) / (max(t, 1) * self.C)
+            self.print_progress({"t": t, "accept_rate": acc})
+
+    def run_iterations(self, k, r_override=None, u_override=None, ratio_out=None):
+        """k iterations in one launch, no host synchronisation."""
+        self._launch(k, r_override, u_override, ratio_out)
+
+    @property
+    def n_accept(self):
+        if self.C == 1 and not self.n_chains:
+            return int(self._n_accept[0].item())
+        return self._n_accept
+
+    def reset(self):
+        """Zeroes t and n_accept (``inference.py:283-285``, ``monte_carlo.py:104``);
+        the next iteration restarts from params[0] as the reference's
+        ``params[max(t - 1, 0)]`` does."""
+        super().reset()
+        self._n_accept.zero_()
+        self._z.copy_(self._samples[0])
+        self._cache_valid = 0

@@ -1,0 +1,173 @@
+"""KL(q||p) variational inference (``edward/inferences/klqp.py``).
+
+``KLqp`` dispatches like the reference (``klqp.py:115-163``): Normal q with
+Normal priors -> analytic-KL reparameterisation; other reparameterisable q
+-> Monte Carlo reparameterisation; otherwise the score-function family.
+The explicit variants pin one estimator.  Each step is one launch of a fused
+kernel (Philox eps -> z -> log-lik + adjoint over X for all samples -> KL /
+log q -> chain rule through softplus -> optimizer apply).
+"""
+import numpy as np
+import torch
+
+from .. import _lib
+from ..compile import UnsupportedModel, compile_glm, parse_normal_q
+from ..expr import Variable, softplus
+from ..models import Normal, RandomVariable
+from ..ops import GLMDevice
+from ..util import next_seed, randn
+from .variational_inference import VariationalInference
+
+_CONTINUOUS = ("01", "nonnegative", "simplex", "real", "multivariate_real")
+
+AUTO, REPARAM_KL, REPARAM, SCORE = None, _lib.KLQP_REPARAM_KL, _lib.KLQP_REPARAM, _lib.KLQP_SCORE
+
+
+class KLqp(VariationalInference):
+    """Variational inference with KL(q(z; lambda) || p(z | x))."""
+
+    _method = AUTO
+
+    def __init__(self, latent_vars=None, data=None):
+        if isinstance(latent_vars, list):
+            d = {}
+            for z in latent_vars:
+                if not hasattr(z, "support") or z.support not in _CONTINUOUS:
+                    raise AttributeError(
+                        "Random variable {} is not continuous or a random "
+                        "variable with supported continuous support.".format(z))
+                shape = tuple(z.batch_shape) + tuple(z.event_shape)
+                loc = Variable(randn(shape))
+                scale = softplus(Variable(randn(shape)))
+                d[z] = Normal(loc=loc, scale=scale)
+            latent_vars = d
+        super().__init__(latent_vars, data)
+
+    def initialize(self, n_samples=1, kl_scaling=None, *args, **kwargs):
+        if kl_scaling is None:
+            kl_scaling = {}
+        if n_samples <= 0:
+            raise ValueError("n_samples should be greater than zero: {}".format(n_samples))
+        self.n_samples = n_samples
+        self.kl_scaling = kl_scaling
+        return super().initialize(*args, **kwargs)
+
+    # ------------------------------------------------------------ dispatch
+    def _choose_method(self):
+        is_reparameterizable = all(q.reparameterizable for q in self.latent_vars.values())
+        is_analytic_kl = all(isinstance(z, Normal) and isinstance(q, Normal)
+                             for z, q in self.latent_vars.items())
+        if not is_analytic_kl and self.kl_scaling:
+            raise TypeError("kl_scaling must be None when using non-analytic KL term")
+        if self._method is not AUTO:
+            if self._method == REPARAM_KL and not is_analytic_kl:
+                raise TypeError("analytic KL needs Normal priors and Normal q")
+            return self._method
+        if is_reparameterizable:
+            return REPARAM_KL if is_analytic_kl else REPARAM
+        return "score_rb"
+
+    def _validate(self):
+        method = self._choose_method()
+        if method == "score_rb":
+            raise NotImplementedError(
+                "Rao-Blackwellised score gradients (ScoreRBKLqp) for this model family")
+        self._method_id = method
+        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        for blk in self._spec.blocks:
+            parse_normal_q(self.latent_vars[blk.rv])
+
+    def build_loss_and_gradients(self, var_list):
+        method = self._method_id
+        spec = self._spec
+        self._glm = GLMDevice(spec, self._device)
+        P = spec.P
+        dev = self._device
+        self._mu = torch.empty(P, dtype=torch.float32, device=dev)
+        self._rho = torch.empty(P, dtype=torch.float32, device=dev)
+        kls = np.ones(P, np.float32)
+        lsc = np.ones(P, np.float32)
+        q_vars = []
+        for blk in spec.blocks:
+            q = parse_normal_q(self.latent_vars[blk.rv])
+            for var, buf in ((q.loc_var, self._mu), (q.rho_var, self._rho)):
+                if int(np.prod(var.shape)) != blk.size:
+                    raise ValueError(f"q parameter {var.name} has shape {var.shape}; "
+                                     f"latent {blk.rv.name} has {blk.size} elements")
+                var._rebind(buf[blk.offset:blk.offset + blk.size].view(var.shape or ()))
+                q_vars.append(var)
+            kls[blk.offset:blk.offset + blk.size] = np.broadcast_to(
+                np.asarray(self.kl_scaling.get(blk.rv, 1.0), np.float32), blk.shape).reshape(-1)
+            lsc[blk.offset:blk.offset + blk.size] = np.broadcast_to(
+                np.asarray(self.scale.get(blk.rv, 1.0), np.float32), blk.shape).reshape(-1)
+        if var_list is not None and set(map(id, var_list)) != set(map(id, q_vars)):
+            raise NotImplementedError("var_list must be the variational parameters of q")
+        dscale = np.asarray(self.scale.get(spec.observed, 1.0), np.float32)
+        if dscale.size != 1:
+            raise NotImplementedError("per-row data scale is not supported; pass a scalar")
+        self._kls = torch.as_tensor(kls, device=dev)
+        self._lsc = torch.as_tensor(lsc, device=dev)
+        self._slots = torch.zeros(4 * P, dtype=torch.float32, device=dev)
+        self._reset_optimizer()
+        cfg = _lib.EdgKLqp()
+        cfg.method = method
+        cfg.n_samples = self.n_samples
+        cfg.data_scale = float(dscale.reshape(-1)[0])
+        cfg.kl_scaling = self._kls.data_ptr()
+        cfg.latent_scale = self._lsc.data_ptr()
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        self._opt = self.optimizer.to_c()
+        lib = _lib.load()
+        self._ws_bytes = lib.edg_klqp_glm_workspace_bytes(self._glm.ref(), cfg)
+        self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
+        self._grad = torch.zeros(2 * P, dtype=torch.float32, device=dev)
+        return None, [(None, v) for v in q_vars]
+
+    def _reset_optimizer(self):
+        a, b = self.optimizer.slot_init()
+        P = self._spec.P
+        self._slots[: 2 * P].fill_(a)
+        self._slots[2 * P:].fill_(b)
+
+    def _step(self, apply=True, eps=None, grad_out=None):
+        import ctypes
+        _lib.call("edg_klqp_glm_step", self._glm.ref(), ctypes.byref(self._cfg),
+                  ctypes.byref(self._opt), _lib.ptr(self._mu), _lib.ptr(self._rho),
+                  _lib.ptr(self._slots), _lib.ptr(self._state), _lib.ptr(eps), _lib.ptr(grad_out),
+                  1 if apply else 0, _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+
+    def loss_and_gradients(self, eps=None):
+        """(loss, dloss/dmu, dloss/drho) at the current parameters without
+        applying the optimizer; ``eps`` [n_samples, P] overrides the draws."""
+        if eps is not None:
+            eps = torch.as_tensor(eps, dtype=torch.float32, device=self._device).contiguous()
+        self._step(apply=False, eps=eps, grad_out=self._grad)
+        st = self._read_state()
+        P = self._spec.P
+        g = self._grad.detach().clone()
+        return float(st.loss), g[:P], g[P:]
+
+    @property
+    def seed(self):
+        return int(self._cfg.seed)
+
+    @seed.setter
+    def seed(self, v):
+        self._cfg.seed = int(v)
+        self._graphs = {}
+
+
+class ReparameterizationKLqp(KLqp):
+    """Monte Carlo KL with the reparameterisation gradient (klqp.py:166-226, 642-704)."""
+    _method = REPARAM
+
+
+class ReparameterizationKLKLqp(KLqp):
+    """Analytic KL with the reparameterisation gradient (klqp.py:229-303, 707-769)."""
+    _method = REPARAM_KL
+
+
+class ScoreKLqp(KLqp):
+    """Score-function gradient, no baseline (klqp.py:370-430, 840-906)."""
+    _method = SCORE

@@ -1,0 +1,201 @@
+/*
+ * edward_gb300 -- C ABI of the GB300 (sm_103a) inference hot path.
+ *
+ * The reference (blei-lab/edward 1.3.5) has no native code: its hot path is
+ * Python building TensorFlow 1.x graphs.  Each entry point below replaces one
+ * piece of that graph, cited as path:line inside the reference tree.
+ *
+ * Conventions
+ *  - Every pointer argument is DEVICE memory owned by the caller, except the
+ *    descriptor structs themselves (edg_glm_t, edg_klqp_t, ...), which are
+ *    host structs read during the call.
+ *  - `stream` is a cudaStream_t passed as void*; every call is stream-ordered
+ *    and never synchronises the host.
+ *  - Return value: EDG_OK (0) or a negative EDG_E_* code;
+ *    edg_last_error_string() gives the detail (thread-local).
+ *  - Entry points that need scratch take (workspace, workspace_bytes); the
+ *    matching *_workspace_bytes() query gives the size.
+ *  - State that advances between calls (iteration t, optimizer step,
+ *    Adam beta powers) lives in a caller-allocated device edg_state_t so
+ *    that repeated calls can be captured in a CUDA graph.
+ */
+#ifndef EDWARD_GB300_H_
+#define EDWARD_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDG_ABI_VERSION 1
+
+enum {
+  EDG_OK = 0,
+  EDG_E_NULL = -1,        /* required pointer is NULL */
+  EDG_E_SHAPE = -2,       /* bad size / dimension */
+  EDG_E_VALUE = -3,       /* bad scalar argument (e.g. n_samples <= 0) */
+  EDG_E_CUDA = -4,        /* CUDA launch / runtime failure */
+  EDG_E_NONFINITE = -5,   /* non-finite value detected (debug mode) */
+  EDG_E_TIMEOUT = -6,     /* a bounded device-side wait gave up */
+  EDG_E_UNSUPPORTED = -7, /* configuration not supported by the kernels */
+  EDG_E_WORKSPACE = -8    /* workspace too small */
+};
+
+/* Likelihood of the GLM family. */
+enum { EDG_LIK_BERNOULLI = 0, EDG_LIK_NORMAL = 1 };
+
+/* KLqp estimator (klqp.py builders). */
+enum {
+  EDG_KLQP_REPARAM_KL = 0, /* build_reparam_kl_loss_and_gradients, klqp.py:707-769 */
+  EDG_KLQP_REPARAM = 1,    /* build_reparam_loss_and_gradients,    klqp.py:642-704 */
+  EDG_KLQP_SCORE = 2       /* build_score_loss_and_gradients,      klqp.py:840-906 */
+};
+
+/* Optimizers accepted by VariationalInference.initialize
+ * (edward/inferences/variational_inference.py:95-116). */
+enum {
+  EDG_OPT_ADAM = 0,
+  EDG_OPT_SGD = 1,      /* 'gradientdescent' */
+  EDG_OPT_MOMENTUM = 2, /* momentum 0.9 */
+  EDG_OPT_ADAGRAD = 3,
+  EDG_OPT_RMSPROP = 4,
+  EDG_OPT_ADADELTA = 5
+};
+
+/* Generalised linear model: y_n ~ Lik(eta_n), eta = X z[:D] (+ z[D] if bias),
+ * z_p ~ Normal(prior_loc[p], prior_scale[p]), P = D + bias.
+ * Covers ed.dot regressions (edward/util/tensorflow.py:10-47;
+ * tests/inferences/hmc_test.py:48-91) and the Normal-Normal model
+ * (tests/inferences/klqp_test.py:14-44 with X = ones(N, 1)). */
+typedef struct {
+  const float* X;           /* [N, D] row-major */
+  const float* y;           /* [N] (0/1 for Bernoulli) */
+  int32_t N;
+  int32_t D;
+  int32_t bias;             /* 1: last coordinate of z is an intercept */
+  int32_t lik;              /* EDG_LIK_* */
+  float lik_scale;          /* Normal likelihood scale */
+  const float* prior_loc;   /* [P] */
+  const float* prior_scale; /* [P] */
+} edg_glm_t;
+
+/* Device-resident iteration state.  Zero-initialise, then set
+ * beta1_power/beta2_power to beta1/beta2 (TF's Adam accumulators). */
+typedef struct {
+  int64_t t;             /* Inference.t (inference.py:195-197) */
+  int64_t global_step;   /* optimizer global step (lr schedule) */
+  float beta1_power;
+  float beta2_power;
+  uint32_t done;         /* internal completion counter; 0 between calls */
+  uint32_t nonfinite;    /* non-finite loss/gradient values seen */
+  double loss;           /* loss of the last KLqp update */
+  double aux[4];         /* estimator-specific diagnostics */
+} edg_state_t;
+
+/* Optimizer + learning-rate schedule.  lr = lr0 * decay_rate^(step/decay_steps)
+ * (floored if staircase) when decay_steps > 0, else lr0.  The Edward default
+ * (optimizer=None) is Adam with lr0=0.1, decay_steps=100, decay_rate=0.9,
+ * staircase=1 (variational_inference.py:83-97). */
+typedef struct {
+  int32_t optimizer;   /* EDG_OPT_* */
+  float lr0;
+  int64_t decay_steps;
+  float decay_rate;
+  int32_t staircase;
+  float beta1, beta2, epsilon; /* Adam */
+  float momentum;              /* momentum / rmsprop momentum */
+  float rho;                   /* rmsprop decay / adadelta rho */
+} edg_opt_t;
+
+/* KLqp configuration (KLqp.initialize, klqp.py:86-113). */
+typedef struct {
+  int32_t method;            /* EDG_KLQP_* */
+  int32_t n_samples;         /* > 0 */
+  float data_scale;          /* Inference.scale[x] (inference.py:215-220) */
+  const float* kl_scaling;   /* [P] or NULL (= 1) */
+  const float* latent_scale; /* [P] or NULL (= 1): Inference.scale[z] */
+  uint64_t seed;
+} edg_klqp_t;
+
+/* HMC configuration (HMC.initialize, edward/inferences/hmc.py:45-59). */
+typedef struct {
+  float step_size;
+  int32_t n_steps;
+  uint64_t seed;
+  int32_t chains_per_block; /* 0 = library default; else 8, 16 or 32 */
+} edg_hmc_t;
+
+/* ---------------------------------------------------------------- library */
+int edg_abi_version(void);
+const char* edg_last_error_string(void);
+/* SM count and compute capability of the current device. */
+int edg_device_info(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* ---------------------------------------------------------------- RNG
+ * Philox4x32-10 streams that replace tf.random_normal / tf.random_uniform
+ * (hmc.py:88-91,108) and the reparameterised draw in copy(qz)
+ * (klqp.py:727-731).  Counter = (element/4, row, iteration, kind). */
+int edg_philox_u32(uint64_t seed, uint32_t kind, uint32_t iteration, int32_t rows,
+                   int32_t n, uint32_t* out /* [rows, round_up(n,4)] */, void* stream);
+int edg_philox_normal(uint64_t seed, uint32_t kind, uint32_t iteration, int32_t rows,
+                      int32_t n, float* out /* [rows, n] */, void* stream);
+int edg_philox_uniform64(uint64_t seed, uint32_t kind, uint32_t iteration, int32_t rows,
+                         double* out /* [rows] */, void* stream);
+
+/* ---------------------------------------------------------------- GLM log joint
+ * Batched log joint and its adjoint for B parameter vectors Z [B, P]:
+ *   lp[b]   = data_scale * sum_n log p(y_n | eta_nb)  (+ log prior if include_prior)
+ *   grad[b] = d lp[b] / d z_b
+ * Replaces the per-sample `x_copy.log_prob` + tf.gradients of
+ * klqp.py:682-686,702 and hmc.py:161-192,199,206 (ed.dot:
+ * edward/util/tensorflow.py:41-47). */
+size_t edg_glm_logjoint_grad_workspace_bytes(const edg_glm_t* model, int32_t B);
+int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int32_t B,
+                          int32_t include_prior, float data_scale,
+                          double* lp_out /* [B] or NULL */, float* grad_out /* [B,P] or NULL */,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------- KLqp
+ * One fused ELBO-gradient step for a mean-field Normal q = N(mu, softplus(rho))
+ * over a GLM: Philox eps -> z_s -> log-lik + adjoint over X for all samples
+ * -> KL / log q terms -> chain rule to (mu, rho) -> optimizer apply.
+ * Replaces build_*_loss_and_gradients (klqp.py:642-906) plus
+ * VariationalInference.update (variational_inference.py:133-164).
+ * opt_slots: [4 * P] floats (two slots of 2P: Adam m and v, etc.), zeroed at
+ * start (adagrad/rmsprop initial accumulators are set by the caller).
+ * eps_override: [n_samples, P] or NULL (NULL = Philox stream KIND 0 at
+ * iteration state->t).  grad_out: [2P] = (dloss/dmu, dloss/drho) or NULL.
+ * apply = 0 computes loss/gradients without touching mu/rho/slots/state.
+ * The loss (pre-update) is written to state->loss. */
+size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg_klqp_t* cfg);
+int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg, const edg_opt_t* opt,
+                      float* mu, float* rho, float* opt_slots, edg_state_t* state,
+                      const float* eps_override, float* grad_out, int32_t apply,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------- HMC
+ * n_iter HMC iterations for C independent chains over a GLM in one launch.
+ * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and
+ * MonteCarlo.update (edward/inferences/monte_carlo.py:111-150).
+ * z, grad, lj: current state, its log-joint gradient and value (the cache is
+ * rebuilt when cache_valid = 0).  Iteration i uses t = state->t + i for its
+ * Philox counters and writes the kept sample to samples[t] (Empirical.params,
+ * [T_cap, C, P]) when samples != NULL and t < T_cap.  moments (or NULL):
+ * [2, C, P] FP64 running sum and sum of squares of kept samples.
+ * r_override [n_iter, C, P] / u_override [n_iter, C] replace the momentum
+ * and Metropolis uniform draws.  ratio_out [n_iter, C] (or NULL) receives
+ * the FP64 log acceptance ratio.  state->t advances by n_iter. */
+int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
+                    float* z, float* grad, double* lj, int32_t cache_valid,
+                    int32_t* n_accept, edg_state_t* state,
+                    float* samples, int64_t T_cap, double* moments,
+                    const float* r_override, const double* u_override, double* ratio_out,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EDWARD_GB300_H_ */

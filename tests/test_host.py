@@ -1,0 +1,151 @@
+"""Host-side logic of the drop-in surface (no GPU): model compilation,
+optimizer resolution and the reference's error behaviour."""
+import numpy as np
+import pytest
+
+import edward_gb300 as ed
+from edward_gb300 import train
+from edward_gb300.compile import UnsupportedModel, compile_glm
+from edward_gb300.models import Bernoulli, Empirical, HalfNormal, Normal
+
+
+def logreg(N=20, D=3, bias=True):
+    X = np.random.default_rng(0).standard_normal((N, D)).astype(np.float32)
+    w = Normal(loc=ed.zeros(D), scale=ed.ones(D))
+    eta = ed.dot(X, w)
+    lat = [w]
+    if bias:
+        b = Normal(loc=0.5, scale=2.0)
+        eta = eta + b
+        lat.append(b)
+    y = Bernoulli(logits=eta)
+    return X, lat, y
+
+
+def test_compile_logistic_regression():
+    X, lat, y = logreg()
+    spec = compile_glm(lat, {y: np.zeros(20)})
+    assert spec.P == 4 and spec.bias and spec.lik == 0
+    np.testing.assert_array_equal(spec.prior_loc, [0, 0, 0, 0.5])
+    np.testing.assert_array_equal(spec.prior_scale, [1, 1, 1, 2])
+    assert [b.offset for b in spec.blocks] == [0, 3]
+
+
+def test_compile_normal_normal():
+    mu = Normal(loc=0.0, scale=1.0)
+    x = Normal(loc=mu, scale=1.0, sample_shape=50)
+    spec = compile_glm([mu], {x: np.zeros(50)})
+    assert spec.X.shape == (50, 1) and not spec.bias and spec.lik == 1 and spec.P == 1
+
+
+def test_compile_placeholder_linear_regression():
+    N, D = 40, 10
+    X = ed.placeholder(np.float32, [N, D])
+    w = Normal(loc=ed.zeros(D), scale=ed.ones(D))
+    b = Normal(loc=ed.zeros(1), scale=ed.ones(1))
+    y = Normal(loc=ed.dot(X, w) + b, scale=0.1 * np.ones(N, np.float32))
+    xv = np.ones((N, D), np.float32)
+    spec = compile_glm([w, b], {X: xv, y: np.zeros(N)})
+    assert spec.bias and abs(spec.lik_scale - 0.1) < 1e-7 and spec.P == 11
+
+
+@pytest.mark.parametrize("bad", ["two_dots", "unused", "prior"])
+def test_compile_unsupported(bad):
+    X = np.ones((5, 2), np.float32)
+    w = Normal(loc=ed.zeros(2), scale=ed.ones(2))
+    v = Normal(loc=ed.zeros(2), scale=ed.ones(2))
+    if bad == "two_dots":
+        y = Bernoulli(logits=ed.dot(X, w) + ed.dot(X, v))
+        lat = [w, v]
+    elif bad == "unused":
+        y = Bernoulli(logits=ed.dot(X, w))
+        lat = [w, v]
+    else:
+        h = HalfNormal(scale=1.0)
+        y = Bernoulli(logits=ed.dot(X, w) + h)
+        lat = [w, h]
+    with pytest.raises(NotImplementedError):
+        compile_glm(lat, {y: np.zeros(5)})
+
+
+def test_klqp_n_samples_check():
+    """klqp_test.py:63-80."""
+    X, lat, y = logreg()
+    inf = ed.KLqp(lat, data={y: np.zeros(20)})
+    with pytest.raises(ValueError, match="n_samples should be greater than zero: 0"):
+        inf.initialize(n_samples=0)
+
+
+def test_klqp_list_latents_build_normal_q():
+    X, lat, y = logreg()
+    inf = ed.KLqp(lat, data={y: np.zeros(20)})
+    for z, q in inf.latent_vars.items():
+        assert isinstance(q, Normal) and q.mean().shape == z.shape
+
+
+def test_klqp_rejects_discrete_list_latent():
+    z = Bernoulli(logits=0.0)
+    with pytest.raises(AttributeError):
+        ed.KLqp([z], data={})
+
+
+def test_kl_scaling_requires_analytic_kl():
+    X, lat, y = logreg()
+    inf = ed.ReparameterizationKLqp(lat, data={y: np.zeros(20)})
+    inf.latent_vars = {z: Bernoulli(logits=0.0) for z in lat}
+    with pytest.raises(TypeError, match="kl_scaling must be None"):
+        inf.initialize(n_samples=1, kl_scaling={lat[0]: 2.0})
+
+
+def test_hmc_requires_empirical():
+    X, lat, y = logreg()
+    with pytest.raises(TypeError, match="Empirical"):
+        ed.HMC({lat[0]: Normal(0.0, 1.0)}, data={y: np.zeros(20)})
+
+
+def test_hmc_requires_auto_transform():
+    X, lat, y = logreg()
+    inf = ed.HMC(lat, data={y: np.zeros(20)})
+    with pytest.raises(ValueError, match="unconstrained support"):
+        inf.initialize(auto_transform=False)
+
+
+def test_hmc_list_latents_default_store():
+    """monte_carlo.py:78-83: list latents get Empirical(zeros([1e4, ...]))."""
+    X, lat, y = logreg()
+    inf = ed.HMC(lat, data={y: np.zeros(20)})
+    assert all(isinstance(q, Empirical) and q.n == 10000 for q in inf.latent_vars.values())
+    inf2 = ed.HMC(lat, data={y: np.zeros(20)}, n_chains=8)
+    assert inf2.latent_vars[lat[0]].params.shape == (10000, 8, 3)
+
+
+def test_optimizer_resolution():
+    """variational_inference.py:83-116."""
+    o = train.resolve(None, None)
+    assert isinstance(o, train.AdamOptimizer)
+    assert isinstance(o.learning_rate, train.ExponentialDecay)
+    assert o.learning_rate.staircase and o.learning_rate.decay_steps == 100
+    o = train.resolve("adam", None)
+    assert o.learning_rate == 0.01
+    assert isinstance(train.resolve("rmsprop", None), train.RMSPropOptimizer)
+    with pytest.raises(ValueError):
+        train.resolve("nope", None)
+    with pytest.raises(TypeError):
+        train.resolve(3, None)
+
+
+def test_compute_fails_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    X, lat, y = logreg()
+    inf = ed.KLqp(lat, data={y: np.zeros(20)})
+    with pytest.raises(RuntimeError, match="CUDA"):
+        inf.run(n_samples=2, n_iter=3)
+
+
+def test_scale_must_be_dict():
+    X, lat, y = logreg()
+    inf = ed.KLqp(lat, data={y: np.zeros(20)})
+    with pytest.raises(TypeError, match="scale must be a dict"):
+        inf.initialize(scale=3.0)

@@ -1,0 +1,158 @@
+"""Pins of the CPU oracle (no GPU): Philox known answers, FP64 finite
+differences, the golden fixtures and the closed-form posteriors that the
+reference's own tests assert."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import densities as dn
+from oracle.glm import GLM, NORMAL, conjugate_linreg_posterior, synthetic_logreg
+from oracle.hmc import glm_lj_grad, hmc_step, run_hmc
+from oracle.klqp import REPARAM, REPARAM_KL, SCORE, TFAdam, klqp_glm_loss_and_grads, run_klqp_glm
+from oracle.philox import philox4x32_10, raw_u32, normals, uniforms64
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "oracle_small.npz")
+
+
+# Published Philox4x32-10 known-answer vectors (Salmon et al., SC 2011;
+# the Random123 distribution's kat_vectors): (counter, key) -> output.
+PHILOX_KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+@pytest.mark.parametrize("ctr,key,expect", PHILOX_KAT)
+def test_philox_known_answers(ctr, key, expect):
+    out = philox4x32_10(*ctr, *key)
+    assert tuple(int(x) for x in out) == expect
+
+
+def test_philox_normals_moments():
+    z = normals(7, 0, 3, 4000, 64).ravel()
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+    u = uniforms64(7, 2, 3, 100000)
+    assert 0 < u.min() and u.max() < 1 and abs(u.mean() - 0.5) < 0.005
+
+
+def _fd(f, x, h=1e-6):
+    g = np.zeros_like(x)
+    for i in range(x.size):
+        xp, xm = x.copy(), x.copy()
+        xp.flat[i] += h
+        xm.flat[i] -= h
+        g.flat[i] = (f(xp) - f(xm)) / (2 * h)
+    return g
+
+
+@pytest.mark.parametrize("lik", [0, 1])
+def test_glm_gradient_finite_differences(lik):
+    X, y, _, _ = synthetic_logreg(60, 4, seed=2)
+    if lik == 1:
+        y = X @ np.arange(4) * 0.3 + 0.1
+    m = GLM(X, y, bias=True, lik=lik, lik_scale=0.7, prior_loc=0.3, prior_scale=2.0)
+    Z = np.random.default_rng(0).standard_normal((3, 5))
+    g = m.grad_log_joint(Z)
+    for b in range(3):
+        fd = _fd(lambda z: m.log_joint(z[None])[0], Z[b])
+        np.testing.assert_allclose(g[b], fd, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("method", [REPARAM_KL, REPARAM])
+def test_klqp_gradient_finite_differences(method):
+    X, y, _, _ = synthetic_logreg(40, 3, seed=5)
+    m = GLM(X, y, bias=True, prior_scale=1.3, data_scale=2.0)
+    rng = np.random.default_rng(1)
+    mu, rho, eps = rng.standard_normal(4), rng.standard_normal(4), rng.standard_normal((3, 4))
+    _, gmu, grho, _ = klqp_glm_loss_and_grads(m, mu, rho, eps, method, latent_scale=1.5)
+    fmu = _fd(lambda v: klqp_glm_loss_and_grads(m, v, rho, eps, method, latent_scale=1.5)[0], mu)
+    frho = _fd(lambda v: klqp_glm_loss_and_grads(m, mu, v, eps, method, latent_scale=1.5)[0], rho)
+    np.testing.assert_allclose(gmu, fmu, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(grho, frho, rtol=1e-6, atol=1e-6)
+
+
+def test_score_gradient_is_unbiased():
+    """E_eps[score gradient] = gradient of the exact negative ELBO (checked
+    against the reparameterisation gradient averaged over many draws)."""
+    m = GLM(np.ones((5, 1)), np.zeros(5), bias=False, lik=NORMAL, lik_scale=1.0)
+    mu, rho = np.array([0.4]), np.array([-0.5])
+    eps = np.random.default_rng(3).standard_normal((200000, 1))
+    _, gs_mu, gs_rho, _ = klqp_glm_loss_and_grads(m, mu, rho, eps, SCORE)
+    _, gr_mu, gr_rho, _ = klqp_glm_loss_and_grads(m, mu, rho, eps, REPARAM)
+    np.testing.assert_allclose(gs_mu, gr_mu, rtol=0.05, atol=0.05)
+    np.testing.assert_allclose(gs_rho, gr_rho, rtol=0.05, atol=0.05)
+
+
+def test_golden_fixture_regression():
+    """The oracle still produces the committed fixtures (make_golden.py)."""
+    g = np.load(GOLD)
+    seed = 0x0123456789ABCDEF
+    np.testing.assert_array_equal(raw_u32(seed, 1, 7, 5, 10), g["philox_u32"])
+    np.testing.assert_allclose(normals(seed, 1, 7, 5, 10), g["philox_normal"], rtol=0, atol=0)
+    m = GLM(g["lr_X"], g["lr_y"], bias=True, prior_loc=0.25, prior_scale=1.5)
+    np.testing.assert_allclose(m.log_joint(g["lr_Z"]), g["lr_lp"], rtol=1e-12)
+    np.testing.assert_allclose(m.grad_log_joint(g["lr_Z"]), g["lr_grad"], rtol=1e-12)
+    for name, meth in (("kl", REPARAM_KL), ("re", REPARAM), ("sc", SCORE)):
+        loss, gmu, grho, _ = klqp_glm_loss_and_grads(m, g["kq_mu"], g["kq_rho"], g["kq_eps"], meth)
+        np.testing.assert_allclose(loss, g[f"kq_{name}_loss"], rtol=1e-12)
+        np.testing.assert_allclose(gmu, g[f"kq_{name}_gmu"], rtol=1e-12)
+        np.testing.assert_allclose(grho, g[f"kq_{name}_grho"], rtol=1e-12)
+    f = glm_lj_grad(m)
+    lj0, g0 = f(g["hmc_z0"])
+    res = hmc_step(f, g["hmc_z0"], g0, lj0, g["hmc_r0"], g["hmc_u"], 0.05, 3)
+    np.testing.assert_allclose(res["z_prop"], g["hmc_zprop"], rtol=1e-12)
+    np.testing.assert_array_equal(res["accept"].astype(np.int32), g["hmc_accept"])
+
+
+def test_tf_adam_first_step():
+    """TF's Adam: the first step moves each parameter by ~lr * sign(g)."""
+    opt = TFAdam(3)
+    p = opt.apply(np.zeros(3), np.array([2.0, -0.5, 1e-3]), 0.1)
+    np.testing.assert_allclose(p, [-0.1, 0.1, -0.1], rtol=1e-3)
+
+
+def test_kl_normal_normal_closed_form():
+    kl = dn.kl_normal_normal(0.3, 0.7, -0.2, 1.4)
+    x = np.linspace(-12, 12, 200001)
+    q = np.exp(dn.normal_log_prob(x, 0.3, 0.7))
+    num = np.trapezoid(q * (dn.normal_log_prob(x, 0.3, 0.7) - dn.normal_log_prob(x, -0.2, 1.4)), x)
+    assert abs(kl - num) < 1e-8
+
+
+# ------------------------------------------------ statistical pins (reference tests)
+
+def test_oracle_klqp_normal_normal_posterior():
+    """klqp_test.py:14-35: q -> N(0, sqrt(1/51)) for x = 0 (x50)."""
+    m = GLM(np.ones((50, 1)), np.zeros(50), bias=False, lik=NORMAL, lik_scale=1.0)
+    mu, rho, _ = run_klqp_glm(m, [0.5], [0.3], 1500, 1, seed=11)
+    assert abs(mu[0]) < 0.05
+    assert abs(dn.softplus(rho[0]) - np.sqrt(1 / 51)) < 0.02
+
+
+def test_oracle_hmc_normal_normal_posterior():
+    """hmc_test.py:14-45 (mean ~ 0, std ~ sqrt(1/51), acceptance > 0.1)."""
+    m = GLM(np.ones((50, 1)), np.zeros(50), bias=False, lik=NORMAL, lik_scale=1.0)
+    s, na = run_hmc(glm_lj_grad(m), np.ones((8, 1)), 1500, 0.25, 2, seed=5)
+    post = s[300:].reshape(-1)
+    assert abs(post.mean()) < 0.02
+    assert abs(post.std() - np.sqrt(1 / 51)) < 0.01
+    assert (na / 1500).min() > 0.1
+
+
+def test_oracle_hmc_linear_regression_conjugate():
+    """hmc_test.py:48-91 against the closed-form conjugate posterior."""
+    rng = np.random.default_rng(0)
+    N, D = 40, 10
+    w_true = rng.standard_normal(D)
+    X = rng.standard_normal((N, D))
+    y = X @ w_true + rng.normal(0, 0.1, N)
+    m = GLM(X, y, bias=True, lik=NORMAL, lik_scale=0.1)
+    mean, cov = conjugate_linreg_posterior(X, y, 0.1)
+    s, na = run_hmc(glm_lj_grad(m), np.tile(mean, (8, 1)), 400, 0.01, 10, seed=3)
+    est = s[100:].reshape(-1, D + 1).mean(0)
+    sd = np.sqrt(np.diag(cov))
+    assert np.all(np.abs(est - mean) < 4 * sd / np.sqrt(8 * 300 / 20) + 1e-3)
+    np.testing.assert_allclose(est[:D], w_true, atol=0.5, rtol=0.5)
