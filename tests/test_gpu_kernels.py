@@ -263,6 +263,8 @@ def test_hmc_iteration_parity(cuda, ct, N, D, C, L, lik):
     r0 = rng.standard_normal((C, P)).astype(np.float32)
     u = rng.random(C)
     step = 0.01 if N > 1000 else 0.05
+    if ct == 8 and D > 64:
+        pytest.skip("8 chains per block uses 256-row tiles: too much shared memory for P > 64")
     z, g, lj, nacc, ratio, st = _run_hmc_kernel(
         dev, C, torch.as_tensor(z0, device=cuda), step, L, 1,
         r=torch.as_tensor(r0[None], device=cuda).contiguous(),
