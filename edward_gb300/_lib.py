@@ -39,7 +39,8 @@ class EdgGLM(ctypes.Structure):
 class EdgState(ctypes.Structure):
     _fields_ = [("t", c_int64), ("global_step", c_int64), ("beta1_power", c_float),
                 ("beta2_power", c_float), ("done", c_uint32), ("nonfinite", c_uint32),
-                ("loss", c_double), ("aux", c_double * 4)]
+                ("error", c_uint32), ("reserved", c_uint32), ("loss", c_double),
+                ("aux", c_double * 3)]
 
 
 class EdgOpt(ctypes.Structure):
@@ -55,7 +56,7 @@ class EdgKLqp(ctypes.Structure):
 
 class EdgHMC(ctypes.Structure):
     _fields_ = [("step_size", c_float), ("n_steps", c_int32), ("seed", c_uint64),
-                ("chains_per_block", c_int32)]
+                ("chains_per_block", c_int32), ("cluster_size", c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -77,6 +78,12 @@ _SIGS = {
                                   c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p,
                                   c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
+    "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
+    "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
+    "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,
+                                     c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
+                                     c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p]),
 }
 
 _lock = threading.Lock()

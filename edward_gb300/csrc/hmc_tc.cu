@@ -1,0 +1,805 @@
+// Tensor-core (tcgen05, 3xTF32) HMC for the GLM family.
+//
+// Work decomposition
+//   * one thread-block CLUSTER per 128 chains (the MMA M dimension); the R CTAs
+//     of a cluster split the rows of X; every leapfrog gradient is reduced
+//     across the cluster through distributed shared memory (DSMEM);
+//   * per CTA and 64-row tile of X, two chained GEMMs on the tensor core:
+//       forward   eta^T[c][n] = sum_d Z[c][d] X[n][d]      (SS: A = Z smem, B = X tile)
+//       backward  G[c][d]    += sum_n r[c][n] X[n][d]      (TS: A = r in TMEM, B = X^T tile)
+//     with r = d log p(y_n | eta) / d eta computed by the epilogue warps from
+//     the forward accumulator (TMEM) and written back to TMEM as the backward
+//     A operand; eta/r are double-buffered so the epilogue of tile i overlaps
+//     the MMAs of tile i+1;
+//   * 3xTF32: every operand is split a = hi + lo (hi = tf32(a), lo = tf32(a - hi))
+//     and each product is hi*hi + hi*lo + lo*hi with FP32 accumulation;
+//   * X is re-laid once per model into 64-row tiles already in the canonical
+//     K-major shared-memory layout (hi, lo, transposed hi, transposed lo, y),
+//     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
+//
+// Warp roles (192 threads): warp 0 bulk-copy producer, warp 1 MMA issuer and
+// TMEM owner, warps 2-5 epilogue; between gradient evaluations warps 2-5 are
+// the "owners" that run the leapfrog / Metropolis arithmetic for this CTA's
+// share of the cluster's chains, with the chain state in registers.
+//
+// Every mbarrier wait is bounded (~1 s of clock64): on timeout the kernel
+// records EDG_E_TIMEOUT in edg_state_t::error and runs to completion without
+// waiting further, so no launch can hang.
+#include <algorithm>
+#include <cstdio>
+
+#include "edg_common.cuh"
+
+namespace edg {
+namespace tc {
+
+constexpr int kCT = 128;        // chains per cluster = MMA M
+constexpr int kNR = 64;         // rows per X tile = forward N = backward K
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 512;
+
+__host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP + 256u; }
+
+// Canonical K-major, no-swizzle layout: 8-row x 16-byte core matrices; core
+// matrices adjacent along K are 128 B apart (LBO), 8-row groups are
+// (K/4)*128 B apart (SBO).
+__host__ __device__ inline uint32_t kmajor_off(int row, int k, int Kext) {
+  return (uint32_t)((row >> 3) * (Kext * 32) + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t u;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+  return __uint_as_float(u);
+}
+
+// ------------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after ~2^31 cycles (about one second), records the
+// timeout and returns so that the launch always terminates.
+__device__ __forceinline__ void mbar_wait(uint32_t bar, uint32_t parity, volatile int* err) {
+  if (mbar_try(bar, parity)) return;
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (*err) return;
+    if (clock64() - t0 > (1LL << 31)) {
+      *err = 1;
+      return;
+    }
+  }
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for the tcgen05 family; no swizzle
+  return d;
+}
+// kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_ss(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_ts(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                       uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+          taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+      "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+      "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_size() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::
+                   : "memory");
+}
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float4 ld_dsmem4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_dsmem_f64(uint32_t addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_dsmem4(uint32_t addr, float4 v) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
+// ------------------------------------------------------------------ tiling
+__global__ void prep_tiles_kernel(const float* __restrict__ X, const float* __restrict__ y, int N,
+                                  int D, int bias, int PP, int ntiles,
+                                  unsigned char* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)ntiles * kNR * PP;
+  if (i >= total) return;
+  const int tile = (int)(i / (kNR * PP));
+  const int rem = (int)(i % (kNR * PP));
+  const int n = rem / PP, d = rem % PP;
+  const int row = tile * kNR + n;
+  float v = 0.0f;
+  if (row < N) {
+    if (d < D)
+      v = X[(size_t)row * D + d];
+    else if (d == D && bias)
+      v = 1.0f;
+  }
+  const float hi = tf32_rna(v);
+  const float lo = tf32_rna(v - hi);
+  unsigned char* base = out + (size_t)tile * stage_bytes(PP);
+  float* xhi = reinterpret_cast<float*>(base);
+  float* xlo = reinterpret_cast<float*>(base + 256 * PP);
+  float* xthi = reinterpret_cast<float*>(base + 512 * PP);
+  float* xtlo = reinterpret_cast<float*>(base + 768 * PP);
+  const uint32_t o1 = kmajor_off(n, d, PP) / 4;   // X tile: rows n, K = d
+  const uint32_t o2 = kmajor_off(d, n, kNR) / 4;  // X^T tile: rows d, K = n
+  xhi[o1] = hi;
+  xlo[o1] = lo;
+  xthi[o2] = hi;
+  xtlo[o2] = lo;
+  if (d == 0) reinterpret_cast<float*>(base + 1024 * PP)[n] = row < N ? y[row] : 0.0f;
+}
+
+// ------------------------------------------------------------------ main kernel
+struct TcArgs {
+  const unsigned char* tiles;
+  int ntiles, N, P, PP, lik;
+  float inv_lik_var, lik_norm;
+  const float* prior_loc;
+  const float* prior_scale;
+  int C, n_iter, n_steps, cache_valid;
+  float step_size;
+  uint64_t seed;
+  float* z;
+  float* grad;
+  double* lj;
+  int32_t* n_accept;
+  edg_state_t* state;
+  float* samples;
+  int64_t T_cap;
+  double* moments;
+  const float* r_ovr;
+  const double* u_ovr;
+  double* ratio_out;
+};
+
+constexpr int kMaxEPT = 16;  // chain-state elements per owner thread
+
+__global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int PP = a.PP, P = a.P;
+  const uint32_t SB = stage_bytes(PP);
+  unsigned char* stage0 = smem;
+  unsigned char* stage1 = smem + SB;
+  float* Zhi = reinterpret_cast<float*>(smem + 2 * SB);
+  float* Zlo = Zhi + kCT * PP;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Zlo + kCT * PP);
+  // bars: full[2] empty[2] eta[2] r[2] G[1]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 12);
+  volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  __shared__ bool s_last;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t R = cluster_size(), rank = cluster_rank();
+  const int cluster_id = blockIdx.x / R;
+  const int c_base = cluster_id * kCT;
+  const int t_begin = (int)((int64_t)a.ntiles * rank / R);
+  const int t_end = (int)((int64_t)a.ntiles * (rank + 1) / R);
+  const int nt = t_end - t_begin;
+
+  const uint32_t bar_full0 = smem_u32(bars + 0), bar_empty0 = smem_u32(bars + 2);
+  const uint32_t bar_eta0 = smem_u32(bars + 4), bar_r0 = smem_u32(bars + 6);
+  const uint32_t bar_G = smem_u32(bars + 8);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(bar_full0 + 8 * i, 1);
+      mbar_init(bar_empty0 + 8 * i, 1);
+      mbar_init(bar_eta0 + 8 * i, 1);
+      mbar_init(bar_r0 + 8 * i, 4);
+    }
+    mbar_init(bar_G, 1);
+    *err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tmem_slot;
+  // TMEM columns: G [0, 64); per buffer b: eta, r_hi, r_lo at 64 + 192 b + {0, 64, 128}
+  const uint32_t col_G = 0;
+#define COL_ETA(b) (64u + 192u * (b))
+#define COL_RHI(b) (128u + 192u * (b))
+#define COL_RLO(b) (192u + 192u * (b))
+
+  // ---- owner mapping (warps 2-5): R threads per chain, EPT elements each
+  const bool owner = warp >= 2;
+  const int et = threadIdx.x - 64;
+  const int CPO = kCT / (int)R;
+  const int EPT = PP / (int)R;
+  const int chain_local = owner ? et / (int)R : 0;
+  const int part = owner ? et % (int)R : 0;
+  const int d0 = part * EPT;
+  const int cc = (int)rank * CPO + chain_local;  // chain within the cluster (MMA row)
+  const int cg = c_base + cc;                    // global chain
+  const bool cvalid = owner && cg < a.C;
+  float z0r[kMaxEPT], g0r[kMaxEPT], zr[kMaxEPT], rr[kMaxEPT], gr[kMaxEPT];
+  double lj0 = 0.0, kin0 = 0.0;
+#pragma unroll
+  for (int i = 0; i < kMaxEPT; ++i) {
+    const int d = d0 + i;
+    const bool ok = cvalid && i < EPT && d < P;
+    z0r[i] = ok ? a.z[(size_t)cg * P + d] : 0.0f;
+    g0r[i] = (ok && a.cache_valid) ? a.grad[(size_t)cg * P + d] : 0.0f;
+    zr[i] = z0r[i];
+    rr[i] = 0.0f;
+    gr[i] = g0r[i];
+  }
+  if (cvalid && a.cache_valid) lj0 = a.lj[cg];
+  const int64_t t0 = *(volatile int64_t*)&a.state->t;
+  const float eps = a.step_size, half = 0.5f * a.step_size;
+  const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
+  const uint32_t gpart_addr = smem_u32(stage0);
+  const uint32_t llpart_addr = gpart_addr + 512u * PP;
+
+  // every CTA of the cluster must be running before any DSMEM access
+  cluster_sync();
+
+  const int L = a.n_steps;
+  const int E = (a.cache_valid ? 0 : 1) + a.n_iter * L;
+  uint32_t gt = 0;  // running tile counter (identical in every role)
+  for (int e = 0; e < E; ++e) {
+    const bool cache_eval = !a.cache_valid && e == 0;
+    const int ee = e - (a.cache_valid ? 0 : 1);
+    const int it = cache_eval ? 0 : ee / L;
+    const int l = cache_eval ? 0 : ee % L;
+    const bool need_ll = cache_eval || l == L - 1;
+    const int64_t t = t0 + it;
+    const uint32_t iter = (uint32_t)t;
+
+    // ================= pre phase: position for this evaluation, broadcast as Z
+    if (owner) {
+      if (!cache_eval) {
+        if (l == 0) {
+          double k = 0.0;
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) {
+            const int d = d0 + i;
+            float r = 0.0f;
+            if (cvalid && i < EPT && d < P)
+              r = a.r_ovr ? a.r_ovr[((size_t)it * a.C + cg) * P + d]
+                          : philox_normal(a.seed, 1u, iter, (uint32_t)cg, (uint32_t)d);
+            rr[i] = r;
+            zr[i] = z0r[i];
+            gr[i] = g0r[i];
+            k += (double)r * (double)r;
+          }
+          for (int o = (int)R >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+          kin0 = k;
+        }
+#pragma unroll
+        for (int i = 0; i < kMaxEPT; ++i) {
+          rr[i] = rr[i] + half * gr[i];
+          zr[i] = zr[i] + eps * rr[i];
+        }
+      }
+      // Z hi/lo into every CTA of the cluster (canonical K-major layout)
+#pragma unroll
+      for (int i = 0; i < kMaxEPT; i += 4) {
+        if (i < EPT) {
+          float h[4], lo4[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float v = zr[i + j];
+            h[j] = tf32_rna(v);
+            lo4[j] = tf32_rna(v - h[j]);
+          }
+          const uint32_t off = kmajor_off(cc, d0 + i, PP);
+          for (uint32_t q = 0; q < R; ++q) {
+            st_dsmem4(mapa(zhi_addr + off, q), make_float4(h[0], h[1], h[2], h[3]));
+            st_dsmem4(mapa(zlo_addr + off, q), make_float4(lo4[0], lo4[1], lo4[2], lo4[3]));
+          }
+        }
+      }
+      fence_proxy_async();
+    }
+    __syncwarp();
+    cluster_sync();  // Z ready in every CTA
+
+    // ================= gradient evaluation over this CTA's row tiles
+    if (warp == 0) {
+      if (lane == 0) {
+        for (int i = 0; i < nt; ++i) {
+          const uint32_t g = gt + i, s = g & 1u;
+          if (g >= 2) mbar_wait(bar_empty0 + 8 * s, ((g >> 1) - 1) & 1u, err);
+          mbar_expect_tx(bar_full0 + 8 * s, SB);
+          bulk_g2s(smem_u32(s ? stage1 : stage0), a.tiles + (size_t)(t_begin + i) * SB, SB,
+                   bar_full0 + 8 * s);
+        }
+      }
+      __syncwarp();
+    } else if (warp == 1) {
+      if (lane == 0) {
+        fence_proxy_async();
+        const uint32_t id_f = idesc_tf32(kCT, kNR);
+        const uint32_t id_b = idesc_tf32(kCT, PP);
+        const uint32_t sbo_k = 32u * PP, sbo_t = 32u * kNR;
+        for (int i = 0; i <= nt; ++i) {
+          if (i < nt) {
+            const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
+            mbar_wait(bar_full0 + 8 * s, (g >> 1) & 1u, err);
+            tc_fence_after();
+            const uint32_t st = smem_u32(s ? stage1 : stage0);
+            const uint32_t dt = tbase + COL_ETA(b);
+            for (int kk = 0; kk < PP / 8; ++kk) {
+              const uint32_t off = 256u * kk;
+              const uint64_t ah = sdesc(zhi_addr + off, 128, sbo_k);
+              const uint64_t al = sdesc(zlo_addr + off, 128, sbo_k);
+              const uint64_t bh = sdesc(st + off, 128, sbo_k);
+              const uint64_t bl = sdesc(st + 256u * PP + off, 128, sbo_k);
+              mma_ss(dt, ah, bh, id_f, kk > 0 ? 1u : 0u);
+              mma_ss(dt, ah, bl, id_f, 1u);
+              mma_ss(dt, al, bh, id_f, 1u);
+            }
+            mma_commit(bar_eta0 + 8 * b);
+          }
+          if (i >= 1) {
+            const int j = i - 1;
+            const uint32_t g = gt + j, s = g & 1u, b = g & 1u;
+            mbar_wait(bar_r0 + 8 * b, (g >> 1) & 1u, err);
+            tc_fence_after();
+            const uint32_t st = smem_u32(s ? stage1 : stage0);
+            for (int kk = 0; kk < kNR / 8; ++kk) {
+              const uint32_t off = 256u * kk;
+              const uint64_t bh = sdesc(st + 512u * PP + off, 128, sbo_t);
+              const uint64_t bl = sdesc(st + 768u * PP + off, 128, sbo_t);
+              const uint32_t ah = tbase + COL_RHI(b) + 8u * kk;
+              const uint32_t al = tbase + COL_RLO(b) + 8u * kk;
+              const uint32_t acc0 = (j == 0 && kk == 0) ? 0u : 1u;
+              mma_ts(tbase + col_G, ah, bh, id_b, acc0);
+              mma_ts(tbase + col_G, ah, bl, id_b, 1u);
+              mma_ts(tbase + col_G, al, bh, id_b, 1u);
+            }
+            mma_commit(bar_empty0 + 8 * s);
+          }
+        }
+        mma_commit(bar_G);
+      }
+      __syncwarp();
+    } else {
+      // epilogue: this thread's TMEM lane = chain row 32*(warp%4) + lane
+      const int q = warp & 3;
+      const int row = 32 * q + lane;
+      const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16);
+      Kahan kl;
+      for (int i = 0; i < nt; ++i) {
+        const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
+        mbar_wait(bar_eta0 + 8 * b, (g >> 1) & 1u, err);
+        tc_fence_after();
+        const float* yt = reinterpret_cast<const float*>((s ? stage1 : stage0) + 1024 * PP);
+        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR);
+#pragma unroll 1
+        for (int ch = 0; ch < kNR / 16; ++ch) {
+          float v[16], hi[16], lo[16];
+          tmem_ld16(tl + COL_ETA(b) + 16 * ch, v);
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int n = 16 * ch + k;
+            float r = 0.0f;
+            if (n < nvalid) {
+              const float yv = yt[n], eta = v[k];
+              if (a.lik == EDG_LIK_BERNOULLI) {
+                if (need_ll) {
+                  const float ex = expf(-fabsf(eta));
+                  const float sg = 1.0f / (1.0f + ex);
+                  r = yv - (eta >= 0.0f ? sg : ex * sg);
+                  kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
+                } else {
+                  r = yv - 1.0f / (1.0f + __expf(-eta));
+                }
+              } else {
+                const float diff = yv - eta;
+                r = diff * a.inv_lik_var;
+                if (need_ll) kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
+              }
+            }
+            hi[k] = tf32_rna(r);
+            lo[k] = tf32_rna(r - hi[k]);
+          }
+          tmem_st16(tl + COL_RHI(b) + 16 * ch, hi);
+          tmem_st16(tl + COL_RLO(b) + 16 * ch, lo);
+        }
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_r0 + 8 * b);
+      }
+      mbar_wait(bar_G, (uint32_t)e & 1u, err);
+      tc_fence_after();
+      float* Gpart = reinterpret_cast<float*>(stage0);
+      for (int ch = 0; ch < PP / 16; ++ch) {
+        float v[16];
+        tmem_ld16(tl + col_G + 16 * ch, v);
+        float4* dst = reinterpret_cast<float4*>(Gpart + row * PP + 16 * ch);
+        dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+        dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+        dst[2] = make_float4(v[8], v[9], v[10], v[11]);
+        dst[3] = make_float4(v[12], v[13], v[14], v[15]);
+      }
+      if (need_ll) reinterpret_cast<double*>(stage0 + 512 * PP)[row] = kl.value();
+      tc_fence_before();
+    }
+    gt += (uint32_t)nt;
+    __syncwarp();
+    cluster_sync();  // partial gradients of every CTA ready
+
+    // ================= post phase: reduce, leapfrog kick, Metropolis
+    if (owner) {
+      float G[kMaxEPT];
+#pragma unroll
+      for (int i = 0; i < kMaxEPT; ++i) G[i] = 0.0f;
+      for (uint32_t q = 0; q < R; ++q) {
+#pragma unroll
+        for (int i = 0; i < kMaxEPT; i += 4) {
+          if (i < EPT) {
+            const float4 v = ld_dsmem4(mapa(gpart_addr + 4u * (cc * PP + d0 + i), q));
+            G[i] += v.x;
+            G[i + 1] += v.y;
+            G[i + 2] += v.z;
+            G[i + 3] += v.w;
+          }
+        }
+      }
+      double llsum = 0.0;
+      if (need_ll)
+        for (uint32_t q = 0; q < R; ++q) llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * cc, q));
+      // prior: gradient and (when needed) FP64 log density of the evaluated position
+      double lp = 0.0;
+#pragma unroll
+      for (int i = 0; i < kMaxEPT; ++i) {
+        const int d = d0 + i;
+        if (i < EPT && d < P) {
+          const float sc = a.prior_scale[d];
+          const float zz = zr[i];
+          G[i] += -(zz - a.prior_loc[d]) / (sc * sc);
+          if (need_ll) {
+            const float u = (zz - a.prior_loc[d]) / sc;
+            lp += (double)(-0.5f * u * u - logf(sc)) - kHalfLog2Pi;
+          }
+        } else {
+          G[i] = 0.0f;
+        }
+      }
+      if (need_ll)
+        for (int o = (int)R >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
+      if (cache_eval) {
+#pragma unroll
+        for (int i = 0; i < kMaxEPT; ++i) g0r[i] = G[i];
+        lj0 = llsum + lp;
+      } else {
+#pragma unroll
+        for (int i = 0; i < kMaxEPT; ++i) {
+          gr[i] = G[i];
+          rr[i] = rr[i] + half * G[i];
+        }
+        if (l == L - 1) {
+          // Metropolis test in FP64 (hmc.py:100-109)
+          double k = 0.0;
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) k += (double)rr[i] * (double)rr[i];
+          for (int o = (int)R >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+          const double lj_new = llsum + lp;
+          const double ratio = 0.5 * kin0 - 0.5 * k + lj_new - lj0;
+          double u = 0.5;
+          if (cvalid)
+            u = a.u_ovr ? a.u_ovr[(size_t)it * a.C + cg]
+                        : u01d(philox_at(a.seed, 2u, iter, (uint32_t)cg, 0u).x);
+          const bool accept = log(u) < ratio;
+          if (accept) {
+#pragma unroll
+            for (int i = 0; i < kMaxEPT; ++i) {
+              z0r[i] = zr[i];
+              g0r[i] = gr[i];
+            }
+            lj0 = lj_new;
+          }
+          if (cvalid) {
+            if (part == 0) {
+              if (a.n_accept) a.n_accept[cg] += accept ? 1 : 0;
+              if (a.ratio_out) a.ratio_out[(size_t)it * a.C + cg] = ratio;
+            }
+#pragma unroll
+            for (int i = 0; i < kMaxEPT; ++i) {
+              const int d = d0 + i;
+              if (i < EPT && d < P) {
+                if (a.samples && t < a.T_cap)
+                  a.samples[((size_t)t * a.C + cg) * P + d] = z0r[i];
+                if (a.moments) {
+                  const size_t gi = (size_t)cg * P + d;
+                  a.moments[gi] += (double)z0r[i];
+                  a.moments[(size_t)a.C * P + gi] += (double)z0r[i] * (double)z0r[i];
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // ---- write back the chain state and its cached gradient / log joint
+  if (cvalid) {
+#pragma unroll
+    for (int i = 0; i < kMaxEPT; ++i) {
+      const int d = d0 + i;
+      if (i < EPT && d < P) {
+        a.z[(size_t)cg * P + d] = z0r[i];
+        a.grad[(size_t)cg * P + d] = g0r[i];
+      }
+    }
+    if (part == 0) a.lj[cg] = lj0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(kTmemCols));
+  }
+  cluster_sync();  // no CTA leaves while a peer may still read its shared memory
+  if (threadIdx.x == 0) {
+    if (*err) atomicExch(&a.state->error, (uint32_t)(-EDG_E_TIMEOUT));
+    __threadfence();
+    const unsigned prev = atomicAdd(&a.state->done, 1u);
+    s_last = (prev == gridDim.x - 1);
+    if (s_last) {
+      a.state->t = t0 + a.n_iter;
+      a.state->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static int padded_P(int P) { return round_up(std::max(P, 16), 16); }
+
+// Dynamic shared memory: at least 120 KB so that no two CTAs share an SM
+// (each allocates all 512 TMEM columns; a second resident CTA would block in
+// tcgen05.alloc while its cluster waits on it).
+static size_t smem_bytes(int PP) {
+  return std::max<size_t>(2 * (size_t)stage_bytes(PP) + (size_t)1024 * PP + 256, 120 * 1024);
+}
+
+static int sm_count() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v > 0 ? v : 1;
+}
+
+// Cluster size: a power of two R <= 8 with R <= ntiles, PP/R <= 16,
+// (PP/R) % 4 == 0, and clusters * R close to the SM count.
+static int choose_R(int PP, int C, int ntiles, int want) {
+  const int nclusters = (C + kCT - 1) / kCT;
+  int best = 0;
+  for (int R = 1; R <= 8; R <<= 1) {
+    if (PP / R > kMaxEPT || (PP / R) % 4 != 0 || PP % R != 0 || R > ntiles) continue;
+    if (want > 0) {
+      if (R == want) return R;
+      continue;
+    }
+    if (nclusters * R <= sm_count() || best == 0) best = R;
+  }
+  return best;
+}
+
+}  // namespace tc
+}  // namespace edg
+
+using namespace edg;
+using namespace edg::tc;
+
+extern "C" size_t edg_hmc_glm_tc_tiles_bytes(const edg_glm_t* model) {
+  GLMDev m;
+  if (make_glm(model, &m) != EDG_OK) return 0;
+  const int PP = padded_P(m.P);
+  if (PP > 64) return 0;
+  const int ntiles = (m.N + kNR - 1) / kNR;
+  return (size_t)ntiles * stage_bytes(PP);
+}
+
+extern "C" int edg_hmc_glm_tc_prepare(const edg_glm_t* model, void* tiles, size_t tiles_bytes,
+                                      void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  const int PP = padded_P(m.P);
+  EDG_REQUIRE(PP <= 64, EDG_E_UNSUPPORTED, "tensor-core HMC supports P <= 64 (got %d)", m.P);
+  const int ntiles = (m.N + kNR - 1) / kNR;
+  const size_t need = (size_t)ntiles * stage_bytes(PP);
+  EDG_REQUIRE(tiles && tiles_bytes >= need, EDG_E_WORKSPACE, "tiles buffer of %zu bytes needed",
+              need);
+  const int64_t total = (int64_t)ntiles * kNR * PP;
+  prep_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      m.X, m.y, m.N, m.D, m.bias, PP, ntiles, reinterpret_cast<unsigned char*>(tiles));
+  return check_launch("prep_tiles_kernel");
+}
+
+extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C,
+                                  int32_t n_iter, const void* tiles, float* z, float* grad,
+                                  double* lj, int32_t cache_valid, int32_t* n_accept,
+                                  edg_state_t* state, float* samples, int64_t T_cap,
+                                  double* moments, const float* r_override,
+                                  const double* u_override, double* ratio_out, void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(cfg && tiles, EDG_E_NULL, "cfg and tiles must not be NULL");
+  EDG_REQUIRE(z && grad && lj && state, EDG_E_NULL, "z, grad, lj and state must not be NULL");
+  EDG_REQUIRE(C > 0 && n_iter >= 0, EDG_E_SHAPE, "C must be positive and n_iter >= 0");
+  EDG_REQUIRE(cfg->n_steps > 0, EDG_E_UNSUPPORTED,
+              "tensor-core HMC needs n_steps > 0 (use edg_hmc_glm_run)");
+  EDG_REQUIRE(!samples || T_cap > 0, EDG_E_SHAPE, "T_cap must be positive when samples is given");
+  const int PP = padded_P(m.P);
+  EDG_REQUIRE(PP <= 64, EDG_E_UNSUPPORTED, "tensor-core HMC supports P <= 64 (got %d)", m.P);
+  if (n_iter == 0 && cache_valid) return EDG_OK;
+  const int ntiles = (m.N + kNR - 1) / kNR;
+  const int R = choose_R(PP, C, ntiles, cfg->cluster_size);
+  EDG_REQUIRE(R > 0, EDG_E_UNSUPPORTED,
+              "no cluster size fits P=%d with %d row tiles (requested %d)", m.P, ntiles,
+              cfg->cluster_size);
+  TcArgs a;
+  a.tiles = reinterpret_cast<const unsigned char*>(tiles);
+  a.ntiles = ntiles;
+  a.N = m.N;
+  a.P = m.P;
+  a.PP = PP;
+  a.lik = m.lik;
+  a.inv_lik_var = m.inv_lik_var;
+  a.lik_norm = m.lik_norm;
+  a.prior_loc = m.prior_loc;
+  a.prior_scale = m.prior_scale;
+  a.C = C;
+  a.n_iter = n_iter;
+  a.n_steps = cfg->n_steps;
+  a.cache_valid = cache_valid;
+  a.step_size = cfg->step_size;
+  a.seed = cfg->seed;
+  a.z = z;
+  a.grad = grad;
+  a.lj = lj;
+  a.n_accept = n_accept;
+  a.state = state;
+  a.samples = samples;
+  a.T_cap = T_cap;
+  a.moments = moments;
+  a.r_ovr = r_override;
+  a.u_ovr = u_override;
+  a.ratio_out = ratio_out;
+  const size_t sm = smem_bytes(PP);
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(hmc_glm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_bytes(64));
+    attr_done = true;
+  }
+  const int nclusters = (C + kCT - 1) / kCT;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(nclusters * R);
+  lc.blockDim = dim3(kThreads);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = (cudaStream_t)stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = R;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&lc, hmc_glm_tc_kernel, a);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "hmc_glm_tc_kernel launch: %s", cudaGetErrorString(e));
+  return check_launch("hmc_glm_tc_kernel");
+}

@@ -21,12 +21,20 @@ from .monte_carlo import MonteCarlo
 
 
 class HMC(MonteCarlo):
-    def initialize(self, step_size=0.25, n_steps=2, chains_per_block=0, *args, **kwargs):
-        """``step_size`` / ``n_steps`` as in ``hmc.py:45-59``;
-        ``chains_per_block`` 0 = autotuned."""
+    def initialize(self, step_size=0.25, n_steps=2, engine="auto", chains_per_block=0,
+                   cluster_size=0, *args, **kwargs):
+        """``step_size`` / ``n_steps`` as in ``hmc.py:45-59``.
+
+        engine: "tc" (tcgen05 tensor cores, P <= 64), "simt" (CUDA cores) or
+        "auto" (autotuned between them); ``chains_per_block`` (SIMT) and
+        ``cluster_size`` (tensor cores) pin a launch shape, 0 = autotuned."""
+        if engine not in ("auto", "tc", "simt"):
+            raise ValueError("engine must be 'auto', 'tc' or 'simt'")
         self.step_size = step_size
         self.n_steps = n_steps
+        self._engine_req = engine
         self._cpb = chains_per_block
+        self._cluster = cluster_size
         return super().initialize(*args, **kwargs)
 
     def _validate(self):
@@ -75,38 +83,84 @@ class HMC(MonteCarlo):
         cfg.n_steps = int(self.n_steps)
         cfg.seed = next_seed()
         cfg.chains_per_block = int(self._cpb)
+        cfg.cluster_size = int(self._cluster)
         self._cfg = cfg
-        if cfg.chains_per_block == 0:
-            cfg.chains_per_block = self._autotune()
+        self._tiles = None
+        tc_ok = spec.P <= 64 and self.n_steps > 0
+        if self._engine_req == "tc" and not tc_ok:
+            raise NotImplementedError("the tensor-core engine needs P <= 64 and n_steps > 0")
+        if tc_ok and self._engine_req in ("auto", "tc"):
+            lib = _lib.load()
+            nbytes = lib.edg_hmc_glm_tc_tiles_bytes(self._glm.ref())
+            self._tiles = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+            _lib.call("edg_hmc_glm_tc_prepare", self._glm.ref(), _lib.ptr(self._tiles), nbytes,
+                      _lib.stream_ptr())
+        if self._engine_req == "tc":
+            self.engine = "tc"
+        elif self._engine_req == "simt" or self._tiles is None:
+            self.engine = "simt"
+        else:
+            self.engine = None
+        if self.engine is None or (self.engine == "simt" and cfg.chains_per_block == 0):
+            best = self._autotune()
+            if best == "tc":
+                self.engine = "tc"
+            else:
+                self.engine = "simt"
+                cfg.chains_per_block = int(best)
         self.train = self.update
         return self.train
 
     def _autotune(self):
-        C, P = self.C, self._spec.P
+        C = self.C
         z = self._z.clone()
         g = torch.zeros_like(self._g)
         lj = torch.zeros_like(self._lj)
         st = _lib.new_state(self._device)
-        cands = [8, 16, 32] if C > 8 else [8]
+        cands = ([8, 16, 32] if C > 8 else [8]) if self._engine_req != "tc" else []
+        if self._tiles is not None and self._engine_req != "simt":
+            cands = ["tc"] + cands
 
-        def run(ct):
+        def run(c):
             cfg = _lib.EdgHMC()
             cfg.step_size, cfg.n_steps, cfg.seed = self._cfg.step_size, self._cfg.n_steps, 1
-            cfg.chains_per_block = ct
-            _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(cfg), C, 1,
-                      _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st),
-                      None, 0, None, None, None, None, _lib.stream_ptr())
+            cfg.cluster_size = self._cfg.cluster_size
+            z.copy_(self._z)
+            if c == "tc":
+                _lib.call("edg_hmc_glm_tc_run", self._glm.ref(), ctypes.byref(cfg), C, 1,
+                          _lib.ptr(self._tiles), _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None,
+                          _lib.ptr(st), None, 0, None, None, None, None, _lib.stream_ptr())
+            else:
+                cfg.chains_per_block = c
+                _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(cfg), C, 1,
+                          _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st),
+                          None, 0, None, None, None, None, _lib.stream_ptr())
 
         key = f"N{self._spec.N}_D{self._spec.D}_b{int(self._spec.bias)}_C{C}_L{self.n_steps}"
         return autotune.choose("hmc_glm", key, cands, run)
 
     def _launch(self, n_iter, r_override=None, u_override=None, ratio_out=None):
-        _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C, int(n_iter),
-                  _lib.ptr(self._z), _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
-                  _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
-                  self._samples.shape[0], None, _lib.ptr(r_override), _lib.ptr(u_override),
-                  _lib.ptr(ratio_out), _lib.stream_ptr())
+        if self.engine == "tc":
+            _lib.call("edg_hmc_glm_tc_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(self._tiles), _lib.ptr(self._z), _lib.ptr(self._g),
+                      _lib.ptr(self._lj), self._cache_valid, _lib.ptr(self._n_accept),
+                      _lib.ptr(self._state), _lib.ptr(self._samples), self._samples.shape[0],
+                      None, _lib.ptr(r_override), _lib.ptr(u_override), _lib.ptr(ratio_out),
+                      _lib.stream_ptr())
+        else:
+            _lib.call("edg_hmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(self._z), _lib.ptr(self._g), _lib.ptr(self._lj),
+                      self._cache_valid, _lib.ptr(self._n_accept), _lib.ptr(self._state),
+                      _lib.ptr(self._samples), self._samples.shape[0], None,
+                      _lib.ptr(r_override), _lib.ptr(u_override), _lib.ptr(ratio_out),
+                      _lib.stream_ptr())
         self._cache_valid = 1
+
+    def check_errors(self):
+        """Raises if a kernel recorded a bounded-wait timeout (reads the device state)."""
+        st = self._read_state()
+        if st.error:
+            raise TimeoutError("an HMC kernel gave up a bounded device-side wait")
 
     def update(self, feed_dict=None):
         """One HMC iteration for every chain; returns ``{'t', 'accept_rate'}``

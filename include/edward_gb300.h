@@ -90,8 +90,10 @@ typedef struct {
   float beta2_power;
   uint32_t done;         /* internal completion counter; 0 between calls */
   uint32_t nonfinite;    /* non-finite loss/gradient values seen */
+  uint32_t error;        /* EDG_E_* of a kernel that gave up a bounded wait (0 = none) */
+  uint32_t reserved;
   double loss;           /* loss of the last KLqp update */
-  double aux[4];         /* estimator-specific diagnostics */
+  double aux[3];         /* estimator-specific diagnostics */
 } edg_state_t;
 
 /* Optimizer + learning-rate schedule.  lr = lr0 * decay_rate^(step/decay_steps)
@@ -124,7 +126,8 @@ typedef struct {
   float step_size;
   int32_t n_steps;
   uint64_t seed;
-  int32_t chains_per_block; /* 0 = library default; else 8, 16 or 32 */
+  int32_t chains_per_block; /* SIMT engine: 0 = library default; else 8, 16 or 32 */
+  int32_t cluster_size;     /* tensor-core engine: CTAs per 128 chains (1,2,4,8); 0 = auto */
 } edg_hmc_t;
 
 /* ---------------------------------------------------------------- library */
@@ -193,6 +196,23 @@ int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, int
                     float* samples, int64_t T_cap, double* moments,
                     const float* r_override, const double* u_override, double* ratio_out,
                     void* stream);
+
+/* ---------------------------------------------------------------- HMC, tensor cores
+ * Same contract as edg_hmc_glm_run, computed with tcgen05 3xTF32 GEMMs:
+ * one thread-block cluster per 128 chains, the cluster's CTAs splitting the
+ * rows of X and reducing each leapfrog gradient through distributed shared
+ * memory.  Requires P = D + bias <= 64 and n_steps > 0.  `tiles` is the
+ * model's X re-laid into 64-row operand tiles by edg_hmc_glm_tc_prepare
+ * (once per model; edg_hmc_glm_tc_tiles_bytes gives its size).
+ * Replaces the same reference code as edg_hmc_glm_run (hmc.py:61-130,195-210;
+ * monte_carlo.py:111-150). */
+size_t edg_hmc_glm_tc_tiles_bytes(const edg_glm_t* model);
+int edg_hmc_glm_tc_prepare(const edg_glm_t* model, void* tiles, size_t tiles_bytes, void* stream);
+int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
+                       const void* tiles, float* z, float* grad, double* lj, int32_t cache_valid,
+                       int32_t* n_accept, edg_state_t* state, float* samples, int64_t T_cap,
+                       double* moments, const float* r_override, const double* u_override,
+                       double* ratio_out, void* stream);
 
 #ifdef __cplusplus
 }
