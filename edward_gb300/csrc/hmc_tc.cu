@@ -270,8 +270,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   unsigned char* stage1 = smem + SB;
   float* Zhi = reinterpret_cast<float*>(smem + 2 * SB);
   float* Zlo = Zhi + kCT * PP;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(Zlo + kCT * PP);
-  // bars: full[2] empty[2] eta[2] r[2] G[1]
+  float* Gsum = Zlo + kCT * PP;  // [128][PP] this CTA's gradient partial (FP32, round-to-nearest)
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Gsum + kCT * PP);
+  // bars: full[2] empty[2] eta[2] r[2] gfull[2] gfree[2]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 12);
   volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
   __shared__ bool s_last;
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 
   const uint32_t bar_full0 = smem_u32(bars + 0), bar_empty0 = smem_u32(bars + 2);
   const uint32_t bar_eta0 = smem_u32(bars + 4), bar_r0 = smem_u32(bars + 6);
-  const uint32_t bar_G = smem_u32(bars + 8);
+  const uint32_t bar_gfull0 = smem_u32(bars + 8), bar_gfree0 = smem_u32(bars + 10);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -294,8 +295,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       mbar_init(bar_empty0 + 8 * i, 1);
       mbar_init(bar_eta0 + 8 * i, 1);
       mbar_init(bar_r0 + 8 * i, 4);
+      mbar_init(bar_gfull0 + 8 * i, 1);
+      mbar_init(bar_gfree0 + 8 * i, 4);
     }
-    mbar_init(bar_G, 1);
     *err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -309,11 +311,14 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = *tmem_slot;
-  // TMEM columns: G [0, 64); per buffer b: eta, r_hi, r_lo at 64 + 192 b + {0, 64, 128}
-  const uint32_t col_G = 0;
-#define COL_ETA(b) (64u + 192u * (b))
-#define COL_RHI(b) (128u + 192u * (b))
-#define COL_RLO(b) (192u + 192u * (b))
+  // TMEM columns, per buffer b: eta, r_hi, r_lo at 192 b + {0, 64, 128}; the
+  // per-tile gradient partial at 384 + 64 b.  The tensor core accumulates with
+  // truncation, so G is accumulated per tile in TMEM (24 MMAs) and summed
+  // across tiles in FP32 registers / shared memory with round-to-nearest.
+#define COL_ETA(b) (192u * (b))
+#define COL_RHI(b) (64u + 192u * (b))
+#define COL_RLO(b) (128u + 192u * (b))
+#define COL_GP(b) (384u + 64u * (b))
 
   // ---- owner mapping (warps 2-5): R threads per chain, EPT elements each
   const bool owner = warp >= 2;
@@ -342,8 +347,8 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const int64_t t0 = *(volatile int64_t*)&a.state->t;
   const float eps = a.step_size, half = 0.5f * a.step_size;
   const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
-  const uint32_t gpart_addr = smem_u32(stage0);
-  const uint32_t llpart_addr = gpart_addr + 512u * PP;
+  const uint32_t gpart_addr = smem_u32(Gsum);
+  const uint32_t llpart_addr = smem_u32(stage0);
 
   // every CTA of the cluster must be running before any DSMEM access
   cluster_sync();
@@ -434,15 +439,20 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             tc_fence_after();
             const uint32_t st = smem_u32(s ? stage1 : stage0);
             const uint32_t dt = tbase + COL_ETA(b);
+            // lo products first (small running sum), hi*hi last: fewer
+            // truncating additions land on a large accumulator
             for (int kk = 0; kk < PP / 8; ++kk) {
               const uint32_t off = 256u * kk;
               const uint64_t ah = sdesc(zhi_addr + off, 128, sbo_k);
               const uint64_t al = sdesc(zlo_addr + off, 128, sbo_k);
               const uint64_t bh = sdesc(st + off, 128, sbo_k);
               const uint64_t bl = sdesc(st + 256u * PP + off, 128, sbo_k);
-              mma_ss(dt, ah, bh, id_f, kk > 0 ? 1u : 0u);
-              mma_ss(dt, ah, bl, id_f, 1u);
+              mma_ss(dt, ah, bl, id_f, kk > 0 ? 1u : 0u);
               mma_ss(dt, al, bh, id_f, 1u);
+            }
+            for (int kk = 0; kk < PP / 8; ++kk) {
+              const uint32_t off = 256u * kk;
+              mma_ss(dt, sdesc(zhi_addr + off, 128, sbo_k), sdesc(st + off, 128, sbo_k), id_f, 1u);
             }
             mma_commit(bar_eta0 + 8 * b);
           }
@@ -450,23 +460,26 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             const int j = i - 1;
             const uint32_t g = gt + j, s = g & 1u, b = g & 1u;
             mbar_wait(bar_r0 + 8 * b, (g >> 1) & 1u, err);
+            if (g >= 2) mbar_wait(bar_gfree0 + 8 * b, ((g >> 1) - 1) & 1u, err);
             tc_fence_after();
             const uint32_t st = smem_u32(s ? stage1 : stage0);
+            const uint32_t dg = tbase + COL_GP(b);
             for (int kk = 0; kk < kNR / 8; ++kk) {
               const uint32_t off = 256u * kk;
               const uint64_t bh = sdesc(st + 512u * PP + off, 128, sbo_t);
               const uint64_t bl = sdesc(st + 768u * PP + off, 128, sbo_t);
-              const uint32_t ah = tbase + COL_RHI(b) + 8u * kk;
-              const uint32_t al = tbase + COL_RLO(b) + 8u * kk;
-              const uint32_t acc0 = (j == 0 && kk == 0) ? 0u : 1u;
-              mma_ts(tbase + col_G, ah, bh, id_b, acc0);
-              mma_ts(tbase + col_G, ah, bl, id_b, 1u);
-              mma_ts(tbase + col_G, al, bh, id_b, 1u);
+              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, bl, id_b, kk > 0 ? 1u : 0u);
+              mma_ts(dg, tbase + COL_RLO(b) + 8u * kk, bh, id_b, 1u);
+            }
+            for (int kk = 0; kk < kNR / 8; ++kk) {
+              const uint32_t off = 256u * kk;
+              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + 512u * PP + off, 128, sbo_t),
+                     id_b, 1u);
             }
             mma_commit(bar_empty0 + 8 * s);
+            mma_commit(bar_gfull0 + 8 * b);
           }
         }
-        mma_commit(bar_G);
       }
       __syncwarp();
     } else {
@@ -475,6 +488,29 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       const int row = 32 * q + lane;
       const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16);
       Kahan kl;
+      float4* grow = reinterpret_cast<float4*>(Gsum + row * PP);
+      // adds the per-tile gradient partial of tile i (TMEM) into Gsum[row]
+      auto consume_gpart = [&](int i) {
+        const uint32_t g = gt + i, b = g & 1u;
+        mbar_wait(bar_gfull0 + 8 * b, (g >> 1) & 1u, err);
+        tc_fence_after();
+        for (int ch = 0; ch < PP / 16; ++ch) {
+          float v[16];
+          tmem_ld16(tl + COL_GP(b) + 16 * ch, v);
+#pragma unroll
+          for (int k4 = 0; k4 < 4; ++k4) {
+            float4 acc = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : grow[4 * ch + k4];
+            acc.x += v[4 * k4 + 0];
+            acc.y += v[4 * k4 + 1];
+            acc.z += v[4 * k4 + 2];
+            acc.w += v[4 * k4 + 3];
+            grow[4 * ch + k4] = acc;
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_gfree0 + 8 * b);
+      };
       for (int i = 0; i < nt; ++i) {
         const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
         mbar_wait(bar_eta0 + 8 * b, (g >> 1) & 1u, err);
@@ -516,20 +552,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(bar_r0 + 8 * b);
+        if (i >= 1) consume_gpart(i - 1);
       }
-      mbar_wait(bar_G, (uint32_t)e & 1u, err);
-      tc_fence_after();
-      float* Gpart = reinterpret_cast<float*>(stage0);
-      for (int ch = 0; ch < PP / 16; ++ch) {
-        float v[16];
-        tmem_ld16(tl + col_G + 16 * ch, v);
-        float4* dst = reinterpret_cast<float4*>(Gpart + row * PP + 16 * ch);
-        dst[0] = make_float4(v[0], v[1], v[2], v[3]);
-        dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-        dst[2] = make_float4(v[8], v[9], v[10], v[11]);
-        dst[3] = make_float4(v[12], v[13], v[14], v[15]);
-      }
-      if (need_ll) reinterpret_cast<double*>(stage0 + 512 * PP)[row] = kl.value();
+      consume_gpart(nt - 1);
+      if (need_ll) reinterpret_cast<double*>(stage0)[row] = kl.value();
       tc_fence_before();
     }
     gt += (uint32_t)nt;
@@ -670,7 +696,7 @@ static int padded_P(int P) { return round_up(std::max(P, 16), 16); }
 // (each allocates all 512 TMEM columns; a second resident CTA would block in
 // tcgen05.alloc while its cluster waits on it).
 static size_t smem_bytes(int PP) {
-  return std::max<size_t>(2 * (size_t)stage_bytes(PP) + (size_t)1024 * PP + 256, 120 * 1024);
+  return std::max<size_t>(2 * (size_t)stage_bytes(PP) + (size_t)1536 * PP + 256, 120 * 1024);
 }
 
 static int sm_count() {
