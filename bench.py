@@ -201,8 +201,11 @@ def run_gpu(args):
     qw = Empirical(ed.Variable(qw_init, trainable=False), n_chains=N_CHAINS)
     qb = Empirical(ed.Variable(qb_init, trainable=False), n_chains=N_CHAINS)
     inf = ed.HMC({w: qw, b: qb}, data={yrv: y}, n_chains=N_CHAINS)
-    inf.initialize(step_size=STEP, n_steps=N_LEAP, n_print=0, chains_per_block=args.ct)
-    ct = inf._cfg.chains_per_block
+    inf.initialize(step_size=STEP, n_steps=N_LEAP, n_print=0, engine=args.engine,
+                   chains_per_block=args.ct)
+    kernel_name = ("hmc_glm_tc_kernel (tcgen05 3xTF32, one CTA cluster per 128 chains)"
+                   if inf.engine == "tc"
+                   else "hmc_glm_kernel<%d> (SIMT FP32)" % inf._cfg.chains_per_block)
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
@@ -258,8 +261,8 @@ def run_gpu(args):
         src = "fallback 1.9 PFLOP/s bf16"
     peak = bf16 / 2.0 / 3.0
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": read_traffic(),
-            "kernel": f"hmc_glm_kernel<{ct}>",
+            "frac": achieved / peak, "traffic": read_traffic(inf.engine),
+            "kernel": kernel_name,
             "peak_source": f"{src} {bf16:g} / 2 (TF32 rate) / 3 (3xTF32 passes), of measured",
             "algorithmic_flops_per_launch": flops_per_launch}
 
@@ -270,7 +273,7 @@ def run_gpu(args):
                 "dtype": "f32", "data": "synthetic",
                 "config": dict(CONFIG, parallelism=f"replicas{world}",
                                l2_flush="256 MB write before each step, outside the timed events",
-                               chains_per_block=ct, accept_rate=round(acc, 4)),
+                               engine=inf.engine, accept_rate=round(acc, 4)),
                 "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "wall_s_timed_region": wall}
@@ -343,10 +346,12 @@ def run_e2e(args, inf, X, y, z0, dev):
             "path": "edg_hmc_glm_run (C ABI) with pinned host buffers, wall clock"}
 
 
-def read_traffic():
+def read_traffic(engine):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (a line 'dram_bytes_per_launch: <int>'), else None."""
-    p = os.path.join(ROOT, "profiles", "hmc_glm_kernel_logreg_C4096.txt")
+    name = "hmc_glm_tc_kernel_logreg_C4096.txt" if engine == "tc" else \
+        "hmc_glm_kernel_logreg_C4096.txt"
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             for line in f:
@@ -363,7 +368,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ct", type=int, default=0, help="chains per block (0 = autotune)")
+    ap.add_argument("--ct", type=int, default=0, help="SIMT chains per block (0 = autotune)")
+    ap.add_argument("--engine", default="auto", choices=["auto", "tc", "simt"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
