@@ -17,8 +17,8 @@
 //     K-major shared-memory layout (hi, lo, transposed hi, transposed lo, y),
 //     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
 //
-// Warp roles (192 threads): warp 0 bulk-copy producer, warp 1 MMA issuer and
-// TMEM owner, warps 2-5 epilogue; between gradient evaluations warps 2-5 are
+// Warp roles (320 threads): warp 0 bulk-copy producers, warp 1 MMA issuer and
+// TMEM owner, warps 2-9 epilogue; between gradient evaluations warps 2-9 are
 // the "owners" that run the leapfrog / Metropolis arithmetic for this CTA's
 // share of the cluster's chains, with the chain state in registers.
 //
@@ -35,7 +35,7 @@ namespace tc {
 
 constexpr int kCT = 128;        // chains per cluster = MMA M
 constexpr int kNR = 64;         // rows per X tile = forward N = backward K
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;  // 2 control warps + 8 epilogue warps
 constexpr uint32_t kTmemCols = 512;
 
 __host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP + 256u; }
@@ -260,20 +260,62 @@ struct TcArgs {
   double* ratio_out;
 };
 
-constexpr int kMaxEPT = 16;  // chain-state elements per owner thread
+constexpr int kMaxEPT = 8;  // chain-state elements per owner thread
+constexpr int kEpiWarps = 8;
+
+// 32x32b.x16 twice (32 consecutive columns) with a single wait.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr), "r"(taddr + 16u)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Residual of one (row, chain): d log p(y | eta) / d eta.  The accurate form
+// (expf / log1pf) is used when the log-likelihood is also needed.
+__device__ __forceinline__ float residual_fast(int lik, float y, float eta, float inv_var) {
+  if (lik == EDG_LIK_BERNOULLI) {
+    const float e = __expf(-fminf(fmaxf(eta, -80.0f), 80.0f));
+    return y - __fdividef(1.0f, 1.0f + e);
+  }
+  return (y - eta) * inv_var;
+}
 
 __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int PP = a.PP, P = a.P;
   const uint32_t SB = stage_bytes(PP);
+  const uint32_t XB = 512u * PP;      // forward part of a tile: X hi, X lo
+  const uint32_t TB = SB - XB;        // backward part: X^T hi, X^T lo, y
   unsigned char* stage0 = smem;
   unsigned char* stage1 = smem + SB;
   float* Zhi = reinterpret_cast<float*>(smem + 2 * SB);
   float* Zlo = Zhi + kCT * PP;
-  float* Gsum = Zlo + kCT * PP;  // [128][PP] this CTA's gradient partial (FP32, round-to-nearest)
-  uint64_t* bars = reinterpret_cast<uint64_t*>(Gsum + kCT * PP);
-  // bars: full[2] empty[2] eta[2] r[2] gfull[2] gfree[2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 12);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Zlo + kCT * PP);
+  // bars: fullx[2] fullt[2] emptyx[2] emptyt[2] eta[2] r[2] gfull[2] gfree[2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 16);
   volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
   __shared__ bool s_last;
 
@@ -285,18 +327,21 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const int t_end = (int)((int64_t)a.ntiles * (rank + 1) / R);
   const int nt = t_end - t_begin;
 
-  const uint32_t bar_full0 = smem_u32(bars + 0), bar_empty0 = smem_u32(bars + 2);
-  const uint32_t bar_eta0 = smem_u32(bars + 4), bar_r0 = smem_u32(bars + 6);
-  const uint32_t bar_gfull0 = smem_u32(bars + 8), bar_gfree0 = smem_u32(bars + 10);
+  const uint32_t b_fullx = smem_u32(bars + 0), b_fullt = smem_u32(bars + 2);
+  const uint32_t b_emptyx = smem_u32(bars + 4), b_emptyt = smem_u32(bars + 6);
+  const uint32_t b_eta = smem_u32(bars + 8), b_r = smem_u32(bars + 10);
+  const uint32_t b_gfull = smem_u32(bars + 12), b_gfree = smem_u32(bars + 14);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
-      mbar_init(bar_full0 + 8 * i, 1);
-      mbar_init(bar_empty0 + 8 * i, 1);
-      mbar_init(bar_eta0 + 8 * i, 1);
-      mbar_init(bar_r0 + 8 * i, 4);
-      mbar_init(bar_gfull0 + 8 * i, 1);
-      mbar_init(bar_gfree0 + 8 * i, 4);
+      mbar_init(b_fullx + 8 * i, 1);
+      mbar_init(b_fullt + 8 * i, 1);
+      mbar_init(b_emptyx + 8 * i, 1);
+      mbar_init(b_emptyt + 8 * i, 1);
+      mbar_init(b_eta + 8 * i, 1);
+      mbar_init(b_r + 8 * i, kEpiWarps);
+      mbar_init(b_gfull + 8 * i, 1);
+      mbar_init(b_gfree + 8 * i, kEpiWarps);
     }
     *err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -314,19 +359,20 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   // TMEM columns, per buffer b: eta, r_hi, r_lo at 192 b + {0, 64, 128}; the
   // per-tile gradient partial at 384 + 64 b.  The tensor core accumulates with
   // truncation, so G is accumulated per tile in TMEM (24 MMAs) and summed
-  // across tiles in FP32 registers / shared memory with round-to-nearest.
+  // across tiles in FP32 registers with round-to-nearest.
 #define COL_ETA(b) (192u * (b))
 #define COL_RHI(b) (64u + 192u * (b))
 #define COL_RLO(b) (128u + 192u * (b))
 #define COL_GP(b) (384u + 64u * (b))
 
-  // ---- owner mapping (warps 2-5): R threads per chain, EPT elements each
+  // ---- owner mapping (warps 2-9, 256 threads): 2R threads per chain
   const bool owner = warp >= 2;
   const int et = threadIdx.x - 64;
+  const int TPC = 2 * (int)R;
   const int CPO = kCT / (int)R;
-  const int EPT = PP / (int)R;
-  const int chain_local = owner ? et / (int)R : 0;
-  const int part = owner ? et % (int)R : 0;
+  const int EPT = PP / TPC;
+  const int chain_local = owner ? et / TPC : 0;
+  const int part = owner ? et % TPC : 0;
   const int d0 = part * EPT;
   const int cc = (int)rank * CPO + chain_local;  // chain within the cluster (MMA row)
   const int cg = c_base + cc;                    // global chain
@@ -347,8 +393,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const int64_t t0 = *(volatile int64_t*)&a.state->t;
   const float eps = a.step_size, half = 0.5f * a.step_size;
   const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
-  const uint32_t gpart_addr = smem_u32(Gsum);
-  const uint32_t llpart_addr = smem_u32(stage0);
+  // end-of-evaluation exchange buffers (alias stage 0, idle between evaluations)
+  float* Gsum = reinterpret_cast<float*>(stage0);                   // [128][PP]
+  double* llpart = reinterpret_cast<double*>(stage0 + 512 * PP);    // [2][128]
+  const uint32_t gsum_addr = smem_u32(Gsum), llpart_addr = smem_u32(llpart);
 
   // every CTA of the cluster must be running before any DSMEM access
   cluster_sync();
@@ -382,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             gr[i] = g0r[i];
             k += (double)r * (double)r;
           }
-          for (int o = (int)R >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+          for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
           kin0 = k;
         }
 #pragma unroll
@@ -416,13 +464,19 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 
     // ================= gradient evaluation over this CTA's row tiles
     if (warp == 0) {
-      if (lane == 0) {
+      // lane 0 streams the forward parts (X hi/lo), lane 1 the backward parts
+      // (X^T hi/lo, y); each part is one bulk copy into a double buffer
+      if (lane < 2) {
+        const uint32_t part_off = lane == 0 ? 0u : XB;
+        const uint32_t bytes = lane == 0 ? XB : TB;
+        const uint32_t full = lane == 0 ? b_fullx : b_fullt;
+        const uint32_t empty = lane == 0 ? b_emptyx : b_emptyt;
         for (int i = 0; i < nt; ++i) {
           const uint32_t g = gt + i, s = g & 1u;
-          if (g >= 2) mbar_wait(bar_empty0 + 8 * s, ((g >> 1) - 1) & 1u, err);
-          mbar_expect_tx(bar_full0 + 8 * s, SB);
-          bulk_g2s(smem_u32(s ? stage1 : stage0), a.tiles + (size_t)(t_begin + i) * SB, SB,
-                   bar_full0 + 8 * s);
+          if (g >= 2) mbar_wait(empty + 8 * s, ((g >> 1) - 1) & 1u, err);
+          mbar_expect_tx(full + 8 * s, bytes);
+          bulk_g2s(smem_u32((s ? stage1 : stage0) + part_off),
+                   a.tiles + (size_t)(t_begin + i) * SB + part_off, bytes, full + 8 * s);
         }
       }
       __syncwarp();
@@ -435,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         for (int i = 0; i <= nt; ++i) {
           if (i < nt) {
             const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
-            mbar_wait(bar_full0 + 8 * s, (g >> 1) & 1u, err);
+            mbar_wait(b_fullx + 8 * s, (g >> 1) & 1u, err);
             tc_fence_after();
             const uint32_t st = smem_u32(s ? stage1 : stage0);
             const uint32_t dt = tbase + COL_ETA(b);
@@ -443,119 +497,125 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             // truncating additions land on a large accumulator
             for (int kk = 0; kk < PP / 8; ++kk) {
               const uint32_t off = 256u * kk;
-              const uint64_t ah = sdesc(zhi_addr + off, 128, sbo_k);
-              const uint64_t al = sdesc(zlo_addr + off, 128, sbo_k);
-              const uint64_t bh = sdesc(st + off, 128, sbo_k);
-              const uint64_t bl = sdesc(st + 256u * PP + off, 128, sbo_k);
-              mma_ss(dt, ah, bl, id_f, kk > 0 ? 1u : 0u);
-              mma_ss(dt, al, bh, id_f, 1u);
+              mma_ss(dt, sdesc(zhi_addr + off, 128, sbo_k), sdesc(st + 256u * PP + off, 128, sbo_k),
+                     id_f, kk > 0 ? 1u : 0u);
+              mma_ss(dt, sdesc(zlo_addr + off, 128, sbo_k), sdesc(st + off, 128, sbo_k), id_f, 1u);
             }
             for (int kk = 0; kk < PP / 8; ++kk) {
               const uint32_t off = 256u * kk;
               mma_ss(dt, sdesc(zhi_addr + off, 128, sbo_k), sdesc(st + off, 128, sbo_k), id_f, 1u);
             }
-            mma_commit(bar_eta0 + 8 * b);
+            mma_commit(b_emptyx + 8 * s);  // forward operands consumed
+            mma_commit(b_eta + 8 * b);
           }
           if (i >= 1) {
             const int j = i - 1;
             const uint32_t g = gt + j, s = g & 1u, b = g & 1u;
-            mbar_wait(bar_r0 + 8 * b, (g >> 1) & 1u, err);
-            if (g >= 2) mbar_wait(bar_gfree0 + 8 * b, ((g >> 1) - 1) & 1u, err);
+            mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);
+            mbar_wait(b_r + 8 * b, (g >> 1) & 1u, err);
+            if (g >= 2) mbar_wait(b_gfree + 8 * b, ((g >> 1) - 1) & 1u, err);
             tc_fence_after();
-            const uint32_t st = smem_u32(s ? stage1 : stage0);
+            const uint32_t st = smem_u32(s ? stage1 : stage0) + XB;
             const uint32_t dg = tbase + COL_GP(b);
             for (int kk = 0; kk < kNR / 8; ++kk) {
               const uint32_t off = 256u * kk;
-              const uint64_t bh = sdesc(st + 512u * PP + off, 128, sbo_t);
-              const uint64_t bl = sdesc(st + 768u * PP + off, 128, sbo_t);
-              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, bl, id_b, kk > 0 ? 1u : 0u);
-              mma_ts(dg, tbase + COL_RLO(b) + 8u * kk, bh, id_b, 1u);
+              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + 256u * PP + off, 128, sbo_t),
+                     id_b, kk > 0 ? 1u : 0u);
+              mma_ts(dg, tbase + COL_RLO(b) + 8u * kk, sdesc(st + off, 128, sbo_t), id_b, 1u);
             }
             for (int kk = 0; kk < kNR / 8; ++kk) {
               const uint32_t off = 256u * kk;
-              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + 512u * PP + off, 128, sbo_t),
-                     id_b, 1u);
+              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + off, 128, sbo_t), id_b, 1u);
             }
-            mma_commit(bar_empty0 + 8 * s);
-            mma_commit(bar_gfull0 + 8 * b);
+            mma_commit(b_emptyt + 8 * s);
+            mma_commit(b_gfull + 8 * b);
           }
         }
       }
       __syncwarp();
     } else {
-      // epilogue: this thread's TMEM lane = chain row 32*(warp%4) + lane
+      // epilogue: TMEM lane = chain row 32*(warp%4) + lane; warps 2-5 take tile
+      // rows (columns) 0-31 and gradient columns [0, PP/2), warps 6-9 the rest
       const int q = warp & 3;
+      const int hsel = (warp - 2) >> 2;
       const int row = 32 * q + lane;
       const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16);
+      const int gcols = PP >> 1;        // gradient columns of this half (8..32)
+      const int gc0 = hsel * gcols;
+      float Gacc[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) Gacc[k] = 0.0f;
       Kahan kl;
-      float4* grow = reinterpret_cast<float4*>(Gsum + row * PP);
-      // adds the per-tile gradient partial of tile i (TMEM) into Gsum[row]
       auto consume_gpart = [&](int i) {
         const uint32_t g = gt + i, b = g & 1u;
-        mbar_wait(bar_gfull0 + 8 * b, (g >> 1) & 1u, err);
+        mbar_wait(b_gfull + 8 * b, (g >> 1) & 1u, err);
         tc_fence_after();
-        for (int ch = 0; ch < PP / 16; ++ch) {
-          float v[16];
-          tmem_ld16(tl + COL_GP(b) + 16 * ch, v);
 #pragma unroll
-          for (int k4 = 0; k4 < 4; ++k4) {
-            float4 acc = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : grow[4 * ch + k4];
-            acc.x += v[4 * k4 + 0];
-            acc.y += v[4 * k4 + 1];
-            acc.z += v[4 * k4 + 2];
-            acc.w += v[4 * k4 + 3];
-            grow[4 * ch + k4] = acc;
+        for (int c8 = 0; c8 < 4; ++c8) {
+          if (8 * c8 < gcols) {
+            float v[8];
+            tmem_ld8(tl + COL_GP(b) + gc0 + 8 * c8, v);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) Gacc[8 * c8 + k] += v[k];
           }
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(bar_gfree0 + 8 * b);
+        if (lane == 0) mbar_arrive(b_gfree + 8 * b);
       };
       for (int i = 0; i < nt; ++i) {
         const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
-        mbar_wait(bar_eta0 + 8 * b, (g >> 1) & 1u, err);
+        mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
+        mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);  // y lives in the backward part
         tc_fence_after();
         const float* yt = reinterpret_cast<const float*>((s ? stage1 : stage0) + 1024 * PP);
-        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR);
-#pragma unroll 1
-        for (int ch = 0; ch < kNR / 16; ++ch) {
-          float v[16], hi[16], lo[16];
-          tmem_ld16(tl + COL_ETA(b) + 16 * ch, v);
+        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 32 * hsel;
+        float v[32];
+        tmem_ld32(tl + COL_ETA(b) + 32 * hsel, v);
+#pragma unroll
+        for (int h16 = 0; h16 < 2; ++h16) {
+          float hi[16], lo[16];
 #pragma unroll
           for (int k = 0; k < 16; ++k) {
-            const int n = 16 * ch + k;
+            const int n = 16 * h16 + k;
             float r = 0.0f;
             if (n < nvalid) {
-              const float yv = yt[n], eta = v[k];
-              if (a.lik == EDG_LIK_BERNOULLI) {
-                if (need_ll) {
+              const float yv = yt[32 * hsel + n], eta = v[n];
+              if (need_ll) {
+                if (a.lik == EDG_LIK_BERNOULLI) {
                   const float ex = expf(-fabsf(eta));
                   const float sg = 1.0f / (1.0f + ex);
                   r = yv - (eta >= 0.0f ? sg : ex * sg);
                   kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
                 } else {
-                  r = yv - 1.0f / (1.0f + __expf(-eta));
+                  const float diff = yv - eta;
+                  r = diff * a.inv_lik_var;
+                  kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
                 }
               } else {
-                const float diff = yv - eta;
-                r = diff * a.inv_lik_var;
-                if (need_ll) kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
+                r = residual_fast(a.lik, yv, eta, a.inv_lik_var);
               }
             }
             hi[k] = tf32_rna(r);
             lo[k] = tf32_rna(r - hi[k]);
           }
-          tmem_st16(tl + COL_RHI(b) + 16 * ch, hi);
-          tmem_st16(tl + COL_RLO(b) + 16 * ch, lo);
+          tmem_st16(tl + COL_RHI(b) + 32 * hsel + 16 * h16, hi);
+          tmem_st16(tl + COL_RLO(b) + 32 * hsel + 16 * h16, lo);
         }
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(bar_r0 + 8 * b);
+        if (lane == 0) mbar_arrive(b_r + 8 * b);
         if (i >= 1) consume_gpart(i - 1);
       }
       consume_gpart(nt - 1);
-      if (need_ll) reinterpret_cast<double*>(stage0)[row] = kl.value();
+      // this CTA's partial gradient and log-likelihood for the owners
+#pragma unroll
+      for (int c4 = 0; c4 < 8; ++c4)
+        if (4 * c4 < gcols)
+          *reinterpret_cast<float4*>(Gsum + row * PP + gc0 + 4 * c4) =
+              make_float4(Gacc[4 * c4], Gacc[4 * c4 + 1], Gacc[4 * c4 + 2], Gacc[4 * c4 + 3]);
+      if (need_ll) llpart[hsel * kCT + row] = kl.value();
       tc_fence_before();
     }
     gt += (uint32_t)nt;
@@ -571,7 +631,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
         for (int i = 0; i < kMaxEPT; i += 4) {
           if (i < EPT) {
-            const float4 v = ld_dsmem4(mapa(gpart_addr + 4u * (cc * PP + d0 + i), q));
+            const float4 v = ld_dsmem4(mapa(gsum_addr + 4u * (cc * PP + d0 + i), q));
             G[i] += v.x;
             G[i + 1] += v.y;
             G[i + 2] += v.z;
@@ -581,8 +641,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       }
       double llsum = 0.0;
       if (need_ll)
-        for (uint32_t q = 0; q < R; ++q) llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * cc, q));
-      // prior: gradient and (when needed) FP64 log density of the evaluated position
+        for (uint32_t q = 0; q < R; ++q)
+          llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * cc, q)) +
+                   ld_dsmem_f64(mapa(llpart_addr + 8u * (kCT + cc), q));
       double lp = 0.0;
 #pragma unroll
       for (int i = 0; i < kMaxEPT; ++i) {
@@ -600,7 +661,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         }
       }
       if (need_ll)
-        for (int o = (int)R >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
+        for (int o = TPC >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
       if (cache_eval) {
 #pragma unroll
         for (int i = 0; i < kMaxEPT; ++i) g0r[i] = G[i];
@@ -616,7 +677,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           double k = 0.0;
 #pragma unroll
           for (int i = 0; i < kMaxEPT; ++i) k += (double)rr[i] * (double)rr[i];
-          for (int o = (int)R >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+          for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
           const double lj_new = llsum + lp;
           const double ratio = 0.5 * kin0 - 0.5 * k + lj_new - lj0;
           double u = 0.5;
@@ -696,7 +757,7 @@ static int padded_P(int P) { return round_up(std::max(P, 16), 16); }
 // (each allocates all 512 TMEM columns; a second resident CTA would block in
 // tcgen05.alloc while its cluster waits on it).
 static size_t smem_bytes(int PP) {
-  return std::max<size_t>(2 * (size_t)stage_bytes(PP) + (size_t)1536 * PP + 256, 120 * 1024);
+  return std::max<size_t>(2 * (size_t)stage_bytes(PP) + (size_t)1024 * PP + 256, 120 * 1024);
 }
 
 static int sm_count() {
@@ -706,13 +767,14 @@ static int sm_count() {
   return v > 0 ? v : 1;
 }
 
-// Cluster size: a power of two R <= 8 with R <= ntiles, PP/R <= 16,
-// (PP/R) % 4 == 0, and clusters * R close to the SM count.
+// Cluster size: a power of two R <= 8 with R <= ntiles, owner elements per
+// thread PP/(2R) a multiple of 4 and <= 8, and clusters * R close to the SM count.
 static int choose_R(int PP, int C, int ntiles, int want) {
   const int nclusters = (C + kCT - 1) / kCT;
   int best = 0;
   for (int R = 1; R <= 8; R <<= 1) {
-    if (PP / R > kMaxEPT || (PP / R) % 4 != 0 || PP % R != 0 || R > ntiles) continue;
+    const int ept = PP / (2 * R);
+    if (PP % (2 * R) != 0 || ept > kMaxEPT || ept % 4 != 0 || R > ntiles) continue;
     if (want > 0) {
       if (R == want) return R;
       continue;
