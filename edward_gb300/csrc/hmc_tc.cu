@@ -751,7 +751,8 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 }
 
 // ------------------------------------------------------------------ host side
-static int padded_P(int P) { return round_up(std::max(P, 16), 16); }
+// Operand width: 16, 32 or 64 columns (the owner split needs PP / (2R) in {4, 8}).
+static int padded_P(int P) { return P <= 16 ? 16 : (P <= 32 ? 32 : round_up(P, 64)); }
 
 // Dynamic shared memory: at least 120 KB so that no two CTAs share an SM
 // (each allocates all 512 TMEM columns; a second resident CTA would block in
