@@ -274,7 +274,7 @@ def run_gpu(args):
                 "config": dict(CONFIG, parallelism=f"replicas{world}",
                                l2_flush="256 MB write before each step, outside the timed events",
                                engine=inf.engine, accept_rate=round(acc, 4)),
-                "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
+                "e2e": e2e, "gpu_launches": args.steps,  # one HMC launch per step "roofline": roof,
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
@@ -284,9 +284,10 @@ def run_gpu(args):
 
 
 def run_e2e(args, inf, X, y, z0, dev):
-    """Same metric through edg_hmc_glm_run with host buffers: every step copies
-    X, y and the chain state (z, cached gradient and log joint) from pinned
-    host memory, runs one iteration, and copies the state and the kept
+    """Same metric through the C ABI with host buffers: every step copies X, y
+    and the chain state (z, cached gradient and log joint) from pinned host
+    memory, re-lays X for the engine when it needs it, runs one iteration with
+    the engine the inference selected, and copies the state and the kept
     sample back."""
     import ctypes
     import torch
@@ -314,6 +315,11 @@ def run_e2e(args, inf, X, y, z0, dev):
     stream = torch.cuda.current_stream()
     sp = _lib.stream_ptr(stream)
     state0 = _lib.new_state(dev)
+    lib = _lib.load()
+    tc = inf.engine == "tc"
+    if tc:
+        nb = lib.edg_hmc_glm_tc_tiles_bytes(ctypes.byref(glm))
+        tiles = torch.empty(nb, dtype=torch.uint8, device=dev)
 
     def step(cache_valid):
         d_X.copy_(h_X, non_blocking=True)
@@ -322,9 +328,15 @@ def run_e2e(args, inf, X, y, z0, dev):
         d_g.copy_(h_g, non_blocking=True)
         d_lj.copy_(h_lj, non_blocking=True)
         st.copy_(state0)
-        _lib.call("edg_hmc_glm_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
-                  _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid, None, _lib.ptr(st),
-                  _lib.ptr(d_s), 1, None, None, None, None, sp)
+        if tc:
+            _lib.call("edg_hmc_glm_tc_prepare", ctypes.byref(glm), _lib.ptr(tiles), nb, sp)
+            _lib.call("edg_hmc_glm_tc_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
+                      _lib.ptr(tiles), _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid,
+                      None, _lib.ptr(st), _lib.ptr(d_s), 1, None, None, None, None, sp)
+        else:
+            _lib.call("edg_hmc_glm_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
+                      _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid, None,
+                      _lib.ptr(st), _lib.ptr(d_s), 1, None, None, None, None, sp)
         h_z.copy_(d_z, non_blocking=True)
         h_g.copy_(d_g, non_blocking=True)
         h_lj.copy_(d_lj, non_blocking=True)
@@ -341,9 +353,10 @@ def run_e2e(args, inf, X, y, z0, dev):
     dt = time.perf_counter() - t0
     h2d = h_X.numel() * 4 + h_y.numel() * 4 + h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8
     d2h = h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8 + h_out.numel() * 4
+    name = "edg_hmc_glm_tc_prepare + edg_hmc_glm_tc_run" if tc else "edg_hmc_glm_run"
     return {"value": N_CHAINS * N_LEAP * args.steps / dt, "unit": UNIT,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "path": "edg_hmc_glm_run (C ABI) with pinned host buffers, wall clock"}
+            "path": f"{name} (C ABI) with pinned host buffers, wall clock"}
 
 
 def read_traffic(engine):
