@@ -274,7 +274,7 @@ def run_gpu(args):
                 "config": dict(CONFIG, parallelism=f"replicas{world}",
                                l2_flush="256 MB write before each step, outside the timed events",
                                engine=inf.engine, accept_rate=round(acc, 4)),
-                "e2e": e2e, "gpu_launches": args.steps,  # one HMC launch per step "roofline": roof,
+                "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)

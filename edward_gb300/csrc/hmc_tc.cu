@@ -67,13 +67,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+// try_wait with a suspend-time hint: a waiting thread sleeps (up to 20 us)
+// instead of spinning, leaving issue slots to the epilogue warps; it wakes as
+// soon as the phase completes.
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       " selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(20000u)
       : "memory");
   return ok != 0;
 }
@@ -390,6 +393,20 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     gr[i] = g0r[i];
   }
   if (cvalid && a.cache_valid) lj0 = a.lj[cg];
+  // prior loc and precision 1/scale^2 per coordinate (zero beyond P), and this
+  // thread's share of the log-density normalising constant
+  __shared__ float s_ploc[64], s_pprec[64];
+  for (int d = threadIdx.x; d < PP; d += kThreads) {
+    const bool ok = d < P;
+    const float sc = ok ? a.prior_scale[d] : 1.0f;
+    s_ploc[d] = ok ? a.prior_loc[d] : 0.0f;
+    s_pprec[d] = ok ? 1.0f / (sc * sc) : 0.0f;
+  }
+  double plogc = 0.0;
+  for (int i = 0; i < EPT; ++i) {
+    const int d = d0 + i;
+    if (owner && d < P) plogc += -(double)logf(a.prior_scale[d]) - kHalfLog2Pi;
+  }
   const int64_t t0 = *(volatile int64_t*)&a.state->t;
   const float eps = a.step_size, half = 0.5f * a.step_size;
   const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
@@ -568,7 +585,8 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
         mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);  // y lives in the backward part
         tc_fence_after();
-        const float* yt = reinterpret_cast<const float*>((s ? stage1 : stage0) + 1024 * PP);
+        const float4* yt4 =
+            reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 8 * hsel;
         const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 32 * hsel;
         float v[32];
         tmem_ld32(tl + COL_ETA(b) + 32 * hsel, v);
@@ -579,8 +597,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           for (int k = 0; k < 16; ++k) {
             const int n = 16 * h16 + k;
             float r = 0.0f;
+            const float4 y4 = yt4[n >> 2];
+            const float yv = (n & 3) == 0 ? y4.x : (n & 3) == 1 ? y4.y : (n & 3) == 2 ? y4.z : y4.w;
             if (n < nvalid) {
-              const float yv = yt[32 * hsel + n], eta = v[n];
+              const float eta = v[n];
               if (need_ll) {
                 if (a.lik == EDG_LIK_BERNOULLI) {
                   const float ex = expf(-fabsf(eta));
@@ -644,21 +664,14 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         for (uint32_t q = 0; q < R; ++q)
           llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * cc, q)) +
                    ld_dsmem_f64(mapa(llpart_addr + 8u * (kCT + cc), q));
-      double lp = 0.0;
+      double lp = plogc;
 #pragma unroll
       for (int i = 0; i < kMaxEPT; ++i) {
-        const int d = d0 + i;
-        if (i < EPT && d < P) {
-          const float sc = a.prior_scale[d];
-          const float zz = zr[i];
-          G[i] += -(zz - a.prior_loc[d]) / (sc * sc);
-          if (need_ll) {
-            const float u = (zz - a.prior_loc[d]) / sc;
-            lp += (double)(-0.5f * u * u - logf(sc)) - kHalfLog2Pi;
-          }
-        } else {
-          G[i] = 0.0f;
-        }
+        const int d = min(d0 + i, PP - 1);
+        const float pr = i < EPT ? s_pprec[d] : 0.0f;
+        const float dz = zr[i] - s_ploc[d];
+        G[i] = (i < EPT && d0 + i < P) ? G[i] - dz * pr : 0.0f;
+        if (need_ll) lp += (double)(-0.5f * dz * dz * pr);
       }
       if (need_ll)
         for (int o = TPC >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
