@@ -502,26 +502,38 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         fence_proxy_async();
         const uint32_t id_f = idesc_tf32(kCT, kNR);
         const uint32_t id_b = idesc_tf32(kCT, PP);
+        // Descriptors are built once; a K step of 8 tf32 elements is 256 bytes,
+        // i.e. +16 in the descriptor's start-address field (address >> 4).
         const uint32_t sbo_k = 32u * PP, sbo_t = 32u * kNR;
+        const uint64_t dz_hi = sdesc(zhi_addr, 128, sbo_k), dz_lo = sdesc(zlo_addr, 128, sbo_k);
+        const uint32_t st0 = smem_u32(stage0), st1 = smem_u32(stage1);
+        const uint64_t dx_hi[2] = {sdesc(st0, 128, sbo_k), sdesc(st1, 128, sbo_k)};
+        const uint64_t dx_lo[2] = {sdesc(st0 + 256u * PP, 128, sbo_k),
+                                   sdesc(st1 + 256u * PP, 128, sbo_k)};
+        const uint64_t dt_hi[2] = {sdesc(st0 + 512u * PP, 128, sbo_t),
+                                   sdesc(st1 + 512u * PP, 128, sbo_t)};
+        const uint64_t dt_lo[2] = {sdesc(st0 + 768u * PP, 128, sbo_t),
+                                   sdesc(st1 + 768u * PP, 128, sbo_t)};
+        const int KF = PP / 8;  // forward K steps (2, 4 or 8)
         for (int i = 0; i <= nt; ++i) {
           if (i < nt) {
             const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
             mbar_wait(b_fullx + 8 * s, (g >> 1) & 1u, err);
             tc_fence_after();
-            const uint32_t st = smem_u32(s ? stage1 : stage0);
             const uint32_t dt = tbase + COL_ETA(b);
+            const uint64_t xh = s ? dx_hi[1] : dx_hi[0], xl = s ? dx_lo[1] : dx_lo[0];
             // lo products first (small running sum), hi*hi last: fewer
             // truncating additions land on a large accumulator
-            for (int kk = 0; kk < PP / 8; ++kk) {
-              const uint32_t off = 256u * kk;
-              mma_ss(dt, sdesc(zhi_addr + off, 128, sbo_k), sdesc(st + 256u * PP + off, 128, sbo_k),
-                     id_f, kk > 0 ? 1u : 0u);
-              mma_ss(dt, sdesc(zlo_addr + off, 128, sbo_k), sdesc(st + off, 128, sbo_k), id_f, 1u);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              if (kk < KF) {
+                mma_ss(dt, dz_hi + 16 * kk, xl + 16 * kk, id_f, kk > 0 ? 1u : 0u);
+                mma_ss(dt, dz_lo + 16 * kk, xh + 16 * kk, id_f, 1u);
+              }
             }
-            for (int kk = 0; kk < PP / 8; ++kk) {
-              const uint32_t off = 256u * kk;
-              mma_ss(dt, sdesc(zhi_addr + off, 128, sbo_k), sdesc(st + off, 128, sbo_k), id_f, 1u);
-            }
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+              if (kk < KF) mma_ss(dt, dz_hi + 16 * kk, xh + 16 * kk, id_f, 1u);
             mma_commit(b_emptyx + 8 * s);  // forward operands consumed
             mma_commit(b_eta + 8 * b);
           }
@@ -532,18 +544,16 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             mbar_wait(b_r + 8 * b, (g >> 1) & 1u, err);
             if (g >= 2) mbar_wait(b_gfree + 8 * b, ((g >> 1) - 1) & 1u, err);
             tc_fence_after();
-            const uint32_t st = smem_u32(s ? stage1 : stage0) + XB;
             const uint32_t dg = tbase + COL_GP(b);
+            const uint32_t rh = tbase + COL_RHI(b), rl = tbase + COL_RLO(b);
+            const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
+#pragma unroll
             for (int kk = 0; kk < kNR / 8; ++kk) {
-              const uint32_t off = 256u * kk;
-              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + 256u * PP + off, 128, sbo_t),
-                     id_b, kk > 0 ? 1u : 0u);
-              mma_ts(dg, tbase + COL_RLO(b) + 8u * kk, sdesc(st + off, 128, sbo_t), id_b, 1u);
+              mma_ts(dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
+              mma_ts(dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
             }
-            for (int kk = 0; kk < kNR / 8; ++kk) {
-              const uint32_t off = 256u * kk;
-              mma_ts(dg, tbase + COL_RHI(b) + 8u * kk, sdesc(st + off, 128, sbo_t), id_b, 1u);
-            }
+#pragma unroll
+            for (int kk = 0; kk < kNR / 8; ++kk) mma_ts(dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
             mma_commit(b_emptyt + 8 * s);
             mma_commit(b_gfull + 8 * b);
           }
