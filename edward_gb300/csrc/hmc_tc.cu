@@ -17,8 +17,8 @@
 //     K-major shared-memory layout (hi, lo, transposed hi, transposed lo, y),
 //     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
 //
-// Warp roles (320 threads): warp 0 bulk-copy producers, warp 1 MMA issuer and
-// TMEM owner, warps 2-9 epilogue; between gradient evaluations warps 2-9 are
+// Warp roles (576 threads): warp 0 bulk-copy producers, warp 1 MMA issuer and
+// TMEM owner, warps 2-17 epilogue; between gradient evaluations warps 2-17 are
 // the "owners" that run the leapfrog / Metropolis arithmetic for this CTA's
 // share of the cluster's chains, with the chain state in registers.
 //
@@ -35,7 +35,7 @@ namespace tc {
 
 constexpr int kCT = 128;        // chains per cluster = MMA M
 constexpr int kNR = 64;         // rows per X tile = forward N = backward K
-constexpr int kThreads = 320;  // 2 control warps + 8 epilogue warps
+constexpr int kThreads = 576;  // 2 control warps + 16 epilogue warps
 constexpr uint32_t kTmemCols = 512;
 
 __host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP + 256u; }
@@ -263,8 +263,8 @@ struct TcArgs {
   double* ratio_out;
 };
 
-constexpr int kMaxEPT = 8;  // chain-state elements per owner thread
-constexpr int kEpiWarps = 8;
+constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
+constexpr int kEpiWarps = 16;
 
 // 32x32b.x16 twice (32 consecutive columns) with a single wait.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -294,6 +294,18 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
       : "memory");
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // Residual of one (row, chain): d log p(y | eta) / d eta.  The accurate form
@@ -368,10 +380,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #define COL_RLO(b) (128u + 192u * (b))
 #define COL_GP(b) (384u + 64u * (b))
 
-  // ---- owner mapping (warps 2-9, 256 threads): 2R threads per chain
+  // ---- owner mapping (warps 2-17, 512 threads): 4R threads per chain
   const bool owner = warp >= 2;
   const int et = threadIdx.x - 64;
-  const int TPC = 2 * (int)R;
+  const int TPC = 4 * (int)R;
   const int CPO = kCT / (int)R;
   const int EPT = PP / TPC;
   const int chain_local = owner ? et / TPC : 0;
@@ -380,19 +392,20 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const int cc = (int)rank * CPO + chain_local;  // chain within the cluster (MMA row)
   const int cg = c_base + cc;                    // global chain
   const bool cvalid = owner && cg < a.C;
-  float z0r[kMaxEPT], g0r[kMaxEPT], zr[kMaxEPT], rr[kMaxEPT], gr[kMaxEPT];
-  double lj0 = 0.0, kin0 = 0.0;
+  // Working position / momentum / gradient in registers; the accepted state
+  // (z, its gradient and log joint) stays in the caller's z / grad / lj arrays,
+  // touched once per iteration, which keeps the epilogue's registers free.
+  float zr[kMaxEPT], rr[kMaxEPT], gr[kMaxEPT];
+  double kin0 = 0.0;
+  float* zg = a.z + (size_t)(cvalid ? cg : 0) * P;
+  float* gg = a.grad + (size_t)(cvalid ? cg : 0) * P;
 #pragma unroll
   for (int i = 0; i < kMaxEPT; ++i) {
     const int d = d0 + i;
-    const bool ok = cvalid && i < EPT && d < P;
-    z0r[i] = ok ? a.z[(size_t)cg * P + d] : 0.0f;
-    g0r[i] = (ok && a.cache_valid) ? a.grad[(size_t)cg * P + d] : 0.0f;
-    zr[i] = z0r[i];
+    zr[i] = (cvalid && i < EPT && d < P) ? zg[d] : 0.0f;
     rr[i] = 0.0f;
-    gr[i] = g0r[i];
+    gr[i] = 0.0f;
   }
-  if (cvalid && a.cache_valid) lj0 = a.lj[cg];
   // prior loc and precision 1/scale^2 per coordinate (zero beyond P), and this
   // thread's share of the log-density normalising constant
   __shared__ float s_ploc[64], s_pprec[64];
@@ -412,7 +425,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
   // end-of-evaluation exchange buffers (alias stage 0, idle between evaluations)
   float* Gsum = reinterpret_cast<float*>(stage0);                   // [128][PP]
-  double* llpart = reinterpret_cast<double*>(stage0 + 512 * PP);    // [2][128]
+  double* llpart = reinterpret_cast<double*>(stage0 + 512 * PP);    // [4][128]
   const uint32_t gsum_addr = smem_u32(Gsum), llpart_addr = smem_u32(llpart);
 
   // every CTA of the cluster must be running before any DSMEM access
@@ -442,9 +455,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             if (cvalid && i < EPT && d < P)
               r = a.r_ovr ? a.r_ovr[((size_t)it * a.C + cg) * P + d]
                           : philox_normal(a.seed, 1u, iter, (uint32_t)cg, (uint32_t)d);
+            const bool ok = cvalid && i < EPT && d < P;
             rr[i] = r;
-            zr[i] = z0r[i];
-            gr[i] = g0r[i];
+            zr[i] = ok ? zg[d] : 0.0f;
+            gr[i] = ok ? gg[d] : 0.0f;
             k += (double)r * (double)r;
           }
           for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
@@ -561,30 +575,39 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       }
       __syncwarp();
     } else {
-      // epilogue: TMEM lane = chain row 32*(warp%4) + lane; warps 2-5 take tile
-      // rows (columns) 0-31 and gradient columns [0, PP/2), warps 6-9 the rest
+      // epilogue: TMEM lane = chain row 32*(warp%4) + lane; the four warps of a
+      // lane quarter split the tile's 64 rows (TMEM columns) and the gradient
+      // columns into quarters
       const int q = warp & 3;
-      const int hsel = (warp - 2) >> 2;
+      const int qs = (warp - 2) >> 2;
       const int row = 32 * q + lane;
       const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16);
-      const int gcols = PP >> 1;        // gradient columns of this half (8..32)
-      const int gc0 = hsel * gcols;
-      float Gacc[32];
+      const int gcols = PP >> 2;        // gradient columns of this quarter (4, 8 or 16)
+      const int gc0 = qs * gcols;
+      float Gacc[16];
 #pragma unroll
-      for (int k = 0; k < 32; ++k) Gacc[k] = 0.0f;
+      for (int k = 0; k < 16; ++k) Gacc[k] = 0.0f;
       Kahan kl;
       auto consume_gpart = [&](int i) {
         const uint32_t g = gt + i, b = g & 1u;
         mbar_wait(b_gfull + 8 * b, (g >> 1) & 1u, err);
         tc_fence_after();
+        const uint32_t ga = tl + COL_GP(b) + gc0;
+        if (gcols == 16) {
+          float v[16];
+          tmem_ld16(ga, v);
 #pragma unroll
-        for (int c8 = 0; c8 < 4; ++c8) {
-          if (8 * c8 < gcols) {
-            float v[8];
-            tmem_ld8(tl + COL_GP(b) + gc0 + 8 * c8, v);
+          for (int k = 0; k < 16; ++k) Gacc[k] += v[k];
+        } else if (gcols == 8) {
+          float v[8];
+          tmem_ld8(ga, v);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) Gacc[8 * c8 + k] += v[k];
-          }
+          for (int k = 0; k < 8; ++k) Gacc[k] += v[k];
+        } else {
+          float v[4];
+          tmem_ld4(ga, v);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) Gacc[k] += v[k];
         }
         tc_fence_before();
         __syncwarp();
@@ -596,42 +619,39 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);  // y lives in the backward part
         tc_fence_after();
         const float4* yt4 =
-            reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 8 * hsel;
-        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 32 * hsel;
-        float v[32];
-        tmem_ld32(tl + COL_ETA(b) + 32 * hsel, v);
+            reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 4 * qs;
+        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
+        float v[16], lo[16];
+        tmem_ld16(tl + COL_ETA(b) + 16 * qs, v);
 #pragma unroll
-        for (int h16 = 0; h16 < 2; ++h16) {
-          float hi[16], lo[16];
-#pragma unroll
-          for (int k = 0; k < 16; ++k) {
-            const int n = 16 * h16 + k;
-            float r = 0.0f;
-            const float4 y4 = yt4[n >> 2];
-            const float yv = (n & 3) == 0 ? y4.x : (n & 3) == 1 ? y4.y : (n & 3) == 2 ? y4.z : y4.w;
-            if (n < nvalid) {
-              const float eta = v[n];
-              if (need_ll) {
-                if (a.lik == EDG_LIK_BERNOULLI) {
-                  const float ex = expf(-fabsf(eta));
-                  const float sg = 1.0f / (1.0f + ex);
-                  r = yv - (eta >= 0.0f ? sg : ex * sg);
-                  kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
-                } else {
-                  const float diff = yv - eta;
-                  r = diff * a.inv_lik_var;
-                  kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
-                }
+        for (int k = 0; k < 16; ++k) {
+          float r = 0.0f;
+          const float4 y4 = yt4[k >> 2];
+          const float yv = (k & 3) == 0 ? y4.x : (k & 3) == 1 ? y4.y : (k & 3) == 2 ? y4.z : y4.w;
+          if (k < nvalid) {
+            const float eta = v[k];
+            if (need_ll) {
+              if (a.lik == EDG_LIK_BERNOULLI) {
+                const float ex = expf(-fabsf(eta));
+                const float sg = 1.0f / (1.0f + ex);
+                r = yv - (eta >= 0.0f ? sg : ex * sg);
+                kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
               } else {
-                r = residual_fast(a.lik, yv, eta, a.inv_lik_var);
+                const float diff = yv - eta;
+                r = diff * a.inv_lik_var;
+                kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
               }
+            } else {
+              r = residual_fast(a.lik, yv, eta, a.inv_lik_var);
             }
-            hi[k] = tf32_rna(r);
-            lo[k] = tf32_rna(r - hi[k]);
           }
-          tmem_st16(tl + COL_RHI(b) + 32 * hsel + 16 * h16, hi);
-          tmem_st16(tl + COL_RLO(b) + 32 * hsel + 16 * h16, lo);
+          // hi = tf32(r); lo = r - hi is exact and only the tensor core's own
+          // rounding of lo (a relative 2^-21 of r) remains
+          v[k] = tf32_rna(r);
+          lo[k] = r - v[k];
         }
+        tmem_st16(tl + COL_RHI(b) + 16 * qs, v);
+        tmem_st16(tl + COL_RLO(b) + 16 * qs, lo);
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
@@ -641,11 +661,11 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       consume_gpart(nt - 1);
       // this CTA's partial gradient and log-likelihood for the owners
 #pragma unroll
-      for (int c4 = 0; c4 < 8; ++c4)
+      for (int c4 = 0; c4 < 4; ++c4)
         if (4 * c4 < gcols)
           *reinterpret_cast<float4*>(Gsum + row * PP + gc0 + 4 * c4) =
               make_float4(Gacc[4 * c4], Gacc[4 * c4 + 1], Gacc[4 * c4 + 2], Gacc[4 * c4 + 3]);
-      if (need_ll) llpart[hsel * kCT + row] = kl.value();
+      if (need_ll) llpart[qs * kCT + row] = kl.value();
       tc_fence_before();
     }
     gt += (uint32_t)nt;
@@ -672,8 +692,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       double llsum = 0.0;
       if (need_ll)
         for (uint32_t q = 0; q < R; ++q)
-          llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * cc, q)) +
-                   ld_dsmem_f64(mapa(llpart_addr + 8u * (kCT + cc), q));
+          for (int h = 0; h < 4; ++h) llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * (h * kCT + cc), q));
       double lp = plogc;
 #pragma unroll
       for (int i = 0; i < kMaxEPT; ++i) {
@@ -686,9 +705,12 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       if (need_ll)
         for (int o = TPC >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
       if (cache_eval) {
+        if (cvalid) {
 #pragma unroll
-        for (int i = 0; i < kMaxEPT; ++i) g0r[i] = G[i];
-        lj0 = llsum + lp;
+          for (int i = 0; i < kMaxEPT; ++i)
+            if (i < EPT && d0 + i < P) gg[d0 + i] = G[i];
+          if (part == 0) a.lj[cg] = llsum + lp;
+        }
       } else {
 #pragma unroll
         for (int i = 0; i < kMaxEPT; ++i) {
@@ -702,22 +724,17 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           for (int i = 0; i < kMaxEPT; ++i) k += (double)rr[i] * (double)rr[i];
           for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
           const double lj_new = llsum + lp;
+          const double lj0 = cvalid ? a.lj[cg] : 0.0;
+          __syncwarp();  // every thread of the chain has read lj before it is replaced
           const double ratio = 0.5 * kin0 - 0.5 * k + lj_new - lj0;
           double u = 0.5;
           if (cvalid)
             u = a.u_ovr ? a.u_ovr[(size_t)it * a.C + cg]
                         : u01d(philox_at(a.seed, 2u, iter, (uint32_t)cg, 0u).x);
           const bool accept = log(u) < ratio;
-          if (accept) {
-#pragma unroll
-            for (int i = 0; i < kMaxEPT; ++i) {
-              z0r[i] = zr[i];
-              g0r[i] = gr[i];
-            }
-            lj0 = lj_new;
-          }
           if (cvalid) {
             if (part == 0) {
+              if (accept) a.lj[cg] = lj_new;
               if (a.n_accept) a.n_accept[cg] += accept ? 1 : 0;
               if (a.ratio_out) a.ratio_out[(size_t)it * a.C + cg] = ratio;
             }
@@ -725,12 +742,19 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             for (int i = 0; i < kMaxEPT; ++i) {
               const int d = d0 + i;
               if (i < EPT && d < P) {
-                if (a.samples && t < a.T_cap)
-                  a.samples[((size_t)t * a.C + cg) * P + d] = z0r[i];
+                float kept;
+                if (accept) {
+                  kept = zr[i];
+                  zg[d] = zr[i];
+                  gg[d] = gr[i];
+                } else {
+                  kept = zg[d];
+                }
+                if (a.samples && t < a.T_cap) a.samples[((size_t)t * a.C + cg) * P + d] = kept;
                 if (a.moments) {
                   const size_t gi = (size_t)cg * P + d;
-                  a.moments[gi] += (double)z0r[i];
-                  a.moments[(size_t)a.C * P + gi] += (double)z0r[i] * (double)z0r[i];
+                  a.moments[gi] += (double)kept;
+                  a.moments[(size_t)a.C * P + gi] += (double)kept * (double)kept;
                 }
               }
             }
@@ -740,18 +764,6 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     }
   }
 
-  // ---- write back the chain state and its cached gradient / log joint
-  if (cvalid) {
-#pragma unroll
-    for (int i = 0; i < kMaxEPT; ++i) {
-      const int d = d0 + i;
-      if (i < EPT && d < P) {
-        a.z[(size_t)cg * P + d] = z0r[i];
-        a.grad[(size_t)cg * P + d] = g0r[i];
-      }
-    }
-    if (part == 0) a.lj[cg] = lj0;
-  }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
@@ -791,14 +803,14 @@ static int sm_count() {
   return v > 0 ? v : 1;
 }
 
-// Cluster size: a power of two R <= 8 with R <= ntiles, owner elements per
-// thread PP/(2R) a multiple of 4 and <= 8, and clusters * R close to the SM count.
+// Cluster size: a power of two R <= 8 with R <= ntiles and owner elements per
+// thread PP/(4R) equal to 4 (R = PP/16), and clusters * R close to the SM count.
 static int choose_R(int PP, int C, int ntiles, int want) {
   const int nclusters = (C + kCT - 1) / kCT;
   int best = 0;
   for (int R = 1; R <= 8; R <<= 1) {
-    const int ept = PP / (2 * R);
-    if (PP % (2 * R) != 0 || ept > kMaxEPT || ept % 4 != 0 || R > ntiles) continue;
+    const int ept = PP / (4 * R);
+    if (PP % (4 * R) != 0 || ept > kMaxEPT || ept % 4 != 0 || R > ntiles) continue;
     if (want > 0) {
       if (R == want) return R;
       continue;
