@@ -65,9 +65,9 @@ def run_tc(dev, tiles, C, z0, step, L, n_iter, r=None, u=None, cluster=0, seed=5
 @pytest.mark.parametrize("N,D,C,L,cluster,lik", [
     (640, 50, 128, 2, 4, 0),      # one cluster, 10 row tiles
     (2000, 50, 200, 3, 4, 0),     # partial second cluster, ragged last tile
-    (1000, 13, 130, 2, 2, 1),     # P = 14 -> PP = 16, Normal likelihood
-    (4096, 31, 256, 2, 4, 0),     # PP = 32, cluster of 4
-    (6000, 60, 130, 2, 8, 0),     # PP = 64, cluster of 8
+    (1000, 13, 130, 2, 0, 1),     # P = 14 -> PP = 16 (one CTA per cluster), Normal likelihood
+    (4096, 31, 256, 2, 0, 0),     # PP = 32, cluster of 2
+    (6000, 60, 130, 2, 0, 0),     # PP = 64, partial second cluster
     (10000, 50, 256, 4, 4, 0),    # benchmark shape, 2 clusters
 ])
 def test_tc_iteration_parity(cuda, N, D, C, L, cluster, lik):
