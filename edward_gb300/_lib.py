@@ -70,6 +70,8 @@ _SIGS = {
     "edg_glm_logjoint_grad_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgGLM), c_int32]),
     "edg_glm_logjoint_grad": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_int32, c_int32, c_float,
                                         c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "edg_glm_logjoint_grad_noalloc": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_int32, c_int32,
+                                                c_float, c_void_p, c_void_p, c_void_p]),
     "edg_klqp_glm_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgKLqp)]),
     "edg_klqp_glm_step": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgKLqp),
                                     ctypes.POINTER(EdgOpt), c_void_p, c_void_p, c_void_p, c_void_p,

@@ -13,6 +13,7 @@
 // (klqp.py:725-747 builds S separate GEMV graphs).
 #include <cstdio>
 #include <algorithm>
+#include <mutex>
 
 #include "edg_common.cuh"
 
@@ -1060,4 +1061,72 @@ extern "C" int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int
     case 32: return launch_hmc<32>(m, a, st);
     default: return fail(EDG_E_VALUE, "chains_per_block must be 0, 8, 16 or 32 (got %d)", ct);
   }
+}
+
+// ---------------------------------------------------------------- no-allocation variant
+// Fixed device scratch for edg_glm_logjoint_grad_noalloc.  Every GPU that
+// loads this library holds these bytes until the process exits.
+namespace edg {
+constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The host-side
+// symbol is only a stand-in, so the address is looked up once per device
+// (cudaGetSymbolAddress, with that device current) and cached.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  EDG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, EDG_E_UNSUPPORTED,
+              "device %d is beyond the %d devices the fixed scratch supports", dev,
+              kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(EDG_E_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return EDG_OK;
+}
+}  // namespace edg
+
+extern "C" int edg_glm_logjoint_grad_noalloc(const edg_glm_t* model, const float* Z, int32_t B,
+                                             int32_t include_prior, float data_scale,
+                                             double* lp_out, float* grad_out, void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(Z, EDG_E_NULL, "Z is NULL");
+  EDG_REQUIRE(B > 0, EDG_E_SHAPE, "B must be positive (got %d)", B);
+  if (!lp_out && !grad_out) return EDG_OK;
+  const GradPlan p = plan_grad(m, B);
+  const size_t need = round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+  EDG_REQUIRE(need <= kNoAllocScratchBytes, EDG_E_WORKSPACE,
+              "this call needs %zu bytes of scratch but the fixed scratch holds %zu bytes; "
+              "split the %d vectors into smaller batches or use edg_glm_logjoint_grad",
+              need, kNoAllocScratchBytes, B);
+  void* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  float* wg = reinterpret_cast<float*>(scratch);
+  double* wl = reinterpret_cast<double*>(reinterpret_cast<char*>(scratch) +
+                                         round_up((int)p.ws_g_bytes, 256));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int ng = grad_out ? 1 : 0;
+  switch (p.CT) {
+    case 8: rc = launch_partial<8>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+    case 16: rc = launch_partial<16>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+    default: rc = launch_partial<32>(m, Z, B, p, data_scale, wg, wl, ng, st); break;
+  }
+  if (rc) return rc;
+  const int64_t n = std::max<int64_t>((int64_t)B * m.P, B);
+  glm_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+      m, Z, B, p.nchunks, wg, wl, p.Bpad, include_prior, lp_out, grad_out);
+  return check_launch("glm_reduce_kernel (no-alloc)");
 }

@@ -160,6 +160,29 @@ int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int32_t B,
                           double* lp_out /* [B] or NULL */, float* grad_out /* [B,P] or NULL */,
                           void* workspace, size_t workspace_bytes, void* stream);
 
+/* Same results as edg_glm_logjoint_grad, but this entry point allocates
+ * nothing and takes no workspace.  It has no counterpart in the reference.
+ * It is for callers that cannot allocate device memory at call time: host
+ * frameworks that reserve all device memory in their own pool up front (an
+ * extra cudaMalloc would fail or fragment it), and integrations that must
+ * stay within a fixed memory budget fixed when they were loaded.
+ *  - Scratch: a fixed 8 MiB array compiled into the library (a file-scope
+ *    __device__ array).  Every GPU that loads the library holds it until the
+ *    process exits.  Calls whose partial sums need more than 8 MiB fail with
+ *    EDG_E_WORKSPACE; split B into smaller batches (e.g. 4096 vectors of
+ *    P = 51 over 10,000 rows need 1.8 MB).
+ *  - The first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress) and caches it; make that first call before any
+ *    stream capture.
+ *  - Every call on a device uses the same array, so calls that overlap on the
+ *    GPU (different streams, or threads without ordering) race and corrupt
+ *    each other's results; serialise them on one stream.  Nothing needs to be
+ *    cleared between calls: each call writes every scratch byte it reads. */
+int edg_glm_logjoint_grad_noalloc(const edg_glm_t* model, const float* Z, int32_t B,
+                                  int32_t include_prior, float data_scale,
+                                  double* lp_out /* [B] or NULL */,
+                                  float* grad_out /* [B,P] or NULL */, void* stream);
+
 /* ---------------------------------------------------------------- KLqp
  * One fused ELBO-gradient step for a mean-field Normal q = N(mu, softplus(rho))
  * over a GLM: Philox eps -> z_s -> log-lik + adjoint over X for all samples
