@@ -54,6 +54,12 @@ class EdgKLqp(ctypes.Structure):
                 ("kl_scaling", c_void_p), ("latent_scale", c_void_p), ("seed", c_uint64)]
 
 
+class EdgHier(ctypes.Structure):
+    _fields_ = [("X", c_void_p), ("y", c_void_p), ("x_offset", c_void_p), ("y_offset", c_void_p),
+                ("N", c_void_p), ("D", c_void_p), ("I", c_int32), ("max_D", c_int32),
+                ("mu_loc", c_float), ("mu_scale", c_float), ("tau_scale", c_float)]
+
+
 class EdgHMC(ctypes.Structure):
     _fields_ = [("step_size", c_float), ("n_steps", c_int32), ("seed", c_uint64),
                 ("chains_per_block", c_int32), ("cluster_size", c_int32)]
@@ -80,6 +86,10 @@ _SIGS = {
                                   c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p,
                                   c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
+    "edg_hmc_hier_run": (c_int32, [ctypes.POINTER(EdgHier), ctypes.POINTER(EdgHMC), c_int32,
+                                   c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
+                                   c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

@@ -99,3 +99,50 @@ def philox_uniform64(seed, kind, iteration, rows, device="cuda"):
     _lib.call("edg_philox_uniform64", int(seed), int(kind), int(iteration), rows, _lib.ptr(out),
               _lib.stream_ptr())
     return out
+
+
+class HierDevice:
+    """Device copy of a ragged batch of hierarchical logistic regressions
+    (instance i: X_i [N_i, D_i], y_i [N_i]) packed for edg_hmc_hier_run:
+    X and y concatenated, per-instance offsets/sizes, and a launch order that
+    starts the heaviest instances (N_i * D_i) first."""
+
+    def __init__(self, Xs, ys, mu_loc=0.0, mu_scale=1.0, tau_scale=1.0, device="cuda"):
+        _lib.require_cuda()
+        if len(Xs) != len(ys) or not Xs:
+            raise ValueError("need one y per X and at least one instance")
+        Ns = np.array([np.asarray(x).shape[0] for x in Xs], np.int32)
+        Ds = np.array([np.asarray(x).shape[1] for x in Xs], np.int32)
+        for x, y in zip(Xs, ys):
+            if np.asarray(y).reshape(-1).shape[0] != np.asarray(x).shape[0]:
+                raise ValueError("each y_i must have N_i entries")
+        self.I = len(Xs)
+        self.Ns, self.Ds = Ns, Ds
+        self.max_D = int(Ds.max())
+        x_off = np.concatenate([[0], np.cumsum(Ns.astype(np.int64) * Ds)[:-1]]).astype(np.int64)
+        y_off = np.concatenate([[0], np.cumsum(Ns.astype(np.int64))[:-1]]).astype(np.int64)
+        self.device = torch.device(device)
+        self.X = torch.as_tensor(np.concatenate([np.asarray(x, np.float32).reshape(-1) for x in Xs]),
+                                 device=self.device)
+        self.y = torch.as_tensor(np.concatenate([np.asarray(y, np.float32).reshape(-1) for y in ys]),
+                                 device=self.device)
+        self.x_off = torch.as_tensor(x_off, device=self.device)
+        self.y_off = torch.as_tensor(y_off, device=self.device)
+        self.N_t = torch.as_tensor(Ns, device=self.device)
+        self.D_t = torch.as_tensor(Ds, device=self.device)
+        work = Ns.astype(np.int64) * Ds
+        self.order = torch.as_tensor(np.argsort(-work, kind="stable").astype(np.int32),
+                                     device=self.device)
+        self.c = _lib.EdgHier()
+        self.c.X, self.c.y = self.X.data_ptr(), self.y.data_ptr()
+        self.c.x_offset, self.c.y_offset = self.x_off.data_ptr(), self.y_off.data_ptr()
+        self.c.N, self.c.D = self.N_t.data_ptr(), self.D_t.data_ptr()
+        self.c.I, self.c.max_D = self.I, self.max_D
+        self.c.mu_loc, self.c.mu_scale, self.c.tau_scale = mu_loc, mu_scale, tau_scale
+
+    @property
+    def SP(self):
+        return self.max_D + 2
+
+    def ref(self):
+        return ctypes.byref(self.c)

@@ -220,6 +220,38 @@ int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, int
                     const float* r_override, const double* u_override, double* ratio_out,
                     void* stream);
 
+/* ---------------------------------------------------------------- HMC, ragged hierarchical batch
+ * I independent hierarchical logistic regressions, each with C chains:
+ *   mu ~ Normal(mu_loc, mu_scale), tau ~ HalfNormal(tau_scale),
+ *   w_d ~ Normal(mu, tau) (d < D_i), y_n ~ Bernoulli(logits = X_i[n] . w).
+ * HMC runs on (w, mu, u) with tau = softplus(u) and the log-det-Jacobian
+ * log sigmoid(u) added, as auto_transform does for a 'nonnegative' latent
+ * (edward/util/random_variables.py:903-904; edward/inferences/hmc.py:132-159).
+ * Chain k of instance i is global chain i*C + k; its state row has stride
+ * max_D + 2 with w in [0, D_i), mu at D_i and u at D_i + 1.  z / grad: [I*C, max_D+2],
+ * lj / n_accept: [I*C]; samples [T_cap, I*C, max_D+2]; moments [2, I*C, max_D+2];
+ * r_override [n_iter, I*C, max_D+2]; u_override / ratio_out [n_iter, I*C].
+ * `order` (or NULL) is a permutation of the instances giving the launch order
+ * (heaviest first balances the ragged work).  Replaces, per instance, the
+ * same reference code as edg_hmc_glm_run. */
+typedef struct {
+  const float* X;          /* all X_i concatenated, each [N_i, D_i] row-major */
+  const float* y;          /* all y_i concatenated */
+  const int64_t* x_offset; /* [I] element offset of X_i in X */
+  const int64_t* y_offset; /* [I] element offset of y_i in y */
+  const int32_t* N;        /* [I] rows of each instance */
+  const int32_t* D;        /* [I] features of each instance (<= max_D) */
+  int32_t I;
+  int32_t max_D;           /* <= 160 */
+  float mu_loc, mu_scale, tau_scale;
+} edg_hier_t;
+
+int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
+                     const int32_t* order, float* z, float* grad, double* lj, int32_t cache_valid,
+                     int32_t* n_accept, edg_state_t* state, float* samples, int64_t T_cap,
+                     double* moments, const float* r_override, const double* u_override,
+                     double* ratio_out, void* stream);
+
 /* ---------------------------------------------------------------- HMC, tensor cores
  * Same contract as edg_hmc_glm_run, computed with tcgen05 3xTF32 GEMMs:
  * one thread-block cluster per 128 chains, the cluster's CTAs splitting the

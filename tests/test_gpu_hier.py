@@ -1,0 +1,107 @@
+"""GPU parity of the ragged hierarchical HMC kernel against the oracle."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import hier
+from oracle.hmc import hmc_step
+from oracle.philox import normals, uniforms64
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(seed=3):
+    Xs, ys = hier.synthetic_instances(5, seed=seed, n_range=(50, 700), d_range=(8, 40))
+    X2, y2 = hier.synthetic_instances(1, seed=seed + 1, n_range=(300, 300), d_range=(128, 128))
+    return Xs + X2, ys + y2
+
+
+def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None):
+    from edward_gb300 import _lib
+    cuda = z0.device
+    cfg = _lib.EdgHMC()
+    cfg.step_size, cfg.n_steps, cfg.seed = step, L, seed
+    n = hd.I * C
+    z = z0.clone()
+    g = torch.zeros_like(z)
+    lj = torch.zeros(n, dtype=torch.float64, device=cuda)
+    nacc = torch.zeros(n, dtype=torch.int32, device=cuda)
+    st = _lib.new_state(cuda)
+    ratio = torch.zeros(max(n_iter, 1), n, dtype=torch.float64, device=cuda)
+    _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(hd.order),
+              _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, _lib.ptr(nacc), _lib.ptr(st),
+              _lib.ptr(samples), samples.shape[0] if samples is not None else 0, None,
+              _lib.ptr(r), _lib.ptr(u), _lib.ptr(ratio), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    return z, g, lj, nacc, ratio, _lib.read_state(st)
+
+
+def test_hier_iteration_parity(cuda):
+    from edward_gb300.ops import HierDevice
+    Xs, ys = _instances()
+    kw = dict(mu_loc=0.1, mu_scale=1.2, tau_scale=0.8)
+    hd = HierDevice(Xs, ys, **kw)
+    C, L, step = 40, 3, 0.01
+    SP = hd.SP
+    rng = np.random.default_rng(0)
+    z0 = np.zeros((hd.I * C, SP), np.float32)
+    r0 = np.zeros((1, hd.I * C, SP), np.float32)
+    for i, X in enumerate(Xs):
+        D = X.shape[1]
+        z0[i * C:(i + 1) * C, :D + 2] = rng.standard_normal((C, D + 2)) * 0.2
+        r0[0, i * C:(i + 1) * C, :D + 2] = rng.standard_normal((C, D + 2))
+    u = rng.random((1, hd.I * C))
+    z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
+                                     r=torch.as_tensor(r0, device=cuda),
+                                     u=torch.as_tensor(u, device=cuda))
+    assert st.t == 1
+    zk, rk, ak = z.cpu().numpy(), ratio.cpu().numpy()[0], nacc.cpu().numpy().astype(bool)
+    for i, (X, y) in enumerate(zip(Xs, ys)):
+        D = X.shape[1]
+        sl = slice(i * C, (i + 1) * C)
+        f = hier.lj_grad_fn(X, y, **kw)
+        zi = z0[sl, :D + 2].astype(np.float64)
+        lj0, g0 = f(zi)
+        res = hmc_step(f, zi, g0, lj0, r0[0, sl, :D + 2], u[0, sl], step, L)
+        scale = max(np.abs(lj0).max(), np.abs(res["lj"]).max())
+        np.testing.assert_allclose(rk[sl], res["ratio"], rtol=0, atol=1e-5 * scale)
+        differ = ak[sl] != res["accept"]
+        assert np.all(np.abs(np.log(u[0, sl]) - res["ratio"])[differ] < 1e-3)
+        same = ~differ
+        exp = res["z"][same]
+        np.testing.assert_allclose(zk[sl, :D + 2][same], exp, rtol=1e-4,
+                                   atol=1e-4 * np.abs(exp).max())
+
+
+def test_hier_in_kernel_rng_two_iterations(cuda):
+    from edward_gb300.ops import HierDevice
+    Xs, ys = _instances(seed=9)
+    hd = HierDevice(Xs, ys)
+    C, L, step, T, seed = 33, 2, 0.02, 2, 11
+    SP = hd.SP
+    z0 = np.zeros((hd.I * C, SP), np.float32)
+    rng = np.random.default_rng(1)
+    for i, X in enumerate(Xs):
+        z0[i * C:(i + 1) * C, :X.shape[1] + 2] = rng.standard_normal((C, X.shape[1] + 2)) * 0.1
+    samples = torch.zeros(T, hd.I * C, SP, device=cuda)
+    z, _, _, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), T, step, L,
+                                    seed=seed, samples=samples)
+    assert st.t == T
+    sk = samples.cpu().numpy()
+    rk = ratio.cpu().numpy()
+    for i, (X, y) in enumerate(zip(Xs, ys)):
+        D = X.shape[1]
+        f = hier.lj_grad_fn(X, y)
+        zi = z0[i * C:(i + 1) * C, :D + 2].astype(np.float64)
+        lj, gr = f(zi)
+        for t in range(T):
+            r0 = normals(seed, 1, t, C, D + 2, row0=i * C)
+            uu = uniforms64(seed, 2, t, C, row0=i * C)
+            res = hmc_step(f, zi, gr, lj, r0, uu, step, L)
+            scale = max(np.abs(lj).max(), 1.0)
+            np.testing.assert_allclose(rk[t, i * C:(i + 1) * C], res["ratio"], rtol=0,
+                                       atol=2e-5 * scale)
+            zi = sk[t, i * C:(i + 1) * C, :D + 2].astype(np.float64)  # resync on kept states
+            lj, gr = f(zi)
