@@ -194,3 +194,72 @@ def parse_normal_q(qz):
     if not (isinstance(sc, Op) and sc.op == "softplus" and isinstance(sc.args[0], Variable)):
         raise UnsupportedModel("q scale must be softplus(Variable)")
     return NormalQ(qz.loc, sc.args[0])
+
+
+# ------------------------------------------------------------- hierarchical family
+
+@dataclass
+class HierSpec:
+    """Ragged batch of hierarchical logistic regressions (one model instance
+    per (X_i, y_i)): mu ~ N(mu_loc, mu_scale), tau ~ HalfNormal(tau_scale)
+    with support 'nonnegative', w ~ N(mu, tau) elementwise, y ~ Bernoulli(X w)."""
+    Xs: list
+    ys: list
+    mu_loc: float
+    mu_scale: float
+    tau_scale: float
+    w: RandomVariable = None
+    mu: RandomVariable = None
+    tau: RandomVariable = None
+
+
+def _strip_ones(node):
+    """x, x * ones(..) or ones(..) * x  ->  x."""
+    if isinstance(node, Op) and node.op == "mul":
+        a, b = node.args
+        for u, v in ((a, b), (b, a)):
+            cv = const_value(v)
+            if cv is not None and np.all(cv == 1.0):
+                return u
+    return node
+
+
+def compile_hier(latents, data):
+    """Recognises  mu ~ Normal, tau ~ HalfNormal (support 'nonnegative'),
+    w ~ Normal(mu, tau), y ~ Bernoulli(logits = ed.dot(X, w)).  X and y may be
+    bound to lists of arrays: each element is one independent instance."""
+    from .models import HalfNormal
+    observed, bindings = _split_data(data)
+    if len(observed) != 1:
+        raise UnsupportedModel("the hierarchical family has one observed variable")
+    (yrv, yval), = observed.items()
+    if not (isinstance(yrv, Bernoulli) and yrv.logits is not None):
+        raise UnsupportedModel("hierarchical family: y must be Bernoulli(logits=ed.dot(X, w))")
+    eta = yrv.logits
+    if not (isinstance(eta, Op) and eta.op == "dot" and isinstance(eta.args[1], Normal)):
+        raise UnsupportedModel("hierarchical family: logits must be ed.dot(X, w)")
+    Xn, w = eta.args
+    mu, tau = _strip_ones(w.loc), _strip_ones(w.scale)
+    if not (isinstance(mu, Normal) and isinstance(tau, HalfNormal)):
+        raise UnsupportedModel("hierarchical family: w ~ Normal(mu, tau), mu Normal, tau HalfNormal")
+    if set(map(id, latents)) != {id(w), id(mu), id(tau)}:
+        raise UnsupportedModel("hierarchical family: latent variables must be exactly w, mu, tau")
+    if getattr(tau, "support", None) != "nonnegative":
+        raise UnsupportedModel("set tau.support = 'nonnegative' so that auto_transform samples "
+                               "u = softplus^{-1}(tau) on the real line")
+    if isinstance(Xn, Placeholder):
+        Xv = bindings.get(Xn)
+    else:
+        Xv = const_value(Xn)
+    if Xv is None:
+        raise UnsupportedModel("X must be data")
+    Xs = list(Xv) if isinstance(Xv, (list, tuple)) else [np.asarray(Xv, np.float32)]
+    ys = list(yval) if isinstance(yval, (list, tuple)) else [np.asarray(yval, np.float32)]
+    if len(Xs) != len(ys):
+        raise ValueError("X and y must hold the same number of instances")
+    Xs = [np.ascontiguousarray(np.asarray(x, np.float32)) for x in Xs]
+    ys = [np.asarray(v, np.float32).reshape(-1) for v in ys]
+    mu_loc = float(_const_param(mu.loc, "mu loc", bindings).reshape(-1)[0])
+    mu_scale = float(_const_param(mu.scale, "mu scale", bindings).reshape(-1)[0])
+    tau_scale = float(_const_param(tau.scale, "tau scale", bindings).reshape(-1)[0])
+    return HierSpec(Xs, ys, mu_loc, mu_scale, tau_scale, w=w, mu=mu, tau=tau)

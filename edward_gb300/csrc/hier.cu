@@ -3,7 +3,8 @@
 // Instance i: X_i [N_i, D_i], y_i [N_i];  mu ~ N(mu_loc, mu_scale),
 // tau ~ HalfNormal(tau_scale) sampled as u = softplus^{-1}(tau),
 // w_d ~ N(mu, tau), y ~ Bernoulli(X_i w).  C chains per instance, state per
-// chain (w [D_i], mu, u) stored with a fixed stride SP = max_D + 2.
+// chain stored with a fixed stride SP = max_D + 2: w in [0, D_i), zeros up to
+// max_D, mu at SP - 2 and u at SP - 1.
 //
 // One CTA per (instance, 32 chains).  Every gradient evaluation streams the
 // instance's X through shared memory with glm_grad_eval (forward + adjoint
@@ -147,10 +148,10 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
     const int c = threadIdx.x;
     const bool ok = c < nc;
     const size_t g = gchain(ok ? c : 0) * SP;
-    mu0[c] = ok ? a.z[g + D] : 0.0f;
-    u0[c] = ok ? a.z[g + D + 1] : 0.0f;
-    gmu0[c] = (ok && a.cache_valid) ? a.grad[g + D] : 0.0f;
-    gu0[c] = (ok && a.cache_valid) ? a.grad[g + D + 1] : 0.0f;
+    mu0[c] = ok ? a.z[g + SP - 2] : 0.0f;
+    u0[c] = ok ? a.z[g + SP - 1] : 0.0f;
+    gmu0[c] = (ok && a.cache_valid) ? a.grad[g + SP - 2] : 0.0f;
+    gu0[c] = (ok && a.cache_valid) ? a.grad[g + SP - 1] : 0.0f;
     lj0[c] = (ok && a.cache_valid) ? a.lj[gchain(c)] : 0.0;
   }
   __syncthreads();
@@ -189,7 +190,7 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
   for (int it = 0; it < a.n_iter; ++it) {
     const int64_t t = t0 + it;
     const uint32_t iter = (uint32_t)t;
-    // momenta for (w, mu, u); coordinate index d < D is w_d, D is mu, D + 1 is u
+    // momenta for (w, mu, u): Philox elements 0..D-1 are w, D is mu, D + 1 is u
     for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
       const int c = idx / PP, d = idx - c * PP;
       float r = 0.0f;
@@ -206,8 +207,8 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
       if (c < nc) {
         if (a.r_ovr) {
           const size_t b = ((size_t)it * a.I * a.C + gchain(c)) * SP;
-          r1 = a.r_ovr[b + D];
-          r2 = a.r_ovr[b + D + 1];
+          r1 = a.r_ovr[b + SP - 2];
+          r2 = a.r_ovr[b + SP - 1];
         } else {
           r1 = philox_normal(a.seed, 1u, iter, (uint32_t)gchain(c), (uint32_t)D);
           r2 = philox_normal(a.seed, 1u, iter, (uint32_t)gchain(c), (uint32_t)(D + 1));
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
     for (int idx = threadIdx.x; idx < nc * W; idx += kThreads) {
       const int c = idx / W, d = idx - c * W;
       const float v = d < D ? Z0[c * PP + d] : (d == D ? mu0[c] : u0[c]);
-      const size_t g = gchain(c) * SP + d;
+      const size_t g = gchain(c) * SP + (d < D ? d : SP - 2 + (d - D));
       if (a.samples && t < a.T_cap) a.samples[(size_t)t * a.I * a.C * SP + g] = v;
       if (a.moments) {
         a.moments[g] += (double)v;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
   // write back the state and its cache
   for (int idx = threadIdx.x; idx < nc * (D + 2); idx += kThreads) {
     const int c = idx / (D + 2), d = idx - c * (D + 2);
-    const size_t g = gchain(c) * SP + d;
+    const size_t g = gchain(c) * SP + (d < D ? d : SP - 2 + (d - D));
     a.z[g] = d < D ? Z0[c * PP + d] : (d == D ? mu0[c] : u0[c]);
     a.grad[g] = d < D ? G0[c * PP + d] : (d == D ? gmu0[c] : gu0[c]);
   }

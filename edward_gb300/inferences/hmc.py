@@ -14,8 +14,8 @@ import numpy as np
 import torch
 
 from .. import _lib, autotune
-from ..compile import compile_glm
-from ..ops import GLMDevice
+from ..compile import UnsupportedModel, compile_glm, compile_hier
+from ..ops import GLMDevice, HierDevice
 from ..util import next_seed
 from .monte_carlo import MonteCarlo
 
@@ -44,17 +44,29 @@ class HMC(MonteCarlo):
                              "initialize with auto_transform=True to ensure "
                              "this. (if your variables already have unconstrained "
                              "support then doing this is a no-op).")
-        for z, qz in self.latent_vars.items():
-            if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
-                raise NotImplementedError(
-                    f"auto_transform of support '{z.support}' for this model family")
-        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        try:
+            self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+            self._family = "glm"
+        except UnsupportedModel as e_glm:
+            try:
+                self._spec = compile_hier(list(self.latent_vars.keys()), self.data)
+                self._family = "hier"
+            except UnsupportedModel as e_hier:
+                raise UnsupportedModel(f"model is neither in the GLM family ({e_glm}) nor in "
+                                       f"the hierarchical family ({e_hier})") from None
+        if self._family == "glm":
+            for z in self.latent_vars:
+                if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
+                    raise NotImplementedError(
+                        f"auto_transform of support '{z.support}' for this model family")
         C = self.n_chains or 1
         for qz in self.latent_vars.values():
             if (qz.n_chains or 1) != C:
                 raise ValueError("every Empirical must hold the same number of chains")
 
     def build_update(self):
+        if self._family == "hier":
+            return self._build_hier()
         spec = self._spec
         self._glm = GLMDevice(spec, self._device)
         C = self.n_chains or 1
@@ -139,7 +151,60 @@ class HMC(MonteCarlo):
         key = f"N{self._spec.N}_D{self._spec.D}_b{int(self._spec.bias)}_C{C}_L{self.n_steps}"
         return autotune.choose("hmc_glm", key, cands, run)
 
+    def _build_hier(self):
+        """Ragged batch of hierarchical logistic regressions (edg_hmc_hier_run).
+        Samples live in one [T, I*C, max_D + 2] store (w, zeros, mu, u); the
+        Empiricals are views of it (tau is shown as softplus(u))."""
+        spec = self._spec
+        hd = HierDevice(spec.Xs, spec.ys, spec.mu_loc, spec.mu_scale, spec.tau_scale,
+                        self._device)
+        self._hier = hd
+        C = self.n_chains or 1
+        self.C = C
+        I, SP, T = hd.I, hd.SP, self.n_iter
+        dev = self._device
+        self._samples = torch.zeros(T, I * C, SP, dtype=torch.float32, device=dev)
+        view = self._samples.view(T, I, C, SP)
+        lead = (T, I) if I > 1 else (T,)
+        lead = lead + ((C,) if self.n_chains else ())
+        Dmax = hd.max_D
+        parts = {spec.w: view[..., :Dmax], spec.mu: view[..., SP - 2], spec.tau: view[..., SP - 1]}
+        for z, v in parts.items():
+            qz = self.latent_vars[z]
+            init = qz.params_var.value
+            tgt = v[0]
+            if init[0].numel() == tgt.numel():
+                tgt.copy_(init[0].to(dev).reshape(tgt.shape))
+            # else (ragged w declared with another width): the chains start from zeros
+            shape = lead + ((Dmax,) if z is spec.w else ())
+            qz.params_var._value = v.view(shape)
+            qz.params_var.shape = shape
+            qz.n = T
+        self.latent_vars[spec.tau]._constrain = torch.nn.functional.softplus
+        self._z = self._samples[0].clone()
+        self._g = torch.zeros_like(self._z)
+        self._lj = torch.zeros(I * C, dtype=torch.float64, device=dev)
+        self._cache_valid = 0
+        self._n_accept = torch.zeros(I * C, dtype=torch.int32, device=dev)
+        cfg = _lib.EdgHMC()
+        cfg.step_size = float(self.step_size)
+        cfg.n_steps = int(self.n_steps)
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        self.engine = "hier"
+        self.train = self.update
+        return self.train
+
     def _launch(self, n_iter, r_override=None, u_override=None, ratio_out=None):
+        if self.engine == "hier":
+            _lib.call("edg_hmc_hier_run", self._hier.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),
+                      _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
+                      _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
+                      self._samples.shape[0], None, _lib.ptr(r_override), _lib.ptr(u_override),
+                      _lib.ptr(ratio_out), _lib.stream_ptr())
+            self._cache_valid = 1
+            return
         if self.engine == "tc":
             _lib.call("edg_hmc_glm_tc_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
                       int(n_iter), _lib.ptr(self._tiles), _lib.ptr(self._z), _lib.ptr(self._g),
@@ -169,7 +234,7 @@ class HMC(MonteCarlo):
             raise NotImplementedError("feed_dict is not supported for this model family")
         self._launch(1)
         t = self.t
-        acc = float(self._n_accept.sum().item()) / (max(t, 1) * self.C)
+        acc = float(self._n_accept.sum().item()) / (max(t, 1) * self._n_accept.numel())
         return {"t": t, "accept_rate": acc}
 
     def _run_loop(self):
@@ -180,7 +245,7 @@ class HMC(MonteCarlo):
             self._launch(k)
             done += k
             t = self.t
-            acc = float(self._n_accept.sum().item()) / (max(t, 1) * self.C)
+            acc = float(self._n_accept.sum().item()) / (max(t, 1) * self._n_accept.numel())
             self.print_progress({"t": t, "accept_rate": acc})
 
     def run_iterations(self, k, r_override=None, u_override=None, ratio_out=None):
@@ -189,7 +254,7 @@ class HMC(MonteCarlo):
 
     @property
     def n_accept(self):
-        if self.C == 1 and not self.n_chains:
+        if self._n_accept.numel() == 1:
             return int(self._n_accept[0].item())
         return self._n_accept
 

@@ -190,10 +190,16 @@ class Empirical(RandomVariable):
         if n_chains is not None and (len(shp) < 2 or shp[1] != n_chains):
             raise ValueError(f"Empirical params with n_chains={n_chains} must have shape [T, C, ...]")
         self.n = shp[0]
+        self._constrain = None
 
     @property
     def params(self):
-        return self.params_var.value
+        """Samples [T, ...]; for a latent sampled in an unconstrained space the
+        stored values are mapped back through the transform, as
+        ``qz_constrained.params = bijector.inverse(params)`` does in the reference
+        (``edward/inferences/inference.py:247-253``)."""
+        v = self.params_var.value
+        return self._constrain(v) if self._constrain is not None else v
 
     @property
     def event_shape(self):

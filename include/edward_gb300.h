@@ -228,7 +228,7 @@ int edg_hmc_glm_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, int
  * log sigmoid(u) added, as auto_transform does for a 'nonnegative' latent
  * (edward/util/random_variables.py:903-904; edward/inferences/hmc.py:132-159).
  * Chain k of instance i is global chain i*C + k; its state row has stride
- * max_D + 2 with w in [0, D_i), mu at D_i and u at D_i + 1.  z / grad: [I*C, max_D+2],
+ * SP = max_D + 2 with w in [0, D_i) (zeros up to max_D), mu at SP-2, u at SP-1.  z / grad: [I*C, max_D+2],
  * lj / n_accept: [I*C]; samples [T_cap, I*C, max_D+2]; moments [2, I*C, max_D+2];
  * r_override [n_iter, I*C, max_D+2]; u_override / ratio_out [n_iter, I*C].
  * `order` (or NULL) is a permutation of the instances giving the launch order

@@ -48,10 +48,11 @@ def test_hier_iteration_parity(cuda):
     rng = np.random.default_rng(0)
     z0 = np.zeros((hd.I * C, SP), np.float32)
     r0 = np.zeros((1, hd.I * C, SP), np.float32)
+    cols = lambda D: list(range(D)) + [SP - 2, SP - 1]   # noqa: E731  (w, mu, u)
     for i, X in enumerate(Xs):
         D = X.shape[1]
-        z0[i * C:(i + 1) * C, :D + 2] = rng.standard_normal((C, D + 2)) * 0.2
-        r0[0, i * C:(i + 1) * C, :D + 2] = rng.standard_normal((C, D + 2))
+        z0[i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2)) * 0.2
+        r0[0, i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2))
     u = rng.random((1, hd.I * C))
     z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
                                      r=torch.as_tensor(r0, device=cuda),
@@ -62,16 +63,16 @@ def test_hier_iteration_parity(cuda):
         D = X.shape[1]
         sl = slice(i * C, (i + 1) * C)
         f = hier.lj_grad_fn(X, y, **kw)
-        zi = z0[sl, :D + 2].astype(np.float64)
+        zi = z0[sl][:, cols(D)].astype(np.float64)
         lj0, g0 = f(zi)
-        res = hmc_step(f, zi, g0, lj0, r0[0, sl, :D + 2], u[0, sl], step, L)
+        res = hmc_step(f, zi, g0, lj0, r0[0, sl][:, cols(D)], u[0, sl], step, L)
         scale = max(np.abs(lj0).max(), np.abs(res["lj"]).max())
         np.testing.assert_allclose(rk[sl], res["ratio"], rtol=0, atol=1e-5 * scale)
         differ = ak[sl] != res["accept"]
         assert np.all(np.abs(np.log(u[0, sl]) - res["ratio"])[differ] < 1e-3)
         same = ~differ
         exp = res["z"][same]
-        np.testing.assert_allclose(zk[sl, :D + 2][same], exp, rtol=1e-4,
+        np.testing.assert_allclose(zk[sl][:, cols(D)][same], exp, rtol=1e-4,
                                    atol=1e-4 * np.abs(exp).max())
 
 
@@ -83,8 +84,9 @@ def test_hier_in_kernel_rng_two_iterations(cuda):
     SP = hd.SP
     z0 = np.zeros((hd.I * C, SP), np.float32)
     rng = np.random.default_rng(1)
+    cols = lambda D: list(range(D)) + [SP - 2, SP - 1]   # noqa: E731
     for i, X in enumerate(Xs):
-        z0[i * C:(i + 1) * C, :X.shape[1] + 2] = rng.standard_normal((C, X.shape[1] + 2)) * 0.1
+        z0[i * C:(i + 1) * C, cols(X.shape[1])] = rng.standard_normal((C, X.shape[1] + 2)) * 0.1
     samples = torch.zeros(T, hd.I * C, SP, device=cuda)
     z, _, _, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), T, step, L,
                                     seed=seed, samples=samples)
@@ -94,7 +96,7 @@ def test_hier_in_kernel_rng_two_iterations(cuda):
     for i, (X, y) in enumerate(zip(Xs, ys)):
         D = X.shape[1]
         f = hier.lj_grad_fn(X, y)
-        zi = z0[i * C:(i + 1) * C, :D + 2].astype(np.float64)
+        zi = z0[i * C:(i + 1) * C][:, cols(D)].astype(np.float64)
         lj, gr = f(zi)
         for t in range(T):
             r0 = normals(seed, 1, t, C, D + 2, row0=i * C)
@@ -103,5 +105,37 @@ def test_hier_in_kernel_rng_two_iterations(cuda):
             scale = max(np.abs(lj).max(), 1.0)
             np.testing.assert_allclose(rk[t, i * C:(i + 1) * C], res["ratio"], rtol=0,
                                        atol=2e-5 * scale)
-            zi = sk[t, i * C:(i + 1) * C, :D + 2].astype(np.float64)  # resync on kept states
+            zi = sk[t, i * C:(i + 1) * C][:, cols(D)].astype(np.float64)  # resync on kept states
             lj, gr = f(zi)
+
+
+def test_hier_public_api_ragged_batch(cuda):
+    """Edward-style model code: mu ~ N(0,1), tau ~ HalfNormal(1) with support
+    'nonnegative', w ~ N(mu, tau), y ~ Bernoulli(X w); X and y bound to lists
+    of arrays form a ragged batch of independent instances."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Empirical, HalfNormal, Normal
+    Xs, ys = hier.synthetic_instances(6, seed=21, n_range=(100, 1500), d_range=(5, 30))
+    Dmax = max(x.shape[1] for x in Xs)
+    X = ed.placeholder(np.float32, [None, None])
+    mu = Normal(loc=0.0, scale=1.0)
+    tau = HalfNormal(scale=1.0)
+    tau.support = "nonnegative"
+    w = Normal(loc=mu * ed.ones(Dmax), scale=tau * ed.ones(Dmax))
+    y = Bernoulli(logits=ed.dot(X, w))
+    T, C = 300, 16
+    qw = Empirical(ed.Variable(np.zeros((T, 6, C, Dmax), np.float32)), n_chains=None)
+    qmu = Empirical(ed.Variable(np.zeros((T, 6, C), np.float32)))
+    qtau = Empirical(ed.Variable(np.zeros((T, 6, C), np.float32)))
+    inf = ed.HMC({w: qw, mu: qmu, tau: qtau}, data={X: Xs, y: ys}, n_chains=C)
+    inf.run(step_size=0.02, n_steps=8, n_print=0)
+    assert inf.engine == "hier" and inf.t == T
+    acc = inf.n_accept.float().mean().item() / T
+    assert 0.2 < acc <= 1.0
+    taus = qtau.params[T // 2:]
+    assert torch.all(taus > 0)
+    # posterior mean of w per instance correlates with the truth-generating direction
+    wm = qw.params[T // 2:].mean(dim=(0, 2)).cpu().numpy()
+    for i, (Xi, yi) in enumerate(zip(Xs, ys)):
+        D = Xi.shape[1]
+        assert np.all(np.isfinite(wm[i, :D])) and np.all(wm[i, D:] == 0)
