@@ -59,10 +59,11 @@ class HMC(MonteCarlo):
                 if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
                     raise NotImplementedError(
                         f"auto_transform of support '{z.support}' for this model family")
-        C = self.n_chains or 1
-        for qz in self.latent_vars.values():
-            if (qz.n_chains or 1) != C:
-                raise ValueError("every Empirical must hold the same number of chains")
+        if self._family == "glm":
+            C = self.n_chains or 1
+            for qz in self.latent_vars.values():
+                if (qz.n_chains or 1) != C:
+                    raise ValueError("every Empirical must hold the same number of chains")
 
     def build_update(self):
         if self._family == "hier":
