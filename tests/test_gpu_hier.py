@@ -52,7 +52,7 @@ def test_hier_iteration_parity(cuda):
     for i, X in enumerate(Xs):
         D = X.shape[1]
         z0[i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2)) * 0.2
-        r0[0, i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2))
+        r0[0][i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2))
     u = rng.random((1, hd.I * C))
     z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
                                      r=torch.as_tensor(r0, device=cuda),
@@ -65,7 +65,7 @@ def test_hier_iteration_parity(cuda):
         f = hier.lj_grad_fn(X, y, **kw)
         zi = z0[sl][:, cols(D)].astype(np.float64)
         lj0, g0 = f(zi)
-        res = hmc_step(f, zi, g0, lj0, r0[0, sl][:, cols(D)], u[0, sl], step, L)
+        res = hmc_step(f, zi, g0, lj0, r0[0][sl][:, cols(D)], u[0, sl], step, L)
         scale = max(np.abs(lj0).max(), np.abs(res["lj"]).max())
         np.testing.assert_allclose(rk[sl], res["ratio"], rtol=0, atol=1e-5 * scale)
         differ = ak[sl] != res["accept"]
