@@ -99,6 +99,8 @@ def compile_glm(latents, data):
     (yrv, yval), = observed.items()
     if isinstance(yval, RandomVariable):
         raise UnsupportedModel("observed values must be arrays, not random variables")
+    if isinstance(yval, (list, tuple)) and yval and np.ndim(yval[0]) > 0:
+        raise UnsupportedModel("a list of observed arrays (ragged instances) is not a GLM")
     y = np.asarray(yval, np.float32).reshape(-1)
     if isinstance(yrv, Bernoulli):
         if yrv.logits is None:
@@ -120,6 +122,8 @@ def compile_glm(latents, data):
             Xn, w = term.args
             if not isinstance(w, RandomVariable) or id(w) not in latent_set:
                 raise UnsupportedModel("ed.dot(X, w) needs w to be a latent random variable")
+            if isinstance(Xn, Placeholder) and isinstance(bindings.get(Xn), (list, tuple)):
+                raise UnsupportedModel("X bound to a list (ragged instances) is not a GLM")
             X = const_value(Xn, bindings)
             if X is None:
                 raise UnsupportedModel("X in ed.dot(X, w) must be data (an array or a bound placeholder)")

@@ -149,3 +149,42 @@ def test_scale_must_be_dict():
     inf = ed.KLqp(lat, data={y: np.zeros(20)})
     with pytest.raises(TypeError, match="scale must be a dict"):
         inf.initialize(scale=3.0)
+
+
+def _hier_model(Dmax=7):
+    X = ed.placeholder(np.float32, [None, None])
+    mu = Normal(loc=0.0, scale=1.0)
+    tau = HalfNormal(scale=1.0)
+    tau.support = "nonnegative"
+    w = Normal(loc=mu * ed.ones(Dmax), scale=tau * ed.ones(Dmax))
+    y = Bernoulli(logits=ed.dot(X, w))
+    return X, mu, tau, w, y
+
+
+def test_compile_hierarchical_ragged_lists():
+    from edward_gb300.compile import compile_hier
+    X, mu, tau, w, y = _hier_model()
+    Xs = [np.ones((5, 3), np.float32), np.ones((9, 7), np.float32)]
+    ys = [np.zeros(5), np.ones(9)]
+    with pytest.raises(NotImplementedError):
+        compile_glm([w, mu, tau], {X: Xs, y: ys})
+    spec = compile_hier([w, mu, tau], {X: Xs, y: ys})
+    assert len(spec.Xs) == 2 and spec.Xs[1].shape == (9, 7) and spec.tau_scale == 1.0
+    assert spec.w is w and spec.mu is mu and spec.tau is tau
+
+
+def test_compile_hierarchical_requires_nonnegative_support():
+    from edward_gb300.compile import compile_hier
+    X, mu, tau, w, y = _hier_model()
+    tau.support = None
+    with pytest.raises(NotImplementedError, match="nonnegative"):
+        compile_hier([w, mu, tau], {X: [np.ones((4, 7))], y: [np.zeros(4)]})
+
+
+def test_hmc_validates_hierarchical_model_on_host():
+    X, mu, tau, w, y = _hier_model()
+    inf = ed.HMC([w, mu, tau], data={X: [np.ones((5, 7), np.float32)], y: [np.zeros(5)]},
+                 n_chains=4)
+    inf.auto_transform = True
+    inf._validate()
+    assert inf._family == "hier"
