@@ -375,6 +375,136 @@ def read_traffic(engine):
     return None
 
 
+# ------------------------------------------------------------------ secondary workloads
+
+def _peak_3xtf32():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+        src = "MEASURED_PEAKS.json bf16_tflops"
+    except (OSError, KeyError, ValueError):
+        bf16, src = 1900.0, "fallback 1.9 PFLOP/s bf16"
+    return bf16 / 6.0, f"{src} {bf16:g} / 2 (TF32 rate) / 3 (3xTF32 passes), of measured"
+
+
+def hier_data(I=2048, seed=0):
+    """Ragged hierarchical logistic regressions: N_i log-uniform in [50, 20000],
+    D_i uniform in {8..128}, X ~ N(0,1), w_i ~ N(mu_i, tau_i^2), mu_i ~ N(0,1),
+    tau_i ~ HalfNormal(1), y ~ Bernoulli(sigmoid(X w_i))."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    Ns = np.exp(rng.uniform(np.log(50), np.log(20000), I)).astype(np.int64)
+    Ds = rng.integers(8, 129, I)
+    Xs, ys = [], []
+    for N, D in zip(Ns, Ds):
+        X = rng.standard_normal((N, D), dtype=np.float32)
+        w = rng.standard_normal() + abs(rng.standard_normal()) * rng.standard_normal(D)
+        eta = X @ w.astype(np.float32)
+        y = (rng.random(N) < 1.0 / (1.0 + np.exp(-np.clip(eta, -60, 60)))).astype(np.float32)
+        Xs.append(X)
+        ys.append(y)
+    return Xs, ys
+
+
+def run_hier(args):
+    """All 2,048 instances x 64 chains, 10 leapfrog steps per iteration, one
+    launch per iteration (edg_hmc_hier_run)."""
+    import ctypes
+    import numpy as np
+    import torch
+    from edward_gb300 import _lib
+    from edward_gb300.ops import HierDevice
+    C, L = 64, 10
+    Xs, ys = hier_data()
+    hd = HierDevice(Xs, ys)
+    dev = torch.device("cuda")
+    n = hd.I * C
+    z = torch.zeros(n, hd.SP, device=dev)
+    g = torch.zeros_like(z)
+    lj = torch.zeros(n, dtype=torch.float64, device=dev)
+    nacc = torch.zeros(n, dtype=torch.int32, device=dev)
+    st = _lib.new_state(dev)
+    cfg = _lib.EdgHMC()
+    cfg.step_size, cfg.n_steps, cfg.seed = 0.01, L, 1
+    sp = _lib.stream_ptr()
+    state = {"cache": 0}
+
+    def step():
+        _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
+                  _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), state["cache"], _lib.ptr(nacc),
+                  _lib.ptr(st), None, 0, None, None, None, None, sp)
+        state["cache"] = 1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        a.record()
+        for _ in range(args.steps):
+            step()
+        b.record()
+        b.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    work = float((hd.Ns.astype(np.int64) * hd.Ds).sum())
+    flops = 4.0 * work * C * L
+    peak, src = _peak_3xtf32()
+    ach = flops / (ms / 1e3) / 1e12
+    line = {"metric": "HMC leapfrog chain-steps/s (2048 ragged hierarchical logistic regressions)",
+            "value": n * L / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "hier_ragged_I2048_C64_L10", "instances": hd.I, "chains": C,
+                       "leapfrog_steps": L, "sum_N_D": int(work),
+                       "x_bytes": int(work * 4),
+                       "l2_flush": "inputs larger than L2 (X is %.2f GB)" % (work * 4 / 1e9)},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                         "frac": ach / peak, "traffic": None, "kernel": "hmc_hier_kernel<32> (SIMT FP32)",
+                         "peak_source": src, "algorithmic_flops_per_launch": flops,
+                         "x_stream_GBs": 2 * L * work * 4 / (ms / 1e3) / 1e9},
+            "accept_rate": float(nacc.sum().item()) / (n * (args.warmup + args.steps)),
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_klqp(args):
+    """KLqp (analytic KL, S = 5) on the 10,000 x 50 logistic regression; one
+    fused launch per ELBO-gradient step + Adam apply, replayed from a CUDA graph."""
+    import numpy as np
+    import torch
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Normal
+    X, y, _ = make_data()
+    w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
+    b = Normal(loc=0.0, scale=1.0)
+    yv = Bernoulli(logits=ed.dot(X, w) + b)
+    inf = ed.KLqp([w, b], data={yv: y})
+    inf.initialize(n_samples=5, n_iter=1000, n_print=0)
+    inf.steps(50)
+    inf.steps(50)
+    torch.cuda.synchronize()
+    K = max(args.steps, 100) // 50 * 50
+    a, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(K // 50):
+        inf.steps(50)
+    b2.record()
+    b2.synchronize()
+    ms = a.elapsed_time(b2) / K
+    st = inf._read_state()
+    line = {"metric": "KLqp ELBO-grad evals/s (Bayesian logistic regression, S=5)",
+            "value": 1e3 / ms, "unit": "evals/s", "n_gpus": 1, "steps": K,
+            "warmup": 100, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "klqp_logreg_N10000_D50_S5", "launch": "CUDA graph of 50 fused steps",
+                       "l2_flush": "none (X is 2 MB, L2-resident by design; latency-bound)"},
+            "gpu_launches": K, "final_loss": float(st.loss), "t": int(st.t)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,11 +515,17 @@ def main():
     ap.add_argument("--engine", default="auto", choices=["auto", "tc", "simt"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp"],
+                    help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "hier":
+        return run_hier(args)
+    if args.workload == "klqp":
+        return run_klqp(args)
     return run_gpu(args)
 
 
