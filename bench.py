@@ -415,7 +415,7 @@ def run_hier(args):
     from edward_gb300 import _lib
     from edward_gb300.ops import HierDevice
     C, L = 64, 10
-    Xs, ys = hier_data()
+    Xs, ys = hier_data(I=args.hier_instances)
     hd = HierDevice(Xs, ys)
     dev = torch.device("cuda")
     n = hd.I * C
@@ -454,7 +454,7 @@ def run_hier(args):
             "value": n * L / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "hier_ragged_I2048_C64_L10", "instances": hd.I, "chains": C,
+            "config": {"workload": f"hier_ragged_I{hd.I}_C64_L10", "instances": hd.I, "chains": C,
                        "leapfrog_steps": L, "sum_N_D": int(work),
                        "x_bytes": int(work * 4),
                        "l2_flush": "inputs larger than L2 (X is %.2f GB)" % (work * 4 / 1e9)},
@@ -515,6 +515,7 @@ def main():
     ap.add_argument("--engine", default="auto", choices=["auto", "tc", "simt"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--hier-instances", type=int, default=2048)
     ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
