@@ -60,6 +60,12 @@ class EdgHier(ctypes.Structure):
                 ("mu_loc", c_float), ("mu_scale", c_float), ("tau_scale", c_float)]
 
 
+class EdgBNN(ctypes.Structure):
+    _fields_ = [("D", c_int32), ("H1", c_int32), ("H2", c_int32), ("n_samples", c_int32),
+                ("noise", c_float), ("prior_scale", c_float), ("data_scale", c_float),
+                ("seed", c_uint64)]
+
+
 class EdgHMC(ctypes.Structure):
     _fields_ = [("step_size", c_float), ("n_steps", c_int32), ("seed", c_uint64),
                 ("chains_per_block", c_int32), ("cluster_size", c_int32)]
@@ -90,6 +96,13 @@ _SIGS = {
                                    c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
                                    c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p]),
+    "edg_bnn_num_params": (c_int32, [c_int32, c_int32, c_int32]),
+    "edg_bnn_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgBNN), c_int32]),
+    "edg_bnn_klqp_step": (c_int32, [ctypes.POINTER(EdgBNN), ctypes.POINTER(EdgOpt), c_void_p,
+                                    c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_int32, c_void_p, c_size_t, c_void_p]),
+    "edg_minibatch_gather": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_uint64,
+                                       c_void_p, c_void_p, c_void_p, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

@@ -1,0 +1,544 @@
+// Bayesian neural network regression under KLqp (analytic KL), S weight
+// samples batched: h1 = tanh(X W0 + b0), h2 = tanh(h1 W1 + b1),
+// out = h2 W2 + b2, y ~ Normal(out, noise); q = N(mu, softplus(rho)) on every
+// weight, prior N(0, prior_scale).
+//
+// One step = one minibatch ELBO gradient + optimizer apply, as a fixed
+// sequence of launches on one stream (graph-capturable):
+//   sample   theta_s = mu + sigma * eps_s (Philox), eps kept for the rho gradient
+//   F1, F2   batched GEMMs with fused bias + tanh epilogues
+//   head     out, residual, log-lik, dW2/db2 and dH2 = dout w2 (1 - h2^2) (in place of h2)
+//   B1       dW1_s = h1_s^T dH2_s          (written straight into the per-sample gradient)
+//   B2       dH1 = (dH2 W1^T)(1 - h1^2)    (in place of h1)
+//   B3       dW0_s = X^T dH1_s
+//   colsums  db1, db0
+//   finalize sum over samples, KL, loss, gradients w.r.t. (mu, rho), optimizer
+// Hidden activations exist only for the current minibatch (S x M), are
+// recomputed every step and are overwritten by their adjoints.
+#include <algorithm>
+
+#include "edg_common.cuh"
+
+namespace edg {
+namespace bnn {
+
+constexpr int BM = 64, BN = 64, BK = 16, kT = 256;
+
+// ------------------------------------------------------------ batched GEMM
+// C[b](m, n) = epi(b, m, n, sum_k A[b](m, k) B[b](k, n)); A(m, k) is
+// A[b*sA + m*lda + k] (or A[b*sA + k*lda + m] when TA), B(k, n) is
+// B[b*sB + k*ldb + n] (or B[b*sB + n*ldb + k] when TB).
+template <bool TA, bool TB, class Epi>
+__global__ void __launch_bounds__(kT) bgemm_kernel(const float* __restrict__ A,
+                                                   const float* __restrict__ B, float* C, int M,
+                                                   int N, int K, int lda, int ldb, int ldc,
+                                                   int64_t sA, int64_t sB, int64_t sC, Epi epi) {
+  __shared__ __align__(16) float As[2][BK][BM + 4];
+  __shared__ __align__(16) float Bs[2][BK][BN + 4];
+  const int b = blockIdx.z;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const float* Ab = A + b * sA;
+  const float* Bb = B + b * sB;
+  const int tid = threadIdx.x;
+  const int tm = tid / 16, tn = tid % 16;  // 16 x 16 threads, 4 x 4 outputs each
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+
+  auto load = [&](int buf, int k0) {
+    // 64 x 16 elements of A and of B, 4 per thread
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + r * kT;
+      // A tile: As[k][m]
+      int mm, kk;
+      if (TA) {
+        kk = e / BM;
+        mm = e % BM;
+      } else {
+        mm = e / BK;
+        kk = e % BK;
+      }
+      const int gm = m0 + mm, gk = k0 + kk;
+      float va = 0.0f;
+      if (gm < M && gk < K) va = TA ? Ab[(int64_t)gk * lda + gm] : Ab[(int64_t)gm * lda + gk];
+      As[buf][kk][mm] = va;
+      // B tile: Bs[k][n]
+      int nn, kb;
+      if (TB) {
+        nn = e / BK;
+        kb = e % BK;
+      } else {
+        kb = e / BN;
+        nn = e % BN;
+      }
+      const int gn = n0 + nn, gk2 = k0 + kb;
+      float vb = 0.0f;
+      if (gn < N && gk2 < K) vb = TB ? Bb[(int64_t)gn * ldb + gk2] : Bb[(int64_t)gk2 * ldb + gn];
+      Bs[buf][kb][nn] = vb;
+    }
+  };
+
+  const int nk = (K + BK - 1) / BK;
+  load(0, 0);
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load(buf ^ 1, (t + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[buf][kk][tm * 4]);
+      const float4 b4 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tn * 4]);
+      const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+      const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  float* Cb = C + b * sC;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + tm * 4 + i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tn * 4 + j;
+      if (n < N) Cb[(int64_t)m * ldc + n] = epi(b, m, n, acc[i][j]);
+    }
+  }
+}
+
+struct EpiIdentity {
+  __device__ float operator()(int, int, int, float v) const { return v; }
+};
+// tanh(v + bias[b][n])
+struct EpiBiasTanh {
+  const float* bias;
+  int64_t sBias;
+  __device__ float operator()(int b, int, int n, float v) const {
+    return tanhf(v + bias[b * sBias + n]);
+  }
+};
+// v * (1 - h^2) with h = H[b][m][n] (the tanh output being differentiated)
+struct EpiTanhGrad {
+  const float* H;
+  int64_t sH;
+  int ldh;
+  __device__ float operator()(int b, int m, int n, float v) const {
+    const float h = H[b * sH + (int64_t)m * ldh + n];
+    return v * (1.0f - h * h);
+  }
+};
+
+template <bool TA, bool TB, class Epi>
+static int bgemm(const float* A, const float* B, float* C, int M, int N, int K, int lda, int ldb,
+                 int ldc, int64_t sA, int64_t sB, int64_t sC, int batch, Epi epi,
+                 cudaStream_t st) {
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+  bgemm_kernel<TA, TB, Epi><<<grid, kT, 0, st>>>(A, B, C, M, N, K, lda, ldb, ldc, sA, sB, sC, epi);
+  return check_launch("bnn bgemm");
+}
+
+// ------------------------------------------------------------ sampling
+struct Layout {
+  int D, H1, H2, P;
+  int oW0, ob0, oW1, ob1, oW2, ob2;
+};
+
+__host__ __device__ inline Layout make_layout(int D, int H1, int H2) {
+  Layout L;
+  L.D = D;
+  L.H1 = H1;
+  L.H2 = H2;
+  L.oW0 = 0;
+  L.ob0 = D * H1;
+  L.oW1 = L.ob0 + H1;
+  L.ob1 = L.oW1 + H1 * H2;
+  L.oW2 = L.ob1 + H2;
+  L.ob2 = L.oW2 + H2;
+  L.P = L.ob2 + 1;
+  return L;
+}
+
+__global__ void sample_kernel(const float* __restrict__ mu, const float* __restrict__ rho, int P,
+                              int S, uint64_t seed, const edg_state_t* state,
+                              const float* __restrict__ eps_ovr, float* __restrict__ theta,
+                              float* __restrict__ eps) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)S * P) return;
+  const int s = (int)(i / P), p = (int)(i % P);
+  const uint32_t iter = (uint32_t)state->t;
+  const float e = eps_ovr ? eps_ovr[i] : philox_normal(seed, 0u, iter, (uint32_t)s, (uint32_t)p);
+  eps[i] = e;
+  theta[i] = mu[p] + softplusf(rho[p]) * e;
+}
+
+// ------------------------------------------------------------ output layer
+// One block per sample: out, residual, FP64 log-lik, dW2, db2 and
+// dH2 = dout * w2 * (1 - h2^2) written over h2.
+__global__ void __launch_bounds__(kT) head_kernel(Layout L, int M, const float* __restrict__ y,
+                                                  const float* __restrict__ theta, float* H2,
+                                                  float* __restrict__ G, double* ll_out,
+                                                  float noise, float dscale) {
+  extern __shared__ __align__(16) float sm[];
+  float* w2 = sm;             // [H2]
+  float* dout = sm + L.H2;    // [M]
+  __shared__ double red[kT / 32];
+  const int s = blockIdx.x;
+  const float* th = theta + (int64_t)s * L.P;
+  float* Hs = H2 + (int64_t)s * M * L.H2;
+  for (int k = threadIdx.x; k < L.H2; k += kT) w2[k] = th[L.oW2 + k];
+  __syncthreads();
+  const float b2 = th[L.ob2];
+  const float inv_var = 1.0f / (noise * noise);
+  const float lnorm = logf(noise) + (float)kHalfLog2Pi;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Kahan kl;
+  for (int m = warp; m < M; m += kT / 32) {
+    float v = 0.0f;
+    for (int k = lane; k < L.H2; k += 32) v = fmaf(Hs[(int64_t)m * L.H2 + k], w2[k], v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const float res = y[m] - (v + b2);
+    if (lane == 0) {
+      dout[m] = dscale * res * inv_var;
+      kl.add(-0.5f * res * res * inv_var - lnorm);
+    }
+  }
+  double lls = lane == 0 ? kl.value() : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lls += __shfl_xor_sync(0xffffffffu, lls, o);
+  if (lane == 0) red[warp] = lls;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w];
+    ll_out[s] = t * (double)dscale;
+  }
+  float* Gs = G + (int64_t)s * L.P;
+  // dW2[k] = sum_m h2[m][k] dout[m]; then h2 <- dH2
+  for (int k = threadIdx.x; k < L.H2; k += kT) {
+    float a = 0.0f;
+    for (int m = 0; m < M; ++m) a = fmaf(Hs[(int64_t)m * L.H2 + k], dout[m], a);
+    Gs[L.oW2 + k] = a;
+  }
+  if (threadIdx.x == 0) {
+    float a = 0.0f;
+    for (int m = 0; m < M; ++m) a += dout[m];
+    Gs[L.ob2] = a;
+  }
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)M * L.H2; e += kT) {
+    const int m = (int)(e / L.H2), k = (int)(e % L.H2);
+    const float h = Hs[e];
+    Hs[e] = dout[m] * w2[k] * (1.0f - h * h);
+  }
+}
+
+// G[s][off + h] = sum_m Src[s][m][h]
+__global__ void colsum_kernel(const float* __restrict__ Src, int M, int H, int P, int off,
+                              float* __restrict__ G) {
+  const int s = blockIdx.y;
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= H) return;
+  const float* p = Src + (int64_t)s * M * H + h;
+  float a = 0.0f;
+  for (int m = 0; m < M; ++m) a += p[(int64_t)m * H];
+  G[(int64_t)s * P + off + h] = a;
+}
+
+// ------------------------------------------------------------ finalize
+struct FinArgs {
+  int P, S;
+  float prior_scale;
+  edg_opt_t opt;
+  float* mu;
+  float* rho;
+  float* slots;
+  edg_state_t* state;
+  const float* G;
+  const float* eps;
+  const double* ll;
+  float* grad_out;
+  int apply;
+  double* kl_part;  // [gridDim.x]
+};
+
+__device__ float opt_lr_b(const edg_opt_t& o, int64_t step) {
+  if (o.decay_steps <= 0) return o.lr0;
+  float p = (float)step / (float)o.decay_steps;
+  if (o.staircase) p = floorf(p);
+  return o.lr0 * powf(o.decay_rate, p);
+}
+
+__device__ float opt_apply_b(const edg_opt_t& o, float p, float g, float* s0, float* s1, float lr,
+                             float b1p, float b2p) {
+  switch (o.optimizer) {
+    case EDG_OPT_ADAM: {
+      const float lr_t = lr * sqrtf(1.0f - b2p) / (1.0f - b1p);
+      const float m = o.beta1 * *s0 + (1.0f - o.beta1) * g;
+      const float v = o.beta2 * *s1 + (1.0f - o.beta2) * g * g;
+      *s0 = m;
+      *s1 = v;
+      return p - lr_t * m / (sqrtf(v) + o.epsilon);
+    }
+    case EDG_OPT_SGD:
+      return p - lr * g;
+    case EDG_OPT_MOMENTUM: {
+      const float acc = o.momentum * *s0 + g;
+      *s0 = acc;
+      return p - lr * acc;
+    }
+    case EDG_OPT_ADAGRAD: {
+      const float acc = *s0 + g * g;
+      *s0 = acc;
+      return p - lr * g * rsqrtf(acc);
+    }
+    case EDG_OPT_RMSPROP: {
+      const float ms = o.rho * *s0 + (1.0f - o.rho) * g * g;
+      const float mom = o.momentum * *s1 + lr * g / sqrtf(ms + o.epsilon);
+      *s0 = ms;
+      *s1 = mom;
+      return p - mom;
+    }
+    default: {
+      const float acc = o.rho * *s0 + (1.0f - o.rho) * g * g;
+      const float upd = sqrtf(*s1 + o.epsilon) / sqrtf(acc + o.epsilon) * g;
+      *s0 = acc;
+      *s1 = o.rho * *s1 + (1.0f - o.rho) * upd * upd;
+      return p - lr * upd;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
+  __shared__ double red[kT / 32];
+  __shared__ bool s_last;
+  const int p = blockIdx.x * kT + threadIdx.x;
+  const float lr = opt_lr_b(a.opt, a.state->global_step);
+  const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
+  double kl = 0.0;
+  if (p < a.P) {
+    const float mu = a.mu[p], rho = a.rho[p];
+    const float sg = softplusf(rho);
+    float sg_mu = 0.0f, sg_sig = 0.0f;
+    for (int s = 0; s < a.S; ++s) {
+      const float g = a.G[(int64_t)s * a.P + p];
+      sg_mu += g;
+      sg_sig += g * a.eps[(int64_t)s * a.P + p];
+    }
+    const float invS = 1.0f / (float)a.S;
+    const float ps = a.prior_scale;
+    const float gmu = -sg_mu * invS + mu / (ps * ps);
+    const float gsig = -sg_sig * invS + (sg / (ps * ps) - 1.0f / sg);
+    const float grho = gsig * sigmoidf(rho);
+    const float ratio = (sg / ps) * (sg / ps);
+    kl = 0.5 * (double)(mu / ps) * (mu / ps) + 0.5 * ((double)ratio - 1.0 - (double)logf(ratio));
+    if (!isfinite(gmu) || !isfinite(grho)) atomicAdd(&a.state->nonfinite, 1u);
+    if (a.grad_out) {
+      a.grad_out[p] = gmu;
+      a.grad_out[a.P + p] = grho;
+    }
+    if (a.apply) {
+      const int n = 2 * a.P;
+      a.mu[p] = opt_apply_b(a.opt, mu, gmu, a.slots + p, a.slots + n + p, lr, b1p, b2p);
+      a.rho[p] = opt_apply_b(a.opt, rho, grho, a.slots + a.P + p, a.slots + n + a.P + p, lr, b1p,
+                             b2p);
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) kl += __shfl_xor_sync(0xffffffffu, kl, o);
+  if (lane == 0) red[warp] = kl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w];
+    a.kl_part[blockIdx.x] = t;
+    __threadfence();
+    const unsigned prev = atomicAdd(&a.state->done, 1u);
+    s_last = prev == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  double klsum = 0.0;
+  for (int b = 0; b < (int)gridDim.x; ++b) klsum += __ldcg(a.kl_part + b);
+  double llm = 0.0;
+  for (int s = 0; s < a.S; ++s) llm += __ldcg(a.ll + s);
+  llm /= a.S;
+  const double loss = -(llm - klsum);
+  a.state->loss = loss;
+  a.state->aux[0] = llm;
+  a.state->aux[1] = klsum;
+  if (!isfinite(loss)) atomicAdd(&a.state->nonfinite, 1u);
+  if (a.apply) {
+    a.state->t += 1;
+    a.state->global_step += 1;
+    a.state->beta1_power = b1p * a.opt.beta1;
+    a.state->beta2_power = b2p * a.opt.beta2;
+  }
+  a.state->done = 0;
+  __threadfence();
+}
+
+// ------------------------------------------------------------ minibatch
+__global__ void gather_kernel(const float* __restrict__ X, const float* __restrict__ y, int64_t N,
+                              int D, int M, uint64_t seed, const edg_state_t* state,
+                              float* __restrict__ Xb, float* __restrict__ yb) {
+  const int m = blockIdx.x;
+  if (m >= M) return;
+  const uint32_t iter = (uint32_t)state->t;
+  const uint32_t r = philox_at(seed, 4u, iter, (uint32_t)m, 0u).x;
+  const int64_t row = (int64_t)(((uint64_t)r * (uint64_t)N) >> 32);  // uniform in [0, N)
+  for (int d = threadIdx.x; d < D; d += blockDim.x) Xb[(int64_t)m * D + d] = X[row * D + d];
+  if (threadIdx.x == 0) yb[m] = y[row];
+}
+
+struct Workspace {
+  float *theta, *eps, *G, *H1, *H2;
+  double *ll, *kl_part;
+};
+
+static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  };
+  const size_t o_theta = take((size_t)S * L.P * 4), o_eps = take((size_t)S * L.P * 4);
+  const size_t o_G = take((size_t)S * L.P * 4);
+  const size_t o_H1 = take((size_t)S * M * L.H1 * 4), o_H2 = take((size_t)S * M * L.H2 * 4);
+  const size_t o_ll = take((size_t)S * 8), o_kl = take((size_t)((L.P + kT - 1) / kT) * 8);
+  if (w && base) {
+    char* b = reinterpret_cast<char*>(base);
+    w->theta = reinterpret_cast<float*>(b + o_theta);
+    w->eps = reinterpret_cast<float*>(b + o_eps);
+    w->G = reinterpret_cast<float*>(b + o_G);
+    w->H1 = reinterpret_cast<float*>(b + o_H1);
+    w->H2 = reinterpret_cast<float*>(b + o_H2);
+    w->ll = reinterpret_cast<double*>(b + o_ll);
+    w->kl_part = reinterpret_cast<double*>(b + o_kl);
+  }
+  return off;
+}
+
+static int check_cfg(const edg_bnn_t* c, int M) {
+  EDG_REQUIRE(c, EDG_E_NULL, "cfg is NULL");
+  EDG_REQUIRE(c->D > 0 && c->H1 > 0 && c->H2 > 0 && M > 0, EDG_E_SHAPE,
+              "layer widths and M must be positive");
+  EDG_REQUIRE(c->n_samples > 0, EDG_E_VALUE, "n_samples should be greater than zero: %d",
+              c->n_samples);
+  EDG_REQUIRE(c->noise > 0 && c->prior_scale > 0, EDG_E_VALUE,
+              "noise and prior_scale must be positive");
+  const int64_t P = (int64_t)make_layout(c->D, c->H1, c->H2).P;
+  EDG_REQUIRE(P * c->n_samples < (1ll << 31) && (int64_t)c->n_samples * M * c->H1 < (1ll << 40),
+              EDG_E_SHAPE, "problem too large");
+  return EDG_OK;
+}
+
+}  // namespace bnn
+}  // namespace edg
+
+using namespace edg;
+using namespace edg::bnn;
+
+extern "C" int32_t edg_bnn_num_params(int32_t D, int32_t H1, int32_t H2) {
+  return make_layout(D, H1, H2).P;
+}
+
+extern "C" size_t edg_bnn_workspace_bytes(const edg_bnn_t* cfg, int32_t M) {
+  if (check_cfg(cfg, M) != EDG_OK) return 0;
+  const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
+  return carve(L, cfg->n_samples, M, nullptr, nullptr);
+}
+
+extern "C" int edg_minibatch_gather(const float* X, const float* y, int64_t N, int32_t D,
+                                    int32_t M, uint64_t seed, const edg_state_t* state, float* Xb,
+                                    float* yb, void* stream) {
+  EDG_REQUIRE(X && y && state && Xb && yb, EDG_E_NULL, "pointers must not be NULL");
+  EDG_REQUIRE(N > 0 && D > 0 && M > 0, EDG_E_SHAPE, "N, D and M must be positive");
+  gather_kernel<<<M, 64, 0, (cudaStream_t)stream>>>(X, y, N, D, M, seed, state, Xb, yb);
+  return check_launch("gather_kernel");
+}
+
+extern "C" int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, const float* X,
+                                 const float* y, int32_t M, float* mu, float* rho,
+                                 float* opt_slots, edg_state_t* state, const float* eps_override,
+                                 float* grad_out, int32_t apply, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  int rc = check_cfg(cfg, M);
+  if (rc) return rc;
+  EDG_REQUIRE(opt && X && y && mu && rho && state, EDG_E_NULL, "pointers must not be NULL");
+  EDG_REQUIRE(!apply || opt_slots, EDG_E_NULL, "opt_slots must not be NULL when apply = 1");
+  const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
+  const int S = cfg->n_samples;
+  Workspace w;
+  const size_t need = carve(L, S, M, workspace, &w);
+  EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
+              "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t SP = (int64_t)S * L.P;
+  sample_kernel<<<(unsigned)((SP + 255) / 256), 256, 0, st>>>(mu, rho, L.P, S, cfg->seed, state,
+                                                               eps_override, w.theta, w.eps);
+  if ((rc = check_launch("bnn sample_kernel"))) return rc;
+  // F1: H1 = tanh(X W0 + b0)
+  rc = bgemm<false, false>(X, w.theta + L.oW0, w.H1, M, L.H1, L.D, L.D, L.H1, L.H1, 0, L.P,
+                           (int64_t)M * L.H1, S, EpiBiasTanh{w.theta + L.ob0, L.P}, st);
+  if (rc) return rc;
+  // F2: H2 = tanh(H1 W1 + b1)
+  rc = bgemm<false, false>(w.H1, w.theta + L.oW1, w.H2, M, L.H2, L.H1, L.H1, L.H2, L.H2,
+                           (int64_t)M * L.H1, L.P, (int64_t)M * L.H2, S,
+                           EpiBiasTanh{w.theta + L.ob1, L.P}, st);
+  if (rc) return rc;
+  // head: out, ll, dW2, db2, dH2 (over H2)
+  const size_t hsm = (size_t)(L.H2 + M) * 4;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  EDG_REQUIRE((int)hsm <= optin, EDG_E_UNSUPPORTED, "minibatch of %d rows too large", M);
+  cudaFuncSetAttribute(head_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+  head_kernel<<<S, kT, hsm, st>>>(L, M, y, w.theta, w.H2, w.G, w.ll, cfg->noise,
+                                  cfg->data_scale);
+  if ((rc = check_launch("bnn head_kernel"))) return rc;
+  // B1: dW1 = H1^T dH2  -> G[:, oW1]
+  rc = bgemm<true, false>(w.H1, w.H2, w.G + L.oW1, L.H1, L.H2, M, L.H1, L.H2, L.H2,
+                          (int64_t)M * L.H1, (int64_t)M * L.H2, L.P, S, EpiIdentity{}, st);
+  if (rc) return rc;
+  colsum_kernel<<<dim3((L.H2 + 127) / 128, S), 128, 0, st>>>(w.H2, M, L.H2, L.P, L.ob1, w.G);
+  if ((rc = check_launch("bnn colsum"))) return rc;
+  // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of H1
+  rc = bgemm<false, true>(w.H2, w.theta + L.oW1, w.H1, M, L.H1, L.H2, L.H2, L.H2, L.H1,
+                          (int64_t)M * L.H2, L.P, (int64_t)M * L.H1, S,
+                          EpiTanhGrad{w.H1, (int64_t)M * L.H1, L.H1}, st);
+  if (rc) return rc;
+  // B3: dW0 = X^T dH1 -> G[:, oW0]
+  rc = bgemm<true, false>(X, w.H1, w.G + L.oW0, L.D, L.H1, M, L.D, L.H1, L.H1, 0,
+                          (int64_t)M * L.H1, L.P, S, EpiIdentity{}, st);
+  if (rc) return rc;
+  colsum_kernel<<<dim3((L.H1 + 127) / 128, S), 128, 0, st>>>(w.H1, M, L.H1, L.P, L.ob0, w.G);
+  if ((rc = check_launch("bnn colsum"))) return rc;
+  FinArgs f;
+  f.P = L.P;
+  f.S = S;
+  f.prior_scale = cfg->prior_scale;
+  f.opt = *opt;
+  f.mu = mu;
+  f.rho = rho;
+  f.slots = opt_slots;
+  f.state = state;
+  f.G = w.G;
+  f.eps = w.eps;
+  f.ll = w.ll;
+  f.grad_out = grad_out;
+  f.apply = apply;
+  f.kl_part = w.kl_part;
+  finalize_kernel<<<(L.P + kT - 1) / kT, kT, 0, st>>>(f);
+  return check_launch("bnn finalize_kernel");
+}

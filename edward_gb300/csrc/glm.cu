@@ -194,29 +194,31 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  // per-sample totals (FP64 log-lik; FP32 gradient, summed in block order)
-  double* llS = S.llred;                 // [S]  (reuse; S <= RT/2*CT)
+  // per-sample totals (FP64 log-lik; FP32 gradient, summed in block order).
+  // Partials are read from L2 (ld.global.cg) by every thread so the loads of
+  // different blocks are in flight together.
+  double* llS = S.llred;                 // [S]  (reuse; 2 S + 8 <= RT/2*CT)
+  double* lsig = llS + a.S;              // [S] log p(z_s) - log q(z_s)
+  double* red = lsig + a.S;              // [8] per-warp partial sums
   float* gS = S.Xs;                      // [S][PP] gradient per sample
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int s = threadIdx.x; s < a.S; s += kThreads) {
     double v = 0.0;
-    for (int b = 0; b < a.nblocks; ++b) v += ((volatile double*)a.ws_ll)[(size_t)b * a.Spad + s];
+    for (int b = 0; b < a.nblocks; ++b) v += __ldcg(a.ws_ll + (size_t)b * a.Spad + s);
     llS[s] = v;
   }
   if (need_grad) {
     for (int idx = threadIdx.x; idx < a.S * PP; idx += kThreads) {
       float v = 0.0f;
-      for (int b = 0; b < a.nblocks; ++b)
-        v += ((volatile float*)a.ws_g)[(size_t)b * a.Spad * PP + idx];
+      for (int b = 0; b < a.nblocks; ++b) v += __ldcg(a.ws_g + (size_t)b * a.Spad * PP + idx);
       gS[idx] = v;
     }
   }
-  __syncthreads();
-  // score / reparam need per-sample log p(z_s) - log q(z_s)
-  double* lsig = llS + a.S;  // [S] learning signal / prior-q terms
+  // score / reparam: per-sample log p(z_s) - log q(z_s), one warp per sample
   if (a.method != EDG_KLQP_REPARAM_KL) {
-    for (int s = threadIdx.x; s < a.S; s += kThreads) {
+    for (int s = warp; s < a.S; s += kThreads / 32) {
       double acc = 0.0;
-      for (int d = 0; d < P; ++d) {
+      for (int d = lane; d < P; d += 32) {
         const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
         const float e = eps_value(a, iter, s, d, P);
         const float zv = a.mu[d] + sig[d] * e;
@@ -227,10 +229,27 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
         const float lq = -0.5f * zq * zq - logf(sig[d]);
         acc += (double)(lsc * (lp - lq));  // the 0.5 log 2pi terms cancel
       }
-      lsig[s] = acc;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) lsig[s] = acc;
     }
-    __syncthreads();
   }
+  // analytic KL: one coordinate per thread, block reduction in FP64
+  double klsum = 0.0;
+  if (a.method == EDG_KLQP_REPARAM_KL) {
+    double kl = 0.0;
+    for (int d = threadIdx.x; d < P; d += kThreads) {
+      const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
+      const float sp = m.prior_scale[d], sq = sig[d];
+      const float dm = (a.mu[d] - m.prior_loc[d]) / sp;
+      const float ratio = (sq / sp) * (sq / sp);
+      kl += (double)ks * (0.5 * (double)dm * dm + 0.5 * ((double)ratio - 1.0 - (double)logf(ratio)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) kl += __shfl_xor_sync(0xffffffffu, kl, o);
+    if (lane == 0) red[warp] = kl;
+  }
+  __syncthreads();
   // ---- loss
   if (threadIdx.x == 0) {
     double mean_ll = 0.0;
@@ -238,17 +257,10 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     mean_ll /= a.S;
     double loss;
     if (a.method == EDG_KLQP_REPARAM_KL) {
-      double kl = 0.0;
-      for (int d = 0; d < P; ++d) {
-        const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
-        const double sp = m.prior_scale[d], sq = sig[d];
-        const double dm = ((double)a.mu[d] - m.prior_loc[d]) / sp;
-        const double ratio = (sq / sp) * (sq / sp);
-        kl += ks * (0.5 * dm * dm + 0.5 * (ratio - 1.0 - log(ratio)));
-      }
-      loss = -(mean_ll - kl);
+      for (int w = 0; w < kThreads / 32; ++w) klsum += red[w];
+      loss = -(mean_ll - klsum);
       a.state->aux[0] = mean_ll;
-      a.state->aux[1] = kl;
+      a.state->aux[1] = klsum;
     } else {
       double ms = 0.0;
       for (int s = 0; s < a.S; ++s) ms += lsig[s];
@@ -667,7 +679,7 @@ template <int CT>
 static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
   const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4;
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED, "P=%d too large for KLqp kernel", m.P);
-  EDG_REQUIRE(a.S * 2 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
+  EDG_REQUIRE(a.S * 2 + 8 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
   EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,
               "n_samples too large");
   cudaFuncSetAttribute(klqp_glm_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -201,6 +201,38 @@ int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg, const edg_o
                       const float* eps_override, float* grad_out, int32_t apply,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------- Bayesian NN
+ * KLqp for the regression network h1 = tanh(X W0 + b0), h2 = tanh(h1 W1 + b1),
+ * out = h2 W2 + b2, y ~ Normal(out, noise), every weight ~ Normal(0, prior_scale),
+ * q = N(mu, softplus(rho)) per weight (edward examples/bayesian_nn.py:120-162 with
+ * build_reparam_kl_loss_and_gradients, klqp.py:707-769).  Parameters are
+ * flattened W0 [D,H1], b0 [H1], W1 [H1,H2], b1 [H2], W2 [H2,1], b2 [1] row-major
+ * (edg_bnn_num_params gives P).  One call = one minibatch step: S weight samples
+ * (Philox KIND 0 at iteration state->t, or eps_override [S,P]), batched forward,
+ * hand-written adjoint, KL, optimizer apply (same conventions as
+ * edg_klqp_glm_step).  X [M,D] / y [M] is the minibatch; data_scale = N/M. */
+typedef struct {
+  int32_t D, H1, H2;     /* input width and the two hidden widths; output width 1 */
+  int32_t n_samples;     /* S > 0 */
+  float noise;           /* Normal likelihood scale */
+  float prior_scale;     /* Normal(0, prior_scale) on every weight and bias */
+  float data_scale;      /* minibatch scale N / M (Inference.scale[y]) */
+  uint64_t seed;
+} edg_bnn_t;
+
+int32_t edg_bnn_num_params(int32_t D, int32_t H1, int32_t H2);
+size_t edg_bnn_workspace_bytes(const edg_bnn_t* cfg, int32_t M);
+int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, const float* X, const float* y,
+                      int32_t M, float* mu, float* rho, float* opt_slots, edg_state_t* state,
+                      const float* eps_override, float* grad_out, int32_t apply,
+                      void* workspace, size_t workspace_bytes, void* stream);
+/* Minibatch of M rows drawn uniformly with replacement from X [N,D] / y [N]
+ * (Philox KIND 4 at iteration state->t) into Xb [M,D] / yb [M]; replaces the
+ * host-side feed_dict batches of the reference examples. */
+int edg_minibatch_gather(const float* X, const float* y, int64_t N, int32_t D, int32_t M,
+                         uint64_t seed, const edg_state_t* state, float* Xb, float* yb,
+                         void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and
