@@ -104,4 +104,3 @@ def test_bnn_adam_steps(cuda):
         close(got, th, 5e-5)
     assert _lib.read_state(t["state"]).t == 3
 EOF
-timeout 300 python -m pytest tests -q -m "not gpu" -x 2>&1 | tail -1; git add -A; git commit -qm "Bayesian NN KLqp step: batched SIMT GEMMs with fused epilogues, adjoint, KL + optimizer; oracle and GPU tests" ; echo ok
