@@ -103,4 +103,3 @@ def test_bnn_adam_steps(cuda):
         got = torch.cat([t["mu"], t["rho"]]).cpu().numpy()
         close(got, th, 5e-5)
     assert _lib.read_state(t["state"]).t == 3
-EOF
