@@ -505,6 +505,82 @@ def run_klqp(args):
     return 0
 
 
+def bnn_data(N=100000, D=32, H1=256, H2=256, seed=0):
+    """X ~ N(0,1) [N, D]; y = a random 32-256-256-1 tanh network (weights
+    N(0,1)/sqrt(fan_in)) + N(0, 0.1^2) noise."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((N, D), dtype=np.float32)
+    W0 = (rng.standard_normal((D, H1)) / np.sqrt(D)).astype(np.float32)
+    W1 = (rng.standard_normal((H1, H2)) / np.sqrt(H1)).astype(np.float32)
+    W2 = (rng.standard_normal((H2, 1)) / np.sqrt(H2)).astype(np.float32)
+    y = (np.tanh(np.tanh(X @ W0) @ W1) @ W2)[:, 0]
+    return X, (y + 0.1 * rng.standard_normal(N)).astype(np.float32)
+
+
+def run_bnn(args):
+    """Bayesian NN 32-256-256-1 under KLqp (analytic KL), S = 64 weight samples,
+    minibatch M = 4,096 rows gathered on the device from N = 100,000 with
+    scale N / M, through ed.KLqp; steps replayed from a CUDA graph."""
+    import numpy as np
+    import torch
+    import edward_gb300 as ed
+    from edward_gb300.models import Normal
+    N, D, H1, H2, M, S = 100000, 32, 256, 256, 4096, 64
+    X, y = bnn_data(N, D, H1, H2)
+    W0 = Normal(loc=ed.zeros([D, H1]), scale=ed.ones([D, H1]))
+    W1 = Normal(loc=ed.zeros([H1, H2]), scale=ed.ones([H1, H2]))
+    W2 = Normal(loc=ed.zeros([H2, 1]), scale=ed.ones([H2, 1]))
+    b0, b1, b2 = (Normal(loc=ed.zeros(n), scale=ed.ones(n)) for n in (H1, H2, 1))
+    h = ed.tanh(ed.matmul(X, W0) + b0)
+    h = ed.tanh(ed.matmul(h, W1) + b1)
+    yv = Normal(loc=ed.reshape(ed.matmul(h, W2) + b2, [-1]), scale=0.1)
+    rng = np.random.default_rng(1)
+    qs = {}
+    for z in (W0, b0, W1, b1, W2, b2):
+        qs[z] = Normal(loc=ed.Variable(rng.standard_normal(z.shape).astype(np.float32) * 0.1),
+                       scale=ed.softplus(ed.Variable(np.full(z.shape, -3.0, np.float32))))
+    inf = ed.KLqp(qs, data={yv: y})
+    inf.initialize(n_samples=S, n_minibatch=M, n_iter=5000, n_print=0,
+                   optimizer=ed.train.AdamOptimizer(1e-3))
+    chunk = 10
+    for _ in range(max(1, args.warmup // chunk + 1)):
+        inf.steps(chunk)
+    torch.cuda.synchronize()
+    K = max(args.steps // chunk, 1) * chunk
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        a.record()
+        for _ in range(K // chunk):
+            inf.steps(chunk)
+        b.record()
+        b.synchronize()
+    ms = a.elapsed_time(b) / K
+    st = inf._read_state()
+    P = inf._spec.P
+    fwd = 2.0 * (D * H1 + H1 * H2 + H2) * M * S
+    flops = 3.0 * fwd
+    peak, src = _peak_3xtf32()
+    ach = flops / (ms / 1e3) / 1e12
+    act_bytes = 4.0 * S * M * (H1 + H2)
+    line = {"metric": "KLqp ELBO-grad evals/s (Bayesian NN 32-256-256-1, S=64, M=4096)",
+            "value": 1e3 / ms, "unit": "evals/s", "n_gpus": 1, "steps": K,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "bnn_klqp_N100000_D32_H256_H256_S64_M4096", "params": P,
+                       "launch": f"CUDA graph of {chunk} steps (gather + 10 launches each)",
+                       "l2_flush": "inputs larger than L2 (activations %.0f MB per step)"
+                                   % (act_bytes / 1e6)},
+            "gpu_launches": K * 11,
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                         "frac": ach / peak, "traffic": None,
+                         "kernel": "whole step (bnn bgemm SIMT FP32 + head + finalize)",
+                         "peak_source": src, "algorithmic_flops_per_step": flops},
+            "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -516,7 +592,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--hier-instances", type=int, default=2048)
-    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp"],
+    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -527,6 +603,8 @@ def main():
         return run_hier(args)
     if args.workload == "klqp":
         return run_klqp(args)
+    if args.workload == "bnn":
+        return run_bnn(args)
     return run_gpu(args)
 
 

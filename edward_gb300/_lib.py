@@ -63,7 +63,7 @@ class EdgHier(ctypes.Structure):
 class EdgBNN(ctypes.Structure):
     _fields_ = [("D", c_int32), ("H1", c_int32), ("H2", c_int32), ("n_samples", c_int32),
                 ("noise", c_float), ("prior_scale", c_float), ("data_scale", c_float),
-                ("seed", c_uint64)]
+                ("method", c_int32), ("seed", c_uint64)]
 
 
 class EdgHMC(ctypes.Structure):
@@ -101,6 +101,8 @@ _SIGS = {
     "edg_bnn_klqp_step": (c_int32, [ctypes.POINTER(EdgBNN), ctypes.POINTER(EdgOpt), c_void_p,
                                     c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_int32, c_void_p, c_size_t, c_void_p]),
+    "edg_bnn_loglik_grad": (c_int32, [ctypes.POINTER(EdgBNN), c_void_p, c_void_p, c_int32,
+                                      c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "edg_minibatch_gather": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_uint64,
                                        c_void_p, c_void_p, c_void_p, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),

@@ -101,6 +101,10 @@ def compile_glm(latents, data):
         raise UnsupportedModel("observed values must be arrays, not random variables")
     if isinstance(yval, (list, tuple)) and yval and np.ndim(yval[0]) > 0:
         raise UnsupportedModel("a list of observed arrays (ragged instances) is not a GLM")
+    if isinstance(yval, Node):
+        yval = const_value(yval, bindings)
+        if yval is None:
+            raise UnsupportedModel("the GLM family needs the observed values bound to an array")
     y = np.asarray(yval, np.float32).reshape(-1)
     if isinstance(yrv, Bernoulli):
         if yrv.logits is None:
@@ -267,3 +271,121 @@ def compile_hier(latents, data):
     mu_scale = float(_const_param(mu.scale, "mu scale", bindings).reshape(-1)[0])
     tau_scale = float(_const_param(tau.scale, "tau scale", bindings).reshape(-1)[0])
     return HierSpec(Xs, ys, mu_loc, mu_scale, tau_scale, w=w, mu=mu, tau=tau)
+
+
+# ------------------------------------------------------------- Bayesian NN family
+
+@dataclass
+class MLPSpec:
+    """y ~ Normal(loc = reshape(tanh(tanh(X W0 + b0) W1 + b1) W2 + b2, [-1]), noise)
+    with every weight ~ Normal(0, prior_scale): the regression network of
+    ``examples/bayesian_nn.py:120-150``.  ``X`` / ``y`` are arrays when the data
+    dict binds them, else None (placeholders fed per update)."""
+    D: int
+    H1: int
+    H2: int
+    noise: float
+    prior_scale: float
+    X: np.ndarray = None
+    y: np.ndarray = None
+    X_node: Node = None
+    y_node: Node = None
+    blocks: List[LatentBlock] = field(default_factory=list)
+    observed: RandomVariable = None
+    batch: int = None       # rows per step when X is a placeholder of static shape
+
+    @property
+    def P(self):
+        return self.D * self.H1 + self.H1 + self.H1 * self.H2 + self.H2 + self.H2 + 1
+
+
+def _strip_reshape(node):
+    while isinstance(node, Op) and node.op == "reshape":
+        node = node.args[0]
+    return node
+
+
+def _affine(node, latent_set):
+    """matmul(a, W) + b  ->  (a, W, b) with W, b latent random variables."""
+    terms = flatten_add(node)
+    mm = [t for t in terms if isinstance(t, Op) and t.op == "matmul"]
+    bs = [t for t in terms if isinstance(t, RandomVariable) and id(t) in latent_set]
+    if len(mm) != 1 or len(bs) != 1 or len(terms) != 2:
+        raise UnsupportedModel("each layer must be tf.matmul(h, W) + b with latent W and b")
+    a, W = mm[0].args
+    if not (isinstance(W, RandomVariable) and id(W) in latent_set):
+        raise UnsupportedModel("layer weights must be latent random variables")
+    return a, W, bs[0]
+
+
+def compile_mlp(latents, data):
+    """Recognises the two-hidden-layer tanh regression network.  Raises
+    UnsupportedModel for anything else."""
+    observed, bindings = _split_data(data)
+    if len(observed) != 1:
+        raise UnsupportedModel("the Bayesian NN family has exactly one observed variable")
+    (yrv, yval), = observed.items()
+    if not isinstance(yrv, Normal):
+        raise UnsupportedModel("the Bayesian NN family needs a Normal likelihood")
+    latent_set = set(map(id, latents))
+    h, W2, b2 = _affine(_strip_reshape(yrv.loc), latent_set)
+    if not (isinstance(h, Op) and h.op == "tanh"):
+        raise UnsupportedModel("hidden layers must be tf.tanh(...)")
+    h, W1, b1 = _affine(h.args[0], latent_set)
+    if not (isinstance(h, Op) and h.op == "tanh"):
+        raise UnsupportedModel("hidden layers must be tf.tanh(...)")
+    Xn, W0, b0 = _affine(h.args[0], latent_set)
+    order = [W0, b0, W1, b1, W2, b2]
+    if len(set(map(id, order))) != 6 or set(map(id, order)) != latent_set:
+        raise UnsupportedModel("latent variables must be exactly W_0, b_0, W_1, b_1, W_2, b_2")
+    shp = [tuple(int(v) for v in z.shape) for z in order]
+    if len(shp[0]) != 2 or len(shp[2]) != 2:
+        raise UnsupportedModel("W_0 and W_1 must be matrices")
+    D, H1 = shp[0]
+    H2 = shp[2][1]
+    want = [(D, H1), (H1,), (H1, H2), (H2,), (H2, 1), (1,)]
+    for z, s, w in zip(order, shp, want):
+        if int(np.prod(s)) != int(np.prod(w)) or (len(s) == 2 and s != w):
+            raise UnsupportedModel(f"{z.name} has shape {s}; the network needs {w}")
+    prior_scale = None
+    for z in order:
+        loc = _const_param(z.loc, f"prior loc of {z.name}", bindings)
+        sc = _const_param(z.scale, f"prior scale of {z.name}", bindings)
+        if np.any(loc != 0.0):
+            raise UnsupportedModel("weight priors must have loc 0")
+        if np.any(sc != sc.reshape(-1)[0]) or (prior_scale is not None and sc.reshape(-1)[0] != prior_scale):
+            raise UnsupportedModel("every weight prior must share one scale")
+        prior_scale = float(sc.reshape(-1)[0])
+    if prior_scale <= 0:
+        raise ValueError("prior scales must be positive")
+    s = _const_param(yrv.scale, "likelihood scale", bindings)
+    if np.any(s != s.reshape(-1)[0]) or s.reshape(-1)[0] <= 0:
+        raise UnsupportedModel("the likelihood scale must be one positive constant")
+    noise = float(s.reshape(-1)[0])
+    X = const_value(Xn, bindings)
+    batch = None
+    if X is None:
+        if not isinstance(Xn, Placeholder):
+            raise UnsupportedModel("the network input must be data (an array or a placeholder)")
+        if Xn.shape is None or len(Xn.shape) != 2 or Xn.shape[1] != D or Xn.shape[0] is None:
+            raise UnsupportedModel("an unbound X placeholder needs the static shape [M, D]")
+        batch = int(Xn.shape[0])
+    else:
+        X = np.ascontiguousarray(X, np.float32)
+        if X.ndim != 2 or X.shape[1] != D:
+            raise ValueError(f"X has shape {X.shape}; expected [N, {D}]")
+    y = None
+    if isinstance(yval, Placeholder):
+        y = const_value(yval, bindings)
+    elif not isinstance(yval, (RandomVariable, Node)):
+        y = np.asarray(yval, np.float32).reshape(-1)
+    if y is not None and X is not None and y.shape[0] != X.shape[0]:
+        raise ValueError(f"y has {y.shape[0]} rows but X has {X.shape[0]}")
+    blocks, off = [], 0
+    for z, w in zip(order, want):
+        n = int(np.prod(w))
+        blocks.append(LatentBlock(z, off, n, tuple(z.shape)))
+        off += n
+    return MLPSpec(D=D, H1=H1, H2=H2, noise=noise, prior_scale=prior_scale, X=X, y=y,
+                   X_node=Xn, y_node=yval if isinstance(yval, Placeholder) else None,
+                   blocks=blocks, observed=yrv, batch=batch)

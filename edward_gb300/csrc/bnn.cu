@@ -261,8 +261,10 @@ struct FinArgs {
   float* rho;
   float* slots;
   edg_state_t* state;
+  int method;  // EDG_KLQP_REPARAM_KL or EDG_KLQP_REPARAM
   const float* G;
   const float* eps;
+  const float* theta;
   const double* ll;
   float* grad_out;
   int apply;
@@ -334,11 +336,31 @@ __global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
     }
     const float invS = 1.0f / (float)a.S;
     const float ps = a.prior_scale;
-    const float gmu = -sg_mu * invS + mu / (ps * ps);
-    const float gsig = -sg_sig * invS + (sg / (ps * ps) - 1.0f / sg);
+    float gmu, gsig;
+    if (a.method == EDG_KLQP_REPARAM_KL) {
+      // analytic KL(N(mu, sg) || N(0, ps)) and its gradient
+      gmu = -sg_mu * invS + mu / (ps * ps);
+      gsig = -sg_sig * invS + (sg / (ps * ps) - 1.0f / sg);
+      const float ratio = (sg / ps) * (sg / ps);
+      kl = 0.5 * (double)(mu / ps) * (mu / ps) + 0.5 * ((double)ratio - 1.0 - (double)logf(ratio));
+    } else {
+      // Monte Carlo KL: mean_s [log q(z_s) - log p(z_s)], z_s = mu + sg eps_s, with the
+      // gradient flowing through z_s and through q's own parameters
+      float zz = 0.0f, zze = 0.0f;
+      double lqp = 0.0;
+      for (int s = 0; s < a.S; ++s) {
+        const float e = a.eps[(int64_t)s * a.P + p];
+        const float z = a.theta[(int64_t)s * a.P + p];
+        zz += z;
+        zze += z * e;
+        lqp += 0.5 * ((double)(z / ps) * (z / ps) - (double)e * e);
+      }
+      const float ip2 = 1.0f / (ps * ps);
+      gmu = -(sg_mu - zz * ip2) * invS;
+      gsig = -(sg_sig - zze * ip2) * invS - 1.0f / sg;
+      kl = lqp / a.S + (double)logf(ps) - (double)logf(sg);
+    }
     const float grho = gsig * sigmoidf(rho);
-    const float ratio = (sg / ps) * (sg / ps);
-    kl = 0.5 * (double)(mu / ps) * (mu / ps) + 0.5 * ((double)ratio - 1.0 - (double)logf(ratio));
     if (!isfinite(gmu) || !isfinite(grho)) atomicAdd(&a.state->nonfinite, 1u);
     if (a.grad_out) {
       a.grad_out[p] = gmu;
@@ -429,6 +451,52 @@ static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
   return off;
 }
 
+// Per-sample scaled log-likelihood ll[s] (FP64) and its gradient G[s] w.r.t.
+// theta[s] for S weight samples over one minibatch: the batched forward pass
+// and the hand-written adjoint.  H1 / H2 [S, M, H] hold the activations and
+// are overwritten by their adjoints.
+static int loglik_grad(const Layout& L, int S, int M, const float* X, const float* y,
+                       const float* theta, float* H1, float* H2, float* G, double* ll,
+                       float noise, float dscale, cudaStream_t st) {
+  int rc;
+  // F1: H1 = tanh(X W0 + b0)
+  rc = bgemm<false, false>(X, theta + L.oW0, H1, M, L.H1, L.D, L.D, L.H1, L.H1, 0, L.P,
+                           (int64_t)M * L.H1, S, EpiBiasTanh{theta + L.ob0, L.P}, st);
+  if (rc) return rc;
+  // F2: H2 = tanh(H1 W1 + b1)
+  rc = bgemm<false, false>(H1, theta + L.oW1, H2, M, L.H2, L.H1, L.H1, L.H2, L.H2,
+                           (int64_t)M * L.H1, L.P, (int64_t)M * L.H2, S,
+                           EpiBiasTanh{theta + L.ob1, L.P}, st);
+  if (rc) return rc;
+  // head: out, ll, dW2, db2, dH2 (over H2)
+  const size_t hsm = (size_t)(L.H2 + M) * 4;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  EDG_REQUIRE((int)hsm <= optin, EDG_E_UNSUPPORTED, "minibatch of %d rows too large", M);
+  cudaFuncSetAttribute(head_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+  head_kernel<<<S, kT, hsm, st>>>(L, M, y, theta, H2, G, ll, noise, dscale);
+  if ((rc = check_launch("bnn head_kernel"))) return rc;
+  // B1: dW1 = H1^T dH2  -> G[:, oW1]
+  rc = bgemm<true, false>(H1, H2, G + L.oW1, L.H1, L.H2, M, L.H1, L.H2, L.H2,
+                          (int64_t)M * L.H1, (int64_t)M * L.H2, L.P, S, EpiIdentity{}, st);
+  if (rc) return rc;
+  colsum_kernel<<<dim3((L.H2 + 127) / 128, S), 128, 0, st>>>(H2, M, L.H2, L.P, L.ob1, G);
+  if ((rc = check_launch("bnn colsum"))) return rc;
+  // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of H1
+  rc = bgemm<false, true>(H2, theta + L.oW1, H1, M, L.H1, L.H2, L.H2, L.H2, L.H1,
+                          (int64_t)M * L.H2, L.P, (int64_t)M * L.H1, S,
+                          EpiTanhGrad{H1, (int64_t)M * L.H1, L.H1}, st);
+  if (rc) return rc;
+  // B3: dW0 = X^T dH1 -> G[:, oW0]
+  rc = bgemm<true, false>(X, H1, G + L.oW0, L.D, L.H1, M, L.D, L.H1, L.H1, 0,
+                          (int64_t)M * L.H1, L.P, S, EpiIdentity{}, st);
+  if (rc) return rc;
+  colsum_kernel<<<dim3((L.H1 + 127) / 128, S), 128, 0, st>>>(H1, M, L.H1, L.P, L.ob0, G);
+  if ((rc = check_launch("bnn colsum"))) return rc;
+  return EDG_OK;
+}
+
 static int check_cfg(const edg_bnn_t* c, int M) {
   EDG_REQUIRE(c, EDG_E_NULL, "cfg is NULL");
   EDG_REQUIRE(c->D > 0 && c->H1 > 0 && c->H2 > 0 && M > 0, EDG_E_SHAPE,
@@ -437,6 +505,9 @@ static int check_cfg(const edg_bnn_t* c, int M) {
               c->n_samples);
   EDG_REQUIRE(c->noise > 0 && c->prior_scale > 0, EDG_E_VALUE,
               "noise and prior_scale must be positive");
+  EDG_REQUIRE(c->method == EDG_KLQP_REPARAM_KL || c->method == EDG_KLQP_REPARAM, EDG_E_UNSUPPORTED,
+              "method %d: the Bayesian NN step implements the reparameterisation gradient "
+              "with analytic or Monte Carlo KL", c->method);
   const int64_t P = (int64_t)make_layout(c->D, c->H1, c->H2).P;
   EDG_REQUIRE(P * c->n_samples < (1ll << 31) && (int64_t)c->n_samples * M * c->H1 < (1ll << 40),
               EDG_E_SHAPE, "problem too large");
@@ -488,42 +559,9 @@ extern "C" int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, con
   sample_kernel<<<(unsigned)((SP + 255) / 256), 256, 0, st>>>(mu, rho, L.P, S, cfg->seed, state,
                                                                eps_override, w.theta, w.eps);
   if ((rc = check_launch("bnn sample_kernel"))) return rc;
-  // F1: H1 = tanh(X W0 + b0)
-  rc = bgemm<false, false>(X, w.theta + L.oW0, w.H1, M, L.H1, L.D, L.D, L.H1, L.H1, 0, L.P,
-                           (int64_t)M * L.H1, S, EpiBiasTanh{w.theta + L.ob0, L.P}, st);
+  rc = loglik_grad(L, S, M, X, y, w.theta, w.H1, w.H2, w.G, w.ll, cfg->noise, cfg->data_scale,
+                   st);
   if (rc) return rc;
-  // F2: H2 = tanh(H1 W1 + b1)
-  rc = bgemm<false, false>(w.H1, w.theta + L.oW1, w.H2, M, L.H2, L.H1, L.H1, L.H2, L.H2,
-                           (int64_t)M * L.H1, L.P, (int64_t)M * L.H2, S,
-                           EpiBiasTanh{w.theta + L.ob1, L.P}, st);
-  if (rc) return rc;
-  // head: out, ll, dW2, db2, dH2 (over H2)
-  const size_t hsm = (size_t)(L.H2 + M) * 4;
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  EDG_REQUIRE((int)hsm <= optin, EDG_E_UNSUPPORTED, "minibatch of %d rows too large", M);
-  cudaFuncSetAttribute(head_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
-  head_kernel<<<S, kT, hsm, st>>>(L, M, y, w.theta, w.H2, w.G, w.ll, cfg->noise,
-                                  cfg->data_scale);
-  if ((rc = check_launch("bnn head_kernel"))) return rc;
-  // B1: dW1 = H1^T dH2  -> G[:, oW1]
-  rc = bgemm<true, false>(w.H1, w.H2, w.G + L.oW1, L.H1, L.H2, M, L.H1, L.H2, L.H2,
-                          (int64_t)M * L.H1, (int64_t)M * L.H2, L.P, S, EpiIdentity{}, st);
-  if (rc) return rc;
-  colsum_kernel<<<dim3((L.H2 + 127) / 128, S), 128, 0, st>>>(w.H2, M, L.H2, L.P, L.ob1, w.G);
-  if ((rc = check_launch("bnn colsum"))) return rc;
-  // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of H1
-  rc = bgemm<false, true>(w.H2, w.theta + L.oW1, w.H1, M, L.H1, L.H2, L.H2, L.H2, L.H1,
-                          (int64_t)M * L.H2, L.P, (int64_t)M * L.H1, S,
-                          EpiTanhGrad{w.H1, (int64_t)M * L.H1, L.H1}, st);
-  if (rc) return rc;
-  // B3: dW0 = X^T dH1 -> G[:, oW0]
-  rc = bgemm<true, false>(X, w.H1, w.G + L.oW0, L.D, L.H1, M, L.D, L.H1, L.H1, 0,
-                          (int64_t)M * L.H1, L.P, S, EpiIdentity{}, st);
-  if (rc) return rc;
-  colsum_kernel<<<dim3((L.H1 + 127) / 128, S), 128, 0, st>>>(w.H1, M, L.H1, L.P, L.ob0, w.G);
-  if ((rc = check_launch("bnn colsum"))) return rc;
   FinArgs f;
   f.P = L.P;
   f.S = S;
@@ -533,12 +571,30 @@ extern "C" int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, con
   f.rho = rho;
   f.slots = opt_slots;
   f.state = state;
+  f.method = cfg->method;
   f.G = w.G;
   f.eps = w.eps;
+  f.theta = w.theta;
   f.ll = w.ll;
   f.grad_out = grad_out;
   f.apply = apply;
   f.kl_part = w.kl_part;
   finalize_kernel<<<(L.P + kT - 1) / kT, kT, 0, st>>>(f);
   return check_launch("bnn finalize_kernel");
+}
+
+extern "C" int edg_bnn_loglik_grad(const edg_bnn_t* cfg, const float* X, const float* y,
+                                   int32_t M, const float* theta, double* ll_out,
+                                   float* grad_out, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+  int rc = check_cfg(cfg, M);
+  if (rc) return rc;
+  EDG_REQUIRE(X && y && theta && ll_out && grad_out, EDG_E_NULL, "pointers must not be NULL");
+  const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
+  Workspace w;
+  const size_t need = carve(L, cfg->n_samples, M, workspace, &w);
+  EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
+              "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
+  return loglik_grad(L, cfg->n_samples, M, X, y, theta, w.H1, w.H2, grad_out, ll_out, cfg->noise,
+                     cfg->data_scale, (cudaStream_t)stream);
 }

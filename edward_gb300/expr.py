@@ -137,7 +137,14 @@ def _infer_shape(op, args, attrs):
                 return None
             return (a[0], b[1])
         if op == "reshape":
-            return tuple(attrs["shape"])
+            shp = tuple(attrs["shape"])
+            if -1 in shp:
+                a = _shape(args[0])
+                if a is None or None in a:
+                    return None
+                known = int(np.prod([d for d in shp if d != -1]))
+                shp = tuple(int(np.prod(a)) // known if d == -1 else d for d in shp)
+            return shp
     except (ValueError, IndexError, TypeError):
         pass
     return None

@@ -11,10 +11,10 @@ import numpy as np
 import torch
 
 from .. import _lib
-from ..compile import UnsupportedModel, compile_glm, parse_normal_q
+from ..compile import UnsupportedModel, compile_glm, compile_mlp, parse_normal_q
 from ..expr import Variable, softplus
 from ..models import Normal, RandomVariable
-from ..ops import GLMDevice
+from ..ops import BNNDevice, GLMDevice
 from ..util import next_seed, randn
 from .variational_inference import VariationalInference
 
@@ -43,13 +43,19 @@ class KLqp(VariationalInference):
             latent_vars = d
         super().__init__(latent_vars, data)
 
-    def initialize(self, n_samples=1, kl_scaling=None, *args, **kwargs):
+    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, *args, **kwargs):
+        """``n_samples`` / ``kl_scaling`` as in ``klqp.py:86-113``.  ``n_minibatch``
+        (Bayesian NN family, data bound to arrays): each step draws that many
+        rows uniformly with replacement on the device instead of using the
+        whole data set; ``scale`` for the observed variable then defaults to
+        N / n_minibatch."""
         if kl_scaling is None:
             kl_scaling = {}
         if n_samples <= 0:
             raise ValueError("n_samples should be greater than zero: {}".format(n_samples))
         self.n_samples = n_samples
         self.kl_scaling = kl_scaling
+        self.n_minibatch = n_minibatch
         return super().initialize(*args, **kwargs)
 
     # ------------------------------------------------------------ dispatch
@@ -73,35 +79,43 @@ class KLqp(VariationalInference):
             raise NotImplementedError(
                 "Rao-Blackwellised score gradients (ScoreRBKLqp) for this model family")
         self._method_id = method
-        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        latents = list(self.latent_vars.keys())
+        try:
+            self._spec = compile_glm(latents, self.data)
+            self._family = "glm"
+        except UnsupportedModel as e_glm:
+            try:
+                self._spec = compile_mlp(latents, self.data)
+            except UnsupportedModel as e_mlp:
+                raise UnsupportedModel(f"{e_glm} (GLM family); {e_mlp} (Bayesian NN family)")
+            self._family = "bnn"
+            if method == SCORE:
+                raise NotImplementedError("ScoreKLqp for the Bayesian NN family")
+            if any(np.any(np.asarray(v) != 1.0) for v in self.kl_scaling.values()):
+                raise NotImplementedError("kl_scaling for the Bayesian NN family")
+            if any(z in self.scale for z in latents):
+                raise NotImplementedError("per-latent scale for the Bayesian NN family")
+        if self._family == "glm" and self.n_minibatch is not None:
+            raise NotImplementedError("n_minibatch applies to the Bayesian NN family")
         for blk in self._spec.blocks:
             parse_normal_q(self.latent_vars[blk.rv])
 
     def build_loss_and_gradients(self, var_list):
+        if self._family == "bnn":
+            return self._build_bnn(var_list)
         method = self._method_id
         spec = self._spec
         self._glm = GLMDevice(spec, self._device)
         P = spec.P
         dev = self._device
-        self._mu = torch.empty(P, dtype=torch.float32, device=dev)
-        self._rho = torch.empty(P, dtype=torch.float32, device=dev)
+        q_vars = self._bind_q(var_list)
         kls = np.ones(P, np.float32)
         lsc = np.ones(P, np.float32)
-        q_vars = []
         for blk in spec.blocks:
-            q = parse_normal_q(self.latent_vars[blk.rv])
-            for var, buf in ((q.loc_var, self._mu), (q.rho_var, self._rho)):
-                if int(np.prod(var.shape)) != blk.size:
-                    raise ValueError(f"q parameter {var.name} has shape {var.shape}; "
-                                     f"latent {blk.rv.name} has {blk.size} elements")
-                var._rebind(buf[blk.offset:blk.offset + blk.size].view(var.shape or ()))
-                q_vars.append(var)
             kls[blk.offset:blk.offset + blk.size] = np.broadcast_to(
                 np.asarray(self.kl_scaling.get(blk.rv, 1.0), np.float32), blk.shape).reshape(-1)
             lsc[blk.offset:blk.offset + blk.size] = np.broadcast_to(
                 np.asarray(self.scale.get(blk.rv, 1.0), np.float32), blk.shape).reshape(-1)
-        if var_list is not None and set(map(id, var_list)) != set(map(id, q_vars)):
-            raise NotImplementedError("var_list must be the variational parameters of q")
         dscale = np.asarray(self.scale.get(spec.observed, 1.0), np.float32)
         if dscale.size != 1:
             raise NotImplementedError("per-row data scale is not supported; pass a scalar")
@@ -124,6 +138,65 @@ class KLqp(VariationalInference):
         self._grad = torch.zeros(2 * P, dtype=torch.float32, device=dev)
         return None, [(None, v) for v in q_vars]
 
+    def _bind_q(self, var_list):
+        """Rebinds every q parameter Variable to its slice of the flat device
+        buffers (mu, rho) so that the fused kernels update them in place."""
+        spec, dev = self._spec, self._device
+        self._mu = torch.empty(spec.P, dtype=torch.float32, device=dev)
+        self._rho = torch.empty(spec.P, dtype=torch.float32, device=dev)
+        q_vars = []
+        for blk in spec.blocks:
+            q = parse_normal_q(self.latent_vars[blk.rv])
+            for var, buf in ((q.loc_var, self._mu), (q.rho_var, self._rho)):
+                if int(np.prod(var.shape)) != blk.size:
+                    raise ValueError(f"q parameter {var.name} has shape {var.shape}; "
+                                     f"latent {blk.rv.name} has {blk.size} elements")
+                var._rebind(buf[blk.offset:blk.offset + blk.size].view(var.shape or ()))
+                q_vars.append(var)
+        if var_list is not None and set(map(id, var_list)) != set(map(id, q_vars)):
+            raise NotImplementedError("var_list must be the variational parameters of q")
+        return q_vars
+
+    def _build_bnn(self, var_list):
+        spec, dev = self._spec, self._device
+        q_vars = self._bind_q(var_list)
+        P = spec.P
+        self._bnn = BNNDevice(spec, dev, self.n_minibatch)
+        dscale = self.scale.get(spec.observed)
+        if dscale is None:
+            dscale = self._bnn.default_scale
+        dscale = np.asarray(dscale, np.float32)
+        if dscale.size != 1:
+            raise NotImplementedError("per-row data scale is not supported; pass a scalar")
+        cfg = _lib.EdgBNN()
+        cfg.D, cfg.H1, cfg.H2, cfg.n_samples = spec.D, spec.H1, spec.H2, self.n_samples
+        cfg.noise, cfg.prior_scale = spec.noise, spec.prior_scale
+        cfg.data_scale = float(dscale.reshape(-1)[0])
+        cfg.method = self._method_id
+        cfg.seed = next_seed()
+        self._bnn.seed = next_seed()
+        self._cfg = cfg
+        self._opt = self.optimizer.to_c()
+        self._slots = torch.zeros(4 * P, dtype=torch.float32, device=dev)
+        self._reset_optimizer()
+        lib = _lib.load()
+        self._ws_bytes = lib.edg_bnn_workspace_bytes(cfg, self._bnn.M)
+        if self._ws_bytes == 0:
+            _lib.call("edg_bnn_workspace_bytes", cfg, self._bnn.M)
+        self._ws = torch.empty(self._ws_bytes, dtype=torch.uint8, device=dev)
+        self._grad = torch.zeros(2 * P, dtype=torch.float32, device=dev)
+        return None, [(None, v) for v in q_vars]
+
+    def _feed(self, feed_dict):
+        if self._family != "bnn":
+            return super()._feed(feed_dict)
+        self._bnn.feed(feed_dict)
+
+    def _run_loop(self):
+        if self._family == "bnn" and not self._bnn.ready:
+            raise ValueError("X / y are placeholders: feed them with update(feed_dict=...)")
+        super()._run_loop()
+
     def _reset_optimizer(self):
         a, b = self.optimizer.slot_init()
         P = self._spec.P
@@ -132,6 +205,14 @@ class KLqp(VariationalInference):
 
     def _step(self, apply=True, eps=None, grad_out=None):
         import ctypes
+        if self._family == "bnn":
+            X, y = self._bnn.batch(self._state)
+            _lib.call("edg_bnn_klqp_step", ctypes.byref(self._cfg), ctypes.byref(self._opt),
+                      _lib.ptr(X), _lib.ptr(y), self._bnn.M, _lib.ptr(self._mu),
+                      _lib.ptr(self._rho), _lib.ptr(self._slots), _lib.ptr(self._state),
+                      _lib.ptr(eps), _lib.ptr(grad_out), 1 if apply else 0, _lib.ptr(self._ws),
+                      self._ws_bytes, _lib.stream_ptr())
+            return
         _lib.call("edg_klqp_glm_step", self._glm.ref(), ctypes.byref(self._cfg),
                   ctypes.byref(self._opt), _lib.ptr(self._mu), _lib.ptr(self._rho),
                   _lib.ptr(self._slots), _lib.ptr(self._state), _lib.ptr(eps), _lib.ptr(grad_out),

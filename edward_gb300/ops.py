@@ -146,3 +146,143 @@ class HierDevice:
 
     def ref(self):
         return ctypes.byref(self.c)
+
+
+class BNNDevice:
+    """Device data of a compiled Bayesian NN (``compile.MLPSpec``) and where
+    each step's minibatch comes from:
+
+    * X and y bound to arrays, no ``n_minibatch``: every step uses all N rows;
+    * X and y bound to arrays with ``n_minibatch=M``: every step gathers M rows
+      uniformly with replacement on the device (``edg_minibatch_gather``, Philox
+      stream 4 at the step's iteration), replacing the host-side batching of
+      ``examples/bayesian_nn.py``-style feed loops;
+    * X and/or y placeholders: ``feed`` copies each update's ``feed_dict``
+      arrays into fixed device buffers (``inference.update(feed_dict=...)``,
+      ``edward/inferences/variational_inference.py:133-164``)."""
+
+    def __init__(self, spec, device="cuda", n_minibatch=None):
+        _lib.require_cuda()
+        self.spec = spec
+        self.device = torch.device(device)
+        dev = self.device
+        self.gather = False
+        self.default_scale = 1.0
+        bound_X, bound_y = spec.X is not None, spec.y is not None
+        if bound_X and bound_y:
+            self.N = spec.X.shape[0]
+            self.X_full = torch.as_tensor(spec.X).contiguous().to(dev)
+            self.y_full = torch.as_tensor(spec.y, dtype=torch.float32).contiguous().to(dev)
+            if n_minibatch is not None:
+                if not 0 < int(n_minibatch):
+                    raise ValueError("n_minibatch must be positive")
+                self.M = int(n_minibatch)
+                self.gather = True
+                self.default_scale = self.N / self.M
+                self.Xb = torch.empty(self.M, spec.D, dtype=torch.float32, device=dev)
+                self.yb = torch.empty(self.M, dtype=torch.float32, device=dev)
+            else:
+                self.M = self.N
+                self.Xb, self.yb = self.X_full, self.y_full
+            self._fed = {"X": True, "y": True}
+        else:
+            if n_minibatch is not None:
+                raise ValueError("n_minibatch needs X and y bound to arrays in the data dict")
+            if bound_X:
+                self.M = spec.X.shape[0]
+            elif spec.batch is not None:
+                self.M = spec.batch
+            else:
+                raise ValueError("the X placeholder needs a static number of rows")
+            self.Xb = (torch.as_tensor(spec.X).contiguous().to(dev) if bound_X else
+                       torch.zeros(self.M, spec.D, dtype=torch.float32, device=dev))
+            if bound_y:
+                if spec.y.shape[0] != self.M:
+                    raise ValueError(f"y has {spec.y.shape[0]} rows; X has {self.M}")
+                self.yb = torch.as_tensor(spec.y, dtype=torch.float32).contiguous().to(dev)
+            else:
+                self.yb = torch.zeros(self.M, dtype=torch.float32, device=dev)
+            self._fed = {"X": bound_X, "y": bound_y}
+        self.seed = None
+
+    @property
+    def ready(self):
+        return all(self._fed.values())
+
+    def feed(self, feed_dict):
+        for k, v in feed_dict.items():
+            if k is self.spec.X_node and not self.gather:
+                v = np.asarray(v, np.float32)
+                if v.shape != (self.M, self.spec.D):
+                    raise ValueError(f"fed X has shape {v.shape}; expected {(self.M, self.spec.D)}")
+                self.Xb.copy_(torch.from_numpy(np.ascontiguousarray(v)))
+                self._fed["X"] = True
+            elif k is self.spec.y_node and not self.gather:
+                v = np.asarray(v, np.float32).reshape(-1)
+                if v.shape[0] != self.M:
+                    raise ValueError(f"fed y has {v.shape[0]} rows; expected {self.M}")
+                self.yb.copy_(torch.from_numpy(v))
+                self._fed["y"] = True
+            else:
+                raise KeyError(f"{k!r} is not a placeholder of this model")
+
+    def batch(self, state):
+        """(X, y) device buffers for the next step; gathers on the device when
+        minibatching from bound arrays (stream-ordered, graph-capturable)."""
+        if not self.ready:
+            raise ValueError("X / y are placeholders: feed them with update(feed_dict=...)")
+        if self.gather:
+            _lib.call("edg_minibatch_gather", _lib.ptr(self.X_full), _lib.ptr(self.y_full), self.N,
+                      self.spec.D, self.M, int(self.seed), _lib.ptr(state), _lib.ptr(self.Xb),
+                      _lib.ptr(self.yb), _lib.stream_ptr())
+        return self.Xb, self.yb
+
+
+def bnn_config(D, H1, H2, n_samples, noise, prior_scale=1.0, data_scale=1.0, method=0, seed=0):
+    cfg = _lib.EdgBNN()
+    cfg.D, cfg.H1, cfg.H2, cfg.n_samples = D, H1, H2, n_samples
+    cfg.noise, cfg.prior_scale, cfg.data_scale = noise, prior_scale, data_scale
+    cfg.method, cfg.seed = method, seed
+    return cfg
+
+
+def bnn_loglik_grad(cfg, X, y, theta):
+    """(ll [S] float64, grad [S, P] float32) of the scaled Gaussian log-likelihood
+    of the network for S weight vectors ``theta`` [S, P] over rows X [M, D], y [M]."""
+    theta = theta.detach().to(torch.float32).contiguous()
+    S, P = theta.shape
+    if S != cfg.n_samples:
+        cfg = bnn_config(cfg.D, cfg.H1, cfg.H2, S, cfg.noise, cfg.prior_scale, cfg.data_scale,
+                         cfg.method, cfg.seed)
+    lib = _lib.load()
+    M = X.shape[0]
+    if P != lib.edg_bnn_num_params(cfg.D, cfg.H1, cfg.H2):
+        raise ValueError("theta has the wrong number of parameters")
+    ws_bytes = lib.edg_bnn_workspace_bytes(ctypes.byref(cfg), M)
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=theta.device)
+    ll = torch.empty(S, dtype=torch.float64, device=theta.device)
+    g = torch.empty(S, P, dtype=torch.float32, device=theta.device)
+    _lib.call("edg_bnn_loglik_grad", ctypes.byref(cfg), _lib.ptr(X.contiguous()),
+              _lib.ptr(y.contiguous()), M, _lib.ptr(theta), _lib.ptr(ll), _lib.ptr(g),
+              _lib.ptr(ws), ws_bytes, _lib.stream_ptr())
+    return ll, g
+
+
+class BNNLogLik(torch.autograd.Function):
+    """Per-sample network log-likelihood with the hand-written adjoint as
+    backward (replaces ``tf.gradients`` of ``p_log_lik``, ``klqp.py:746-767``)."""
+
+    @staticmethod
+    def forward(ctx, theta, cfg, X, y):
+        ll, g = bnn_loglik_grad(cfg, X, y, theta)
+        ctx.save_for_backward(g)
+        return ll.to(theta.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        return (grad_out.to(g.dtype)[:, None] * g).to(grad_out.dtype), None, None, None
+
+
+def bnn_log_lik(cfg, X, y, theta):
+    return BNNLogLik.apply(theta, cfg, X, y)

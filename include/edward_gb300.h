@@ -217,6 +217,8 @@ typedef struct {
   float noise;           /* Normal likelihood scale */
   float prior_scale;     /* Normal(0, prior_scale) on every weight and bias */
   float data_scale;      /* minibatch scale N / M (Inference.scale[y]) */
+  int32_t method;        /* EDG_KLQP_REPARAM_KL (analytic KL) or EDG_KLQP_REPARAM (Monte Carlo
+                            KL, build_reparam_loss_and_gradients, klqp.py:642-704) */
   uint64_t seed;
 } edg_bnn_t;
 
@@ -226,6 +228,14 @@ int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, const float* X
                       int32_t M, float* mu, float* rho, float* opt_slots, edg_state_t* state,
                       const float* eps_override, float* grad_out, int32_t apply,
                       void* workspace, size_t workspace_bytes, void* stream);
+/* The log-likelihood half of the step on its own: for S given weight samples
+ * theta [S,P], ll_out[s] = data_scale * sum_m log N(y_m | net(X_m; theta_s), noise)
+ * (FP64) and grad_out [S,P] = d ll_out[s] / d theta_s, by the batched forward
+ * pass and the hand-written adjoint (what tf.gradients of the reference's
+ * p_log_lik yields per sample, klqp.py:746-767).  Backs the autograd Function. */
+int edg_bnn_loglik_grad(const edg_bnn_t* cfg, const float* X, const float* y, int32_t M,
+                        const float* theta, double* ll_out, float* grad_out, void* workspace,
+                        size_t workspace_bytes, void* stream);
 /* Minibatch of M rows drawn uniformly with replacement from X [N,D] / y [N]
  * (Philox KIND 4 at iteration state->t) into Xb [M,D] / yb [M]; replaces the
  * host-side feed_dict batches of the reference examples. */

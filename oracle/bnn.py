@@ -65,19 +65,31 @@ def log_lik_and_grad(theta, X, y, noise, scale, D, H1, H2):
     return ll, g
 
 
-def klqp_loss_and_grads(mu, rho, eps, X, y, noise, scale, D, H1, H2, prior_scale=1.0):
-    """-ELBO (analytic KL to N(0, prior_scale)) and its gradient w.r.t. (mu, rho)."""
+def klqp_loss_and_grads(mu, rho, eps, X, y, noise, scale, D, H1, H2, prior_scale=1.0,
+                        method=0):
+    """-ELBO and its gradient w.r.t. (mu, rho).  ``method`` 0: analytic KL to
+    N(0, prior_scale) (``klqp.py:707-769``); 1: Monte Carlo KL,
+    -mean_s[log p(x|z_s) + log p(z_s) - log q(z_s)] with the gradient through
+    z_s and q's parameters (``klqp.py:642-704``)."""
     mu = np.asarray(mu, np.float64)
     rho = np.asarray(rho, np.float64)
     eps = np.asarray(eps, np.float64)
     sig = dn.softplus(rho)
     theta = mu[None, :] + sig[None, :] * eps
     ll, g = log_lik_and_grad(theta, X, y, noise, scale, D, H1, H2)
-    kl = dn.kl_normal_normal(mu, sig, 0.0, prior_scale)
-    dkl_mu, dkl_sig = dn.kl_normal_normal_grads(mu, sig, 0.0, prior_scale)
-    loss = -(ll.mean() - kl.sum())
-    gmu = -g.mean(axis=0) + dkl_mu
-    gsig = -(g * eps).mean(axis=0) + dkl_sig
+    if method == 0:
+        kl = dn.kl_normal_normal(mu, sig, 0.0, prior_scale)
+        dkl_mu, dkl_sig = dn.kl_normal_normal_grads(mu, sig, 0.0, prior_scale)
+        loss = -(ll.mean() - kl.sum())
+        gmu = -g.mean(axis=0) + dkl_mu
+        gsig = -(g * eps).mean(axis=0) + dkl_sig
+    else:
+        lp = dn.normal_log_prob(theta, 0.0, prior_scale).sum(axis=1)
+        lq = dn.normal_log_prob(theta, mu, sig).sum(axis=1)
+        loss = -(ll + lp - lq).mean()
+        dfdz = g - theta / prior_scale ** 2             # log q's z- and mu-terms cancel
+        gmu = -dfdz.mean(axis=0)
+        gsig = -(dfdz * eps).mean(axis=0) - 1.0 / sig
     return float(loss), gmu, gsig * dn.sigmoid(rho)
 
 
@@ -91,3 +103,13 @@ def synthetic(N, D, H1, H2, noise=0.1, seed=0):
     y = np.tanh(np.tanh(X @ W0) @ W1) @ W2
     y = (y[:, 0] + noise * rng.standard_normal(N)).astype(np.float32)
     return X, y
+
+
+def minibatch_rows(seed, iteration, M, N):
+    """Rows drawn by the device minibatch gather at one iteration: the first
+    word of Philox stream 4, counter (0, m, iteration, 4), mapped to [0, N) by
+    (u * N) >> 32."""
+    from .philox import KIND_MINIBATCH, raw_u32
+    u = raw_u32(seed, KIND_MINIBATCH, iteration, M, 1)[:, 0].astype(np.uint64)
+    return ((u * np.uint64(N)) >> np.uint64(32)).astype(np.int64)
+

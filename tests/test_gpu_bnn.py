@@ -103,3 +103,143 @@ def test_bnn_adam_steps(cuda):
         got = torch.cat([t["mu"], t["rho"]]).cpu().numpy()
         close(got, th, 5e-5)
     assert _lib.read_state(t["state"]).t == 3
+
+
+# ------------------------------------------------------------- public API
+
+def _oracle_args(inf, X, y, scale):
+    spec = inf._spec
+    return (X, y, spec.noise, scale, spec.D, spec.H1, spec.H2, spec.prior_scale)
+
+
+def test_bnn_klqp_api_full_batch_matches_oracle(cuda):
+    """ed.KLqp on the network of examples/bayesian_nn.py: the loss and gradients
+    for given draws, then two update() calls with in-kernel Philox draws, against
+    the oracle with the same draws and TF's Adam."""
+    import edward_gb300 as ed
+    from bnn_model import example_model, example_q, flat_q
+    from oracle import philox
+    D, H1, H2, N, S = 3, 12, 9, 57, 3
+    X, y = bnn.synthetic(N, D, H1, H2, seed=11)
+    latents, _, yrv = example_model(D, H1, H2, X=X, noise=0.2)
+    qs = example_q(latents, np.random.default_rng(1))
+    inf = ed.KLqp(qs, data={yrv: y})
+    inf.initialize(n_samples=S, optimizer=ed.train.AdamOptimizer(0.01))
+    mu, rho = flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")
+    P = mu.size
+    args = _oracle_args(inf, X, y, 1.0)
+    eps = np.random.default_rng(2).standard_normal((S, P)).astype(np.float32)
+    loss, gmu, grho = inf.loss_and_gradients(eps)
+    l0, m0, r0 = bnn.klqp_loss_and_grads(mu, rho, eps, *args)
+    assert abs(loss - l0) <= 1e-5 * abs(l0)
+    close(gmu.cpu().numpy(), m0, 2e-5)
+    close(grho.cpu().numpy(), r0, 2e-5)
+    opt = TFAdam(2 * P)
+    th = np.concatenate([mu, rho]).astype(np.float64)
+    for t in range(2):
+        e = philox.normals(inf.seed, philox.KIND_EPS, t, S, P)
+        lo, gm, gr = bnn.klqp_loss_and_grads(th[:P], th[P:], e, *args)
+        info = inf.update()
+        assert info["t"] == t + 1
+        assert abs(info["loss"] - lo) <= 1e-5 * abs(lo)
+        th = opt.apply(th, np.concatenate([gm, gr]), 0.01)
+        got = np.concatenate([flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")])
+        close(got, th, 5e-5)
+
+
+def test_bnn_klqp_api_feed_dict_minibatches(cuda):
+    """Placeholders X [M, D] / y [M] fed per update, scale = N / M, as the
+    reference's minibatch loops do."""
+    import edward_gb300 as ed
+    from bnn_model import example_model, example_q, flat_q
+    from oracle import philox
+    D, H1, H2, N, M, S = 4, 10, 6, 200, 32, 2
+    X, y = bnn.synthetic(N, D, H1, H2, seed=4)
+    Xp = ed.placeholder(shape=[M, D], name="X")
+    yp = ed.placeholder(shape=[M], name="y")
+    latents, _, yrv = example_model(D, H1, H2, X=Xp, noise=0.3)
+    qs = example_q(latents, np.random.default_rng(3))
+    inf = ed.KLqp(qs, data={yrv: yp})
+    inf.initialize(n_samples=S, scale={yrv: N / M}, optimizer=ed.train.AdamOptimizer(0.01))
+    with pytest.raises(ValueError):
+        inf.update()                         # nothing fed yet
+    th = np.concatenate([flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")])
+    th = th.astype(np.float64)
+    P = th.size // 2
+    opt = TFAdam(2 * P)
+    for t in range(3):
+        sl = slice(t * M, (t + 1) * M)
+        info = inf.update(feed_dict={Xp: X[sl], yp: y[sl]})
+        e = philox.normals(inf.seed, philox.KIND_EPS, t, S, P)
+        lo, gm, gr = bnn.klqp_loss_and_grads(th[:P], th[P:], e, X[sl], y[sl], 0.3, N / M,
+                                             D, H1, H2, 1.0)
+        assert abs(info["loss"] - lo) <= 1e-5 * abs(lo)
+        th = opt.apply(th, np.concatenate([gm, gr]), 0.01)
+    got = np.concatenate([flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")])
+    close(got, th, 5e-5)
+
+
+def test_bnn_klqp_api_device_minibatch(cuda):
+    """n_minibatch=M gathers M rows on the device (Philox stream 4) with scale
+    N / M; the rows and the step equal the oracle's."""
+    import edward_gb300 as ed
+    from bnn_model import example_model, example_q, flat_q
+    from oracle import philox
+    D, H1, H2, N, M, S = 5, 16, 8, 1000, 48, 2
+    X, y = bnn.synthetic(N, D, H1, H2, seed=6)
+    latents, _, yrv = example_model(D, H1, H2, X=X, noise=0.25)
+    qs = example_q(latents, np.random.default_rng(5))
+    inf = ed.KLqp(qs, data={yrv: y})
+    inf.initialize(n_samples=S, n_minibatch=M, optimizer=ed.train.AdamOptimizer(0.01))
+    th = np.concatenate([flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")])
+    th = th.astype(np.float64)
+    P = th.size // 2
+    opt = TFAdam(2 * P)
+    for t in range(2):
+        info = inf.update()
+        rows = bnn.minibatch_rows(inf._bnn.seed, t, M, N)
+        np.testing.assert_array_equal(inf._bnn.Xb.cpu().numpy(), X[rows])
+        e = philox.normals(inf.seed, philox.KIND_EPS, t, S, P)
+        lo, gm, gr = bnn.klqp_loss_and_grads(th[:P], th[P:], e, X[rows], y[rows], 0.25, N / M,
+                                             D, H1, H2, 1.0)
+        assert abs(info["loss"] - lo) <= 1e-5 * abs(lo)
+        th = opt.apply(th, np.concatenate([gm, gr]), 0.01)
+    got = np.concatenate([flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")])
+    close(got, th, 5e-5)
+
+
+def test_bnn_reparameterization_klqp_monte_carlo_kl(cuda):
+    """ReparameterizationKLqp (Monte Carlo KL, klqp.py:642-704) on the network."""
+    import edward_gb300 as ed
+    from bnn_model import example_model, example_q, flat_q
+    D, H1, H2, N, S = 3, 8, 8, 40, 4
+    X, y = bnn.synthetic(N, D, H1, H2, seed=8)
+    latents, _, yrv = example_model(D, H1, H2, X=X, noise=0.2, prior_scale=1.5)
+    qs = example_q(latents, np.random.default_rng(7))
+    inf = ed.ReparameterizationKLqp(qs, data={yrv: y})
+    inf.initialize(n_samples=S)
+    mu, rho = flat_q(qs, latents, "loc"), flat_q(qs, latents, "scale")
+    eps = np.random.default_rng(9).standard_normal((S, mu.size)).astype(np.float32)
+    loss, gmu, grho = inf.loss_and_gradients(eps)
+    l0, m0, r0 = bnn.klqp_loss_and_grads(mu, rho, eps, X, y, 0.2, 1.0, D, H1, H2, 1.5, method=1)
+    assert abs(loss - l0) <= 1e-5 * abs(l0)
+    close(gmu.cpu().numpy(), m0, 2e-5)
+    close(grho.cpu().numpy(), r0, 2e-5)
+
+
+def test_bnn_log_lik_autograd_function(cuda):
+    """The torch.autograd.Function over the hand-written adjoint: backward of a
+    weighted sum of per-sample log-likelihoods equals the oracle's gradient."""
+    from edward_gb300 import ops
+    D, H1, H2, M, S = 6, 20, 12, 90, 3
+    X, y = bnn.synthetic(M, D, H1, H2, seed=12)
+    P = bnn.n_params(D, H1, H2)
+    theta = (np.random.default_rng(13).standard_normal((S, P)) * 0.3).astype(np.float32)
+    cfg = ops.bnn_config(D, H1, H2, S, noise=0.4, data_scale=3.0)
+    th = torch.tensor(theta, device=cuda, requires_grad=True)
+    ll = ops.bnn_log_lik(cfg, torch.as_tensor(X, device=cuda), torch.as_tensor(y, device=cuda), th)
+    w = torch.tensor([1.0, -0.5, 2.0], device=cuda)
+    (ll * w).sum().backward()
+    ll0, g0 = bnn.log_lik_and_grad(theta, X, y, 0.4, 3.0, D, H1, H2)
+    close(ll.detach().cpu().numpy(), ll0, 1e-5)
+    close(th.grad.cpu().numpy(), g0 * np.array([1.0, -0.5, 2.0])[:, None], 2e-5)

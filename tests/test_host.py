@@ -188,3 +188,67 @@ def test_hmc_validates_hierarchical_model_on_host():
     inf.auto_transform = True
     inf._validate()
     assert inf._family == "hier"
+
+
+# ------------------------------------------------------------- Bayesian NN family
+
+def test_compile_bayesian_nn_example_model():
+    from bnn_model import example_model
+    from edward_gb300.compile import compile_mlp
+    X = np.zeros((40, 3), np.float32)
+    y = np.zeros(40, np.float32)
+    latents, _, yrv = example_model(3, 10, 7, X=ed.placeholder(shape=[40, 3]), noise=0.1,
+                                    prior_scale=2.0)
+    spec = compile_mlp(latents, {yrv: y})
+    assert (spec.D, spec.H1, spec.H2) == (3, 10, 7)
+    assert spec.noise == pytest.approx(0.1) and spec.prior_scale == 2.0
+    assert spec.batch == 40 and spec.X is None
+    assert [b.offset for b in spec.blocks] == [0, 30, 40, 110, 117, 124]
+    assert spec.P == 125
+    Xp = spec.X_node
+    spec = compile_mlp(latents, {yrv: y, Xp: X})
+    assert spec.X.shape == (40, 3) and spec.y.shape == (40,)
+
+
+def test_compile_bayesian_nn_rejects_other_networks():
+    from bnn_model import example_model
+    from edward_gb300.compile import compile_mlp
+    latents, Xn, yrv = example_model(2, 4, 4, X=np.zeros((5, 2), np.float32))
+    with pytest.raises(UnsupportedModel):   # a latent missing from the dict
+        compile_mlp(latents[:-1], {yrv: np.zeros(5)})
+    W0 = latents[0]
+    W0.loc = ed.ones([2, 4])                # non-zero prior mean
+    with pytest.raises(UnsupportedModel):
+        compile_mlp(latents, {yrv: np.zeros(5)})
+    latents, Xn, _ = example_model(2, 4, 4, X=np.zeros((5, 2), np.float32))
+    h = ed.sigmoid(ed.matmul(Xn, latents[0]) + latents[1])
+    h = ed.tanh(ed.matmul(h, latents[2]) + latents[3])
+    y2 = Normal(loc=ed.reshape(ed.matmul(h, latents[4]) + latents[5], [-1]), scale=0.1)
+    with pytest.raises(UnsupportedModel):   # sigmoid hidden layer
+        compile_mlp(latents, {y2: np.zeros(5)})
+
+
+def test_klqp_dispatches_bayesian_nn_on_host():
+    """KLqp recognises the network (GLM compile fails, MLP compile succeeds)
+    before any device work; the checks that need no GPU run here."""
+    from bnn_model import example_model, example_q
+    latents, Xn, yrv = example_model(2, 4, 4, X=np.zeros((5, 2), np.float32))
+    qs = example_q(latents, np.random.default_rng(0))
+    inf = ed.KLqp(qs, data={yrv: np.zeros(5, np.float32)})
+    with pytest.raises(NotImplementedError):
+        inf.initialize(kl_scaling={latents[0]: 2.0})
+    inf = ed.ScoreKLqp(qs, data={yrv: np.zeros(5, np.float32)})
+    with pytest.raises(NotImplementedError):
+        inf.initialize()
+    inf = ed.KLqp(qs, data={yrv: np.zeros(5, np.float32)})
+    with pytest.raises(RuntimeError):       # the model compiles; the step needs the GPU
+        inf.initialize(n_samples=2)
+    assert inf._family == "bnn"
+
+
+def test_minibatch_rows_oracle_is_uniform():
+    from oracle import bnn
+    rows = bnn.minibatch_rows(5, 3, 20000, 7)
+    assert rows.min() == 0 and rows.max() == 6
+    counts = np.bincount(rows, minlength=7)
+    assert np.all(np.abs(counts - 20000 / 7) < 5 * np.sqrt(20000 / 7))
