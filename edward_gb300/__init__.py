@@ -12,7 +12,7 @@ Usage mirrors ``import edward as ed``::
 """
 __version__ = "1.3.5+gb300.0.1"
 
-from . import models, train
+from . import layers, models, train
 from .expr import (Variable, placeholder, dot, matmul, tanh, sigmoid, softplus, reshape, cast,
                    zeros, ones)
 from .inferences import (Inference, VariationalInference, KLqp, ReparameterizationKLqp,

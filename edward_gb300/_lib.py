@@ -27,6 +27,7 @@ EDG_E_NONFINITE, EDG_E_TIMEOUT, EDG_E_UNSUPPORTED, EDG_E_WORKSPACE = -5, -6, -7,
 
 LIK_BERNOULLI, LIK_NORMAL = 0, 1
 KLQP_REPARAM_KL, KLQP_REPARAM, KLQP_SCORE = 0, 1, 2
+BASELINE_NONE, BASELINE_MEAN, BASELINE_MLP = 0, 1, 2
 OPT_ADAM, OPT_SGD, OPT_MOMENTUM, OPT_ADAGRAD, OPT_RMSPROP, OPT_ADADELTA = range(6)
 
 
@@ -64,6 +65,12 @@ class EdgBNN(ctypes.Structure):
     _fields_ = [("D", c_int32), ("H1", c_int32), ("H2", c_int32), ("n_samples", c_int32),
                 ("noise", c_float), ("prior_scale", c_float), ("data_scale", c_float),
                 ("method", c_int32), ("seed", c_uint64)]
+
+
+class EdgSBN(ctypes.Structure):
+    _fields_ = [("V", c_int32), ("H0", c_int32), ("H1", c_int32), ("n_samples", c_int32),
+                ("baseline", c_int32), ("baseline_hidden", c_int32), ("baseline_decay", c_float),
+                ("reserved", c_float), ("seed", c_uint64)]
 
 
 class EdgHMC(ctypes.Structure):
@@ -105,6 +112,16 @@ _SIGS = {
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "edg_minibatch_gather": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_uint64,
                                        c_void_p, c_void_p, c_void_p, c_void_p]),
+    "edg_sbn_num_params": (c_int32, [c_int32, c_int32, c_int32]),
+    "edg_sbn_baseline_num_params": (c_int32, [c_int32, c_int32]),
+    "edg_sbn_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgSBN), c_int32]),
+    "edg_sbn_score_step": (c_int32, [ctypes.POINTER(EdgSBN), ctypes.POINTER(EdgOpt),
+                                     ctypes.POINTER(EdgOpt), c_void_p, c_int32, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_size_t,
+                                     c_void_p]),
+    "edg_minibatch_gather_u8": (c_int32, [c_void_p, c_int64, c_int32, c_int32, c_uint64, c_void_p,
+                                          c_void_p, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

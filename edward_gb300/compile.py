@@ -389,3 +389,106 @@ def compile_mlp(latents, data):
     return MLPSpec(D=D, H1=H1, H2=H2, noise=noise, prior_scale=prior_scale, X=X, y=y,
                    X_node=Xn, y_node=yval if isinstance(yval, Placeholder) else None,
                    blocks=blocks, observed=yrv, batch=batch)
+
+
+# ------------------------------------------------------------- sigmoid belief network
+
+@dataclass
+class SBNSpec:
+    """Two-layer sigmoid belief network with its recognition network
+    (``examples/sigmoid_belief_network.py:54-86``, hidden_sizes = [H0, H1]).
+    ``weights`` holds the eight (kernel, bias) Variables in the order
+    Wq0, bq0, Wq1, bq1, Wp1, bp1, Wp0, bp0."""
+    V: int
+    H0: int
+    H1: int
+    prior_logits: np.ndarray
+    weights: list
+    X: np.ndarray = None          # bound data [N, V] (uint8 or float), else None
+    x_node: Node = None           # the placeholder fed per update
+    batch: int = None             # rows per step of a placeholder with static shape
+    observed: RandomVariable = None
+    z0: RandomVariable = None
+    z1: RandomVariable = None
+
+
+def _strip_cast(node):
+    while isinstance(node, Op) and node.op == "cast":
+        node = node.args[0]
+    return node
+
+
+def _dense_parts(node, what):
+    """matmul(a, W) + b with Variables W, b  ->  (a, W, b)."""
+    terms = flatten_add(node)
+    mm = [t for t in terms if isinstance(t, Op) and t.op == "matmul"]
+    bs = [t for t in terms if isinstance(t, Variable)]
+    if len(terms) != 2 or len(mm) != 1 or len(bs) != 1:
+        raise UnsupportedModel(f"{what}: logits must be a dense layer matmul(h, W) + b")
+    a, W = mm[0].args
+    if not isinstance(W, Variable):
+        raise UnsupportedModel(f"{what}: the dense kernel must be a Variable")
+    return _strip_cast(a), W, bs[0]
+
+
+def compile_sbn(latent_vars, data):
+    """``latent_vars``: {z0: qz0, z1: qz1}; ``data``: {x: x_ph or array}."""
+    observed, bindings = _split_data(data)
+    if len(observed) != 1 or len(latent_vars) != 2:
+        raise UnsupportedModel("the sigmoid belief network has one observed and two latent layers")
+    (xrv, xval), = observed.items()
+    if not (isinstance(xrv, Bernoulli) and xrv.logits is not None):
+        raise UnsupportedModel("the sigmoid belief network needs x ~ Bernoulli(logits=...)")
+    z0, Wp0, bp0 = _dense_parts(xrv.logits, "x")
+    if not (isinstance(z0, Bernoulli) and z0 in latent_vars and z0.logits is not None):
+        raise UnsupportedModel("x's logits must be a dense layer of a latent Bernoulli layer")
+    z1, Wp1, bp1 = _dense_parts(z0.logits, "z0")
+    if not (isinstance(z1, Bernoulli) and z1 in latent_vars and z1.logits is not None):
+        raise UnsupportedModel("z0's logits must be a dense layer of the top latent layer")
+    pl = const_value(z1.logits, bindings)
+    if pl is None:
+        raise UnsupportedModel("the top layer's logits must be constant")
+    pl = np.asarray(pl, np.float32)
+    pl2 = pl.reshape(-1, pl.shape[-1]) if pl.ndim else pl.reshape(1, 1)
+    if not np.all(pl2 == pl2[:1]):
+        raise UnsupportedModel("the top layer's logits must be the same for every row")
+    qz0, qz1 = latent_vars[z0], latent_vars[z1]
+    for q in (qz0, qz1):
+        if not (isinstance(q, Bernoulli) and q.logits is not None):
+            raise UnsupportedModel("the recognition network must be Bernoulli(logits=...) layers")
+    xin, Wq0, bq0 = _dense_parts(qz0.logits, "q(z0)")
+    a1, Wq1, bq1 = _dense_parts(qz1.logits, "q(z1)")
+    if a1 is not qz0:
+        raise UnsupportedModel("q(z1)'s logits must be a dense layer of q(z0)")
+    x_node = xval if isinstance(xval, Node) else None
+    if x_node is not None and xin is not x_node:
+        raise UnsupportedModel("q(z0)'s logits must be a dense layer of the data bound to x")
+    V = int(Wq0.shape[0])
+    H0, H1 = int(Wq0.shape[1]), int(Wq1.shape[1])
+    want = {"Wq0": (Wq0, (V, H0)), "bq0": (bq0, (H0,)), "Wq1": (Wq1, (H0, H1)), "bq1": (bq1, (H1,)),
+            "Wp1": (Wp1, (H1, H0)), "bp1": (bp1, (H0,)), "Wp0": (Wp0, (H0, V)), "bp0": (bp0, (V,))}
+    for k, (var, shp) in want.items():
+        if tuple(var.shape) != shp:
+            raise UnsupportedModel(f"{k} has shape {tuple(var.shape)}; the network needs {shp}")
+    if pl2.shape[-1] != H1:
+        raise UnsupportedModel(f"the top layer's logits have width {pl2.shape[-1]}; expected {H1}")
+    weights = [v for v, _ in want.values()]
+    if len(set(map(id, weights))) != 8:
+        raise UnsupportedModel("every dense layer needs its own kernel and bias")
+    X, batch = None, None
+    if x_node is None:
+        X = np.asarray(xval)
+    else:
+        bound = const_value(x_node, bindings) if isinstance(x_node, Placeholder) else None
+        if bound is not None:
+            X = np.asarray(bindings[x_node])
+        elif isinstance(x_node, Placeholder) and x_node.shape and x_node.shape[0] is not None:
+            batch = int(x_node.shape[0])
+        else:
+            raise UnsupportedModel("the data placeholder needs the static shape [B, V]")
+    if X is not None:
+        if X.ndim != 2 or X.shape[1] != V:
+            raise ValueError(f"x data has shape {X.shape}; expected [N, {V}]")
+        X = np.ascontiguousarray(X if X.dtype == np.uint8 else X.astype(np.float32))
+    return SBNSpec(V=V, H0=H0, H1=H1, prior_logits=pl2[0].astype(np.float32), weights=weights,
+                   X=X, x_node=x_node, batch=batch, observed=xrv, z0=z0, z1=z1)

@@ -18,131 +18,17 @@
 #include <algorithm>
 
 #include "edg_common.cuh"
+#include "gemm_simt.cuh"
+#include "optim.cuh"
 
 namespace edg {
 namespace bnn {
 
-constexpr int BM = 64, BN = 64, BK = 16, kT = 256;
-
-// ------------------------------------------------------------ batched GEMM
-// C[b](m, n) = epi(b, m, n, sum_k A[b](m, k) B[b](k, n)); A(m, k) is
-// A[b*sA + m*lda + k] (or A[b*sA + k*lda + m] when TA), B(k, n) is
-// B[b*sB + k*ldb + n] (or B[b*sB + n*ldb + k] when TB).
-template <bool TA, bool TB, class Epi>
-__global__ void __launch_bounds__(kT) bgemm_kernel(const float* __restrict__ A,
-                                                   const float* __restrict__ B, float* C, int M,
-                                                   int N, int K, int lda, int ldb, int ldc,
-                                                   int64_t sA, int64_t sB, int64_t sC, Epi epi) {
-  __shared__ __align__(16) float As[2][BK][BM + 4];
-  __shared__ __align__(16) float Bs[2][BK][BN + 4];
-  const int b = blockIdx.z;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const float* Ab = A + b * sA;
-  const float* Bb = B + b * sB;
-  const int tid = threadIdx.x;
-  const int tm = tid / 16, tn = tid % 16;  // 16 x 16 threads, 4 x 4 outputs each
-  float acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
-
-  auto load = [&](int buf, int k0) {
-    // 64 x 16 elements of A and of B, 4 per thread
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int e = tid + r * kT;
-      // A tile: As[k][m]
-      int mm, kk;
-      if (TA) {
-        kk = e / BM;
-        mm = e % BM;
-      } else {
-        mm = e / BK;
-        kk = e % BK;
-      }
-      const int gm = m0 + mm, gk = k0 + kk;
-      float va = 0.0f;
-      if (gm < M && gk < K) va = TA ? Ab[(int64_t)gk * lda + gm] : Ab[(int64_t)gm * lda + gk];
-      As[buf][kk][mm] = va;
-      // B tile: Bs[k][n]
-      int nn, kb;
-      if (TB) {
-        nn = e / BK;
-        kb = e % BK;
-      } else {
-        kb = e / BN;
-        nn = e % BN;
-      }
-      const int gn = n0 + nn, gk2 = k0 + kb;
-      float vb = 0.0f;
-      if (gn < N && gk2 < K) vb = TB ? Bb[(int64_t)gn * ldb + gk2] : Bb[(int64_t)gk2 * ldb + gn];
-      Bs[buf][kb][nn] = vb;
-    }
-  };
-
-  const int nk = (K + BK - 1) / BK;
-  load(0, 0);
-  __syncthreads();
-  for (int t = 0; t < nk; ++t) {
-    const int buf = t & 1;
-    if (t + 1 < nk) load(buf ^ 1, (t + 1) * BK);
-#pragma unroll
-    for (int kk = 0; kk < BK; ++kk) {
-      const float4 a4 = *reinterpret_cast<const float4*>(&As[buf][kk][tm * 4]);
-      const float4 b4 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tn * 4]);
-      const float av[4] = {a4.x, a4.y, a4.z, a4.w};
-      const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-  float* Cb = C + b * sC;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + tm * 4 + i;
-    if (m >= M) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int n = n0 + tn * 4 + j;
-      if (n < N) Cb[(int64_t)m * ldc + n] = epi(b, m, n, acc[i][j]);
-    }
-  }
-}
-
-struct EpiIdentity {
-  __device__ float operator()(int, int, int, float v) const { return v; }
-};
-// tanh(v + bias[b][n])
-struct EpiBiasTanh {
-  const float* bias;
-  int64_t sBias;
-  __device__ float operator()(int b, int, int n, float v) const {
-    return tanhf(v + bias[b * sBias + n]);
-  }
-};
-// v * (1 - h^2) with h = H[b][m][n] (the tanh output being differentiated)
-struct EpiTanhGrad {
-  const float* H;
-  int64_t sH;
-  int ldh;
-  __device__ float operator()(int b, int m, int n, float v) const {
-    const float h = H[b * sH + (int64_t)m * ldh + n];
-    return v * (1.0f - h * h);
-  }
-};
-
-template <bool TA, bool TB, class Epi>
-static int bgemm(const float* A, const float* B, float* C, int M, int N, int K, int lda, int ldb,
-                 int ldc, int64_t sA, int64_t sB, int64_t sC, int batch, Epi epi,
-                 cudaStream_t st) {
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
-  bgemm_kernel<TA, TB, Epi><<<grid, kT, 0, st>>>(A, B, C, M, N, K, lda, ldb, ldc, sA, sB, sC, epi);
-  return check_launch("bnn bgemm");
-}
+constexpr int kT = 256;
+using simt::bgemm;
+using simt::EpiBiasTanh;
+using simt::EpiIdentity;
+using simt::EpiTanhGrad;
 
 // ------------------------------------------------------------ sampling
 struct Layout {
@@ -271,58 +157,11 @@ struct FinArgs {
   double* kl_part;  // [gridDim.x]
 };
 
-__device__ float opt_lr_b(const edg_opt_t& o, int64_t step) {
-  if (o.decay_steps <= 0) return o.lr0;
-  float p = (float)step / (float)o.decay_steps;
-  if (o.staircase) p = floorf(p);
-  return o.lr0 * powf(o.decay_rate, p);
-}
-
-__device__ float opt_apply_b(const edg_opt_t& o, float p, float g, float* s0, float* s1, float lr,
-                             float b1p, float b2p) {
-  switch (o.optimizer) {
-    case EDG_OPT_ADAM: {
-      const float lr_t = lr * sqrtf(1.0f - b2p) / (1.0f - b1p);
-      const float m = o.beta1 * *s0 + (1.0f - o.beta1) * g;
-      const float v = o.beta2 * *s1 + (1.0f - o.beta2) * g * g;
-      *s0 = m;
-      *s1 = v;
-      return p - lr_t * m / (sqrtf(v) + o.epsilon);
-    }
-    case EDG_OPT_SGD:
-      return p - lr * g;
-    case EDG_OPT_MOMENTUM: {
-      const float acc = o.momentum * *s0 + g;
-      *s0 = acc;
-      return p - lr * acc;
-    }
-    case EDG_OPT_ADAGRAD: {
-      const float acc = *s0 + g * g;
-      *s0 = acc;
-      return p - lr * g * rsqrtf(acc);
-    }
-    case EDG_OPT_RMSPROP: {
-      const float ms = o.rho * *s0 + (1.0f - o.rho) * g * g;
-      const float mom = o.momentum * *s1 + lr * g / sqrtf(ms + o.epsilon);
-      *s0 = ms;
-      *s1 = mom;
-      return p - mom;
-    }
-    default: {
-      const float acc = o.rho * *s0 + (1.0f - o.rho) * g * g;
-      const float upd = sqrtf(*s1 + o.epsilon) / sqrtf(acc + o.epsilon) * g;
-      *s0 = acc;
-      *s1 = o.rho * *s1 + (1.0f - o.rho) * upd * upd;
-      return p - lr * upd;
-    }
-  }
-}
-
 __global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
   __shared__ double red[kT / 32];
   __shared__ bool s_last;
   const int p = blockIdx.x * kT + threadIdx.x;
-  const float lr = opt_lr_b(a.opt, a.state->global_step);
+  const float lr = opt_lr(a.opt, a.state->global_step);
   const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
   double kl = 0.0;
   if (p < a.P) {
@@ -368,8 +207,8 @@ __global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
     }
     if (a.apply) {
       const int n = 2 * a.P;
-      a.mu[p] = opt_apply_b(a.opt, mu, gmu, a.slots + p, a.slots + n + p, lr, b1p, b2p);
-      a.rho[p] = opt_apply_b(a.opt, rho, grho, a.slots + a.P + p, a.slots + n + a.P + p, lr, b1p,
+      a.mu[p] = opt_apply(a.opt, mu, gmu, a.slots + p, a.slots + n + p, lr, b1p, b2p);
+      a.rho[p] = opt_apply(a.opt, rho, grho, a.slots + a.P + p, a.slots + n + a.P + p, lr, b1p,
                              b2p);
     }
   }

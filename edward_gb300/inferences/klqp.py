@@ -11,10 +11,10 @@ import numpy as np
 import torch
 
 from .. import _lib
-from ..compile import UnsupportedModel, compile_glm, compile_mlp, parse_normal_q
+from ..compile import UnsupportedModel, compile_glm, compile_mlp, compile_sbn, parse_normal_q
 from ..expr import Variable, softplus
 from ..models import Normal, RandomVariable
-from ..ops import BNNDevice, GLMDevice
+from ..ops import BNNDevice, GLMDevice, SBNDevice
 from ..util import next_seed, randn
 from .variational_inference import VariationalInference
 
@@ -77,9 +77,16 @@ class KLqp(VariationalInference):
         method = self._choose_method()
         if method == "score_rb":
             raise NotImplementedError(
-                "Rao-Blackwellised score gradients (ScoreRBKLqp) for this model family")
+                "Rao-Blackwellised score gradients (ScoreRBKLqp) are not implemented; "
+                "use ed.ScoreKLqp for models with discrete latent variables")
         self._method_id = method
         latents = list(self.latent_vars.keys())
+        if method == SCORE and all(not q.reparameterizable for q in self.latent_vars.values()):
+            self._spec = compile_sbn(self.latent_vars, self.data)
+            self._family = "sbn"
+            if self.kl_scaling or self.scale:
+                raise NotImplementedError("scale / kl_scaling for the sigmoid belief network")
+            return
         try:
             self._spec = compile_glm(latents, self.data)
             self._family = "glm"
@@ -103,6 +110,8 @@ class KLqp(VariationalInference):
     def build_loss_and_gradients(self, var_list):
         if self._family == "bnn":
             return self._build_bnn(var_list)
+        if self._family == "sbn":
+            return self._build_sbn(var_list)
         method = self._method_id
         spec = self._spec
         self._glm = GLMDevice(spec, self._device)
@@ -187,24 +196,93 @@ class KLqp(VariationalInference):
         self._grad = torch.zeros(2 * P, dtype=torch.float32, device=dev)
         return None, [(None, v) for v in q_vars]
 
+    def _build_sbn(self, var_list):
+        spec, dev = self._spec, self._device
+        lib = _lib.load()
+        V, H0, H1 = spec.V, spec.H0, spec.H1
+        P = lib.edg_sbn_num_params(V, H0, H1)
+        self._theta = torch.empty(P, dtype=torch.float32, device=dev)
+        off = 0
+        for i, (fin, fout) in enumerate(((V, H0), (H0, H1), (H1, H0), (H0, V))):
+            W, b = spec.weights[2 * i], spec.weights[2 * i + 1]
+            W._rebind(self._theta[off:off + fin * fout].view(fin, fout))
+            b._rebind(self._theta[off + fin * fout:off + (fin + 1) * fout])
+            off += (fin + 1) * fout
+        if var_list is not None and set(map(id, var_list)) != set(map(id, spec.weights)):
+            raise NotImplementedError("var_list must be every trainable weight of the network")
+        self._sbn = SBNDevice(spec, dev, self.n_minibatch)
+        self._sbn.seed = next_seed()
+        self._prior = torch.as_tensor(spec.prior_logits, device=dev)
+        mode = {"none": _lib.BASELINE_NONE, "mean": _lib.BASELINE_MEAN,
+                "mlp": _lib.BASELINE_MLP}[self.baseline]
+        cfg = _lib.EdgSBN()
+        cfg.V, cfg.H0, cfg.H1, cfg.n_samples = V, H0, H1, self.n_samples
+        cfg.baseline, cfg.baseline_hidden = mode, self.baseline_hidden
+        cfg.baseline_decay = self.baseline_decay
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        self._opt = self.optimizer.to_c()
+        self._bopt = self.baseline_optimizer.to_c()
+        self._slots = torch.zeros(2 * P, dtype=torch.float32, device=dev)
+        self._P = P
+        self._reset_optimizer()
+        BH = self.baseline_hidden
+        PB = lib.edg_sbn_baseline_num_params(V, BH)
+        lim = np.sqrt(6.0 / (V + BH))
+        bp = np.zeros(PB, np.float32)
+        bp[:V * BH] = np.random.uniform(-lim, lim, V * BH)
+        self._bparams = torch.as_tensor(bp, device=dev)
+        self._bslots = torch.zeros(2 * PB, dtype=torch.float32, device=dev)
+        a, b = self.baseline_optimizer.slot_init()
+        self._bslots[:PB].fill_(a)
+        self._bslots[PB:].fill_(b)
+        bo = self.baseline_optimizer
+        self._bstats = torch.tensor([0.0, 1.0, 0.0, getattr(bo, "beta1", 0.9),
+                                     getattr(bo, "beta2", 0.999), 0.0, 0.0, 0.0],
+                                    dtype=torch.float32, device=dev)
+        self._ws_bytes = lib.edg_sbn_workspace_bytes(cfg, self._sbn.B)
+        if self._ws_bytes == 0:
+            _lib.call("edg_sbn_workspace_bytes", cfg, self._sbn.B)
+        self._ws = torch.empty(self._ws_bytes, dtype=torch.uint8, device=dev)
+        self._grad = torch.zeros(P, dtype=torch.float32, device=dev)
+        return None, [(None, v) for v in spec.weights]
+
     def _feed(self, feed_dict):
-        if self._family != "bnn":
-            return super()._feed(feed_dict)
-        self._bnn.feed(feed_dict)
+        if self._family == "bnn":
+            return self._bnn.feed(feed_dict)
+        if self._family == "sbn":
+            return self._sbn.feed(feed_dict)
+        return super()._feed(feed_dict)
 
     def _run_loop(self):
         if self._family == "bnn" and not self._bnn.ready:
             raise ValueError("X / y are placeholders: feed them with update(feed_dict=...)")
+        if self._family == "sbn" and not self._sbn.fed:
+            raise ValueError("x is a placeholder: feed it with update(feed_dict=...)")
         super()._run_loop()
 
     def _reset_optimizer(self):
+        if self._family == "sbn":
+            a, b = self.optimizer.slot_init()
+            self._slots[:self._P].fill_(a)
+            self._slots[self._P:].fill_(b)
+            return
         a, b = self.optimizer.slot_init()
         P = self._spec.P
         self._slots[: 2 * P].fill_(a)
         self._slots[2 * P:].fill_(b)
 
-    def _step(self, apply=True, eps=None, grad_out=None):
+    def _step(self, apply=True, eps=None, grad_out=None, signal_out=None):
         import ctypes
+        if self._family == "sbn":
+            X = self._sbn.batch(self._state)
+            _lib.call("edg_sbn_score_step", ctypes.byref(self._cfg), ctypes.byref(self._opt),
+                      ctypes.byref(self._bopt), _lib.ptr(X), self._sbn.B, _lib.ptr(self._prior),
+                      _lib.ptr(self._theta), _lib.ptr(self._slots), _lib.ptr(self._state),
+                      _lib.ptr(self._bparams), _lib.ptr(self._bslots), _lib.ptr(self._bstats),
+                      _lib.ptr(eps), _lib.ptr(grad_out), _lib.ptr(signal_out), 1 if apply else 0,
+                      _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+            return
         if self._family == "bnn":
             X, y = self._bnn.batch(self._state)
             _lib.call("edg_bnn_klqp_step", ctypes.byref(self._cfg), ctypes.byref(self._opt),
@@ -250,5 +328,52 @@ class ReparameterizationKLKLqp(KLqp):
 
 
 class ScoreKLqp(KLqp):
-    """Score-function gradient, no baseline (klqp.py:370-430, 840-906)."""
+    """Score-function gradient (klqp.py:370-430, 840-906).
+
+    ``baseline`` (sigmoid belief network family): ``None`` / ``"none"`` is the
+    reference's estimator (no control variate); ``"mean"`` subtracts a running
+    mean of the per-row learning signal; ``"mlp"`` subtracts
+    c + sigma * mlp(x), a ``baseline_hidden``-unit tanh network trained online
+    on the (x, learning signal) pairs the estimator produces, with
+    ``baseline_optimizer`` (default Adam, learning rate 1e-3)."""
     _method = SCORE
+
+    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, baseline=None,
+                   baseline_hidden=100, baseline_optimizer=None, baseline_decay=0.9,
+                   *args, **kwargs):
+        from .. import train
+        self.baseline = baseline or "none"
+        if self.baseline not in ("none", "mean", "mlp"):
+            raise ValueError(f"baseline must be None, 'mean' or 'mlp'; got {baseline!r}")
+        self.baseline_hidden = int(baseline_hidden)
+        self.baseline_optimizer = (train.AdamOptimizer(1e-3) if baseline_optimizer is None
+                                   else train.resolve(baseline_optimizer, None))
+        if not 0.0 <= baseline_decay < 1.0:
+            raise ValueError("baseline_decay must be in [0, 1)")
+        self.baseline_decay = float(baseline_decay)
+        return super().initialize(n_samples, kl_scaling, n_minibatch, *args, **kwargs)
+
+    def _validate(self):
+        super()._validate()
+        if self._family != "sbn" and self.baseline != "none":
+            raise NotImplementedError("baselines are implemented for the sigmoid belief network")
+
+    def score_gradients(self, z=None, signal=False):
+        """(loss, grad [P]) at the current parameters without applying the
+        optimizer (sigmoid belief network); ``z`` = (z0 [S, B, H0], z1 [S, B, H1])
+        overrides the draws; ``signal=True`` also returns f [S, B] and the
+        learning signal [S, B]."""
+        if self._family != "sbn":
+            raise NotImplementedError("score_gradients is for the sigmoid belief network")
+        zo = None
+        if z is not None:
+            zo = torch.cat([torch.as_tensor(np.asarray(a, np.float32)).reshape(-1) for a in z])
+            zo = zo.to(self._device)
+        S, B = self.n_samples, self._sbn.B
+        sig = torch.empty(2 * S * B, dtype=torch.float32, device=self._device) if signal else None
+        self._step(apply=False, eps=zo, grad_out=self._grad, signal_out=sig)
+        st = self._read_state()
+        out = (float(st.loss), self._grad.detach().clone())
+        if signal:
+            out += (sig[:S * B].view(S, B).clone(), sig[S * B:].view(S, B).clone())
+        return out

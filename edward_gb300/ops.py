@@ -286,3 +286,60 @@ class BNNLogLik(torch.autograd.Function):
 
 def bnn_log_lik(cfg, X, y, theta):
     return BNNLogLik.apply(theta, cfg, X, y)
+
+
+class SBNDevice:
+    """Device data of a compiled sigmoid belief network (``compile.SBNSpec``)
+    and the source of each step's B rows: all N bound rows, a device gather
+    of ``n_minibatch`` rows from the bound data (uint8 on the device, Philox
+    stream 4), or the ``feed_dict`` array of the x placeholder."""
+
+    def __init__(self, spec, device="cuda", n_minibatch=None):
+        _lib.require_cuda()
+        self.spec = spec
+        self.device = torch.device(device)
+        self.gather = False
+        self.seed = None
+        if spec.X is not None:
+            X = np.asarray(spec.X)
+            if X.dtype != np.uint8:
+                if not np.all((X == 0) | (X == 1)):
+                    raise ValueError("Bernoulli data must be 0 or 1")
+                X = X.astype(np.uint8)
+            self.N = X.shape[0]
+            self.X_u8 = torch.as_tensor(np.ascontiguousarray(X)).to(self.device)
+            if n_minibatch is not None:
+                if int(n_minibatch) <= 0:
+                    raise ValueError("n_minibatch must be positive")
+                self.B = int(n_minibatch)
+                self.gather = True
+                self.Xb = torch.empty(self.B, spec.V, dtype=torch.float32, device=self.device)
+            else:
+                self.B = self.N
+                self.Xb = self.X_u8.float()
+            self.fed = True
+        else:
+            if n_minibatch is not None:
+                raise ValueError("n_minibatch needs x bound to an array in the data dict")
+            self.B = spec.batch
+            self.Xb = torch.zeros(self.B, spec.V, dtype=torch.float32, device=self.device)
+            self.fed = False
+
+    def feed(self, feed_dict):
+        for k, v in feed_dict.items():
+            if k is self.spec.x_node and not self.gather:
+                v = np.asarray(v, np.float32)
+                if v.shape != (self.B, self.spec.V):
+                    raise ValueError(f"fed x has shape {v.shape}; expected {(self.B, self.spec.V)}")
+                self.Xb.copy_(torch.from_numpy(np.ascontiguousarray(v)))
+                self.fed = True
+            else:
+                raise KeyError(f"{k!r} is not a placeholder of this model")
+
+    def batch(self, state):
+        if not self.fed:
+            raise ValueError("x is a placeholder: feed it with update(feed_dict=...)")
+        if self.gather:
+            _lib.call("edg_minibatch_gather_u8", _lib.ptr(self.X_u8), self.N, self.spec.V, self.B,
+                      int(self.seed), _lib.ptr(state), _lib.ptr(self.Xb), _lib.stream_ptr())
+        return self.Xb

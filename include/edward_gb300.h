@@ -243,6 +243,60 @@ int edg_minibatch_gather(const float* X, const float* y, int64_t N, int32_t D, i
                          uint64_t seed, const edg_state_t* state, float* Xb, float* yb,
                          void* stream);
 
+/* ---------------------------------------------------------------- sigmoid belief network
+ * ScoreKLqp for the two-layer sigmoid belief network of
+ * examples/sigmoid_belief_network.py:54-86 (hidden_sizes = [H0, H1]):
+ *   p: z1 ~ Bern(prior_logits), z0 ~ Bern(z1 Wp1 + bp1), x ~ Bern(z0 Wp0 + bp0)
+ *   q: z0 ~ Bern(x Wq0 + bq0),  z1 ~ Bern(z0 Wq1 + bq1)
+ * Parameters (edg_sbn_num_params): four blocks [in + 1, out] row-major, the
+ * bias being the last row: Wq0|bq0 [V+1, H0], Wq1|bq1 [H0+1, H1],
+ * Wp1|bp1 [H1+1, H0], Wp0|bp0 [H0+1, V] -- the q variables first.
+ * One call = one score-function gradient of the loss -mean_s sum_b
+ * [log p(x_b, z_sb) - log q(z_sb | x_b)] over B rows and S samples
+ * (build_score_loss_and_gradients, klqp.py:840-906: q-gradient
+ * -mean_s grad log q(z_s) * learning signal, p-gradient grad loss), then the
+ * optimizer apply.  The learning signal is
+ *   EDG_BASELINE_NONE: the sample's total F_s = sum_b f_sb (the reference);
+ *   EDG_BASELINE_MEAN: f_sb - c per row, c a running mean of f;
+ *   EDG_BASELINE_MLP:  f_sb - (c + sigma * mlp(x_b)) per row, mlp a
+ *       V -> baseline_hidden (tanh) -> 1 network trained online (one optimizer
+ *       step per call, on the row targets (mean_s f_sb - c) / sigma).
+ * Every variant is unbiased (the baseline depends on x and on earlier steps
+ * only).  z draws: Philox stream 3 at iteration state->t, counter row
+ * s*B + b, element j (z0) or round_up(H0, 4) + j (z1), z = u < sigmoid(logit)
+ * (TF's Bernoulli sampler); z_override [S*B*H0 z0 | S*B*H1 z1] replaces them. */
+enum { EDG_BASELINE_NONE = 0, EDG_BASELINE_MEAN = 1, EDG_BASELINE_MLP = 2 };
+typedef struct {
+  int32_t V, H0, H1;       /* visible width; hidden widths next to x and at the top */
+  int32_t n_samples;       /* S > 0 */
+  int32_t baseline;        /* EDG_BASELINE_* */
+  int32_t baseline_hidden; /* hidden width of the MLP baseline */
+  float baseline_decay;    /* decay of the running mean / scale, in [0, 1) */
+  float reserved;
+  uint64_t seed;
+} edg_sbn_t;
+
+int32_t edg_sbn_num_params(int32_t V, int32_t H0, int32_t H1);
+/* MLP baseline parameters: Wb0|bb0 [V+1, BH] then Wb1|bb1 [BH+1, 1]. */
+int32_t edg_sbn_baseline_num_params(int32_t V, int32_t BH);
+size_t edg_sbn_workspace_bytes(const edg_sbn_t* cfg, int32_t B);
+/* X [B, V] (0/1 values as floats); prior_logits [H1]; theta [P]; opt_slots [2P];
+ * baseline_params [PB] / baseline_slots [2 PB] (MLP baseline only);
+ * baseline_stats float[8] (running mean, running scale, update count, the
+ * baseline optimizer's beta1 / beta2 powers, last regression loss, 2 unused):
+ * zero-initialise, then set [1] = 1, [3] = beta1, [4] = beta2.
+ * grad_out [P] or NULL; signal_out [2, S*B] (f_sb, then the learning signal
+ * used) or NULL.  apply = 0 leaves theta, slots, state and the baseline alone. */
+int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt, const edg_opt_t* baseline_opt,
+                       const float* X, int32_t B, const float* prior_logits, float* theta,
+                       float* opt_slots, edg_state_t* state, float* baseline_params,
+                       float* baseline_slots, float* baseline_stats, const float* z_override,
+                       float* grad_out, float* signal_out, int32_t apply, void* workspace,
+                       size_t workspace_bytes, void* stream);
+/* uint8 rows (binary images) gathered as in edg_minibatch_gather and widened to float. */
+int edg_minibatch_gather_u8(const uint8_t* X, int64_t N, int32_t V, int32_t B, uint64_t seed,
+                            const edg_state_t* state, float* Xb, void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and

@@ -252,3 +252,48 @@ def test_minibatch_rows_oracle_is_uniform():
     assert rows.min() == 0 and rows.max() == 6
     counts = np.bincount(rows, minlength=7)
     assert np.all(np.abs(counts - 20000 / 7) < 5 * np.sqrt(20000 / 7))
+
+
+# ------------------------------------------------------------- sigmoid belief network
+
+def test_compile_sigmoid_belief_network():
+    from sbn_model import example_sbn
+    from edward_gb300.compile import compile_sbn
+    lv, xr, x_ph, weights = example_sbn(12, 5, 4, 8, prior_logit=0.5)
+    spec = compile_sbn(lv, {xr: x_ph})
+    assert (spec.V, spec.H0, spec.H1, spec.batch) == (12, 5, 4, 8)
+    assert spec.x_node is x_ph and spec.X is None
+    np.testing.assert_array_equal(spec.prior_logits, np.full(4, 0.5, np.float32))
+    assert [id(w) for w in spec.weights] == [id(w) for w in weights]
+    data = (np.random.default_rng(0).random((30, 12)) < 0.5).astype(np.uint8)
+    spec = compile_sbn(lv, {xr: data})
+    assert spec.X.dtype == np.uint8 and spec.X.shape == (30, 12)
+
+
+def test_compile_sbn_rejects_other_networks():
+    from sbn_model import example_sbn
+    from edward_gb300.compile import compile_sbn
+    lv, xr, x_ph, _ = example_sbn(6, 3, 2, 4)
+    (z0, qz0), (z1, qz1) = lv.items()
+    with pytest.raises(UnsupportedModel):      # q(z1) not fed by q(z0)
+        bad = Bernoulli(logits=ed.layers.dense(ed.cast(x_ph), 2))
+        compile_sbn({z0: qz0, z1: bad}, {xr: x_ph})
+    with pytest.raises(UnsupportedModel):      # non-constant top logits
+        z1.logits = ed.layers.dense(ed.cast(x_ph), 2)
+        compile_sbn(lv, {xr: x_ph})
+
+
+def test_sbn_dispatch_on_host():
+    """KLqp on discrete latents wants ScoreRBKLqp (not implemented: says so);
+    ScoreKLqp compiles the network and then needs the GPU."""
+    from sbn_model import example_sbn
+    lv, xr, x_ph, _ = example_sbn(6, 3, 2, 4)
+    with pytest.raises(NotImplementedError, match="ScoreKLqp"):
+        ed.KLqp(lv, data={xr: x_ph}).initialize()
+    inf = ed.ScoreKLqp(lv, data={xr: x_ph})
+    with pytest.raises(ValueError):
+        inf.initialize(baseline="median")
+    inf = ed.ScoreKLqp(lv, data={xr: x_ph})
+    with pytest.raises(RuntimeError):
+        inf.initialize(n_samples=2, baseline="mlp")
+    assert inf._family == "sbn"
