@@ -581,6 +581,112 @@ def run_bnn(args):
     return 0
 
 
+def sbn_data(N=60000, V=784, H0=200, H1=200, seed=0):
+    """Binary rows [N, V] (uint8) from a random sigmoid belief network
+    H1 -> H0 -> V with W ~ N(0, 1) / sqrt(fan_in), zero biases, z1 ~ Bern(1/2)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    W1 = rng.standard_normal((H1, H0)) / np.sqrt(H1)
+    W0 = rng.standard_normal((H0, V)) / np.sqrt(H0)
+    z1 = (rng.random((N, H1)) < 0.5).astype(np.float32)
+    z0 = (rng.random((N, H0)) < 1.0 / (1.0 + np.exp(-(z1 @ W1)))).astype(np.float32)
+    return (rng.random((N, V)) < 1.0 / (1.0 + np.exp(-(z0 @ W0)))).astype(np.uint8)
+
+
+def _sbn_inference(data, B, S, baseline, seed=0):
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli
+    ed.set_seed(seed)
+    V, H0, H1 = data.shape[1], 200, 200
+    x_ph = ed.placeholder(shape=[B, V])
+    z1 = Bernoulli(logits=ed.zeros([B, H1]))
+    z0 = Bernoulli(logits=ed.layers.dense(ed.cast(z1), H0))
+    x = Bernoulli(logits=ed.layers.dense(ed.cast(z0), V))
+    qz0 = Bernoulli(logits=ed.layers.dense(ed.cast(x_ph), H0))
+    qz1 = Bernoulli(logits=ed.layers.dense(ed.cast(qz0), H1))
+    inf = ed.ScoreKLqp({z0: qz0, z1: qz1}, data={x: data})
+    inf.initialize(n_samples=S, n_minibatch=B, baseline=baseline, baseline_hidden=100,
+                   n_print=0, optimizer=ed.train.AdamOptimizer(1e-3))
+    return inf
+
+
+def run_sbn(args):
+    """Sigmoid belief network 784-200-200 under ScoreKLqp with the learned MLP
+    baseline (784 -> 100 -> 1, trained online by its own kernels): S = 16
+    samples, B = 1,024 rows gathered on the device per step from 60,000
+    synthetic binary rows; steps replayed from a CUDA graph.  Also reports
+    the q-gradient variance under each baseline at the trained parameters and
+    the ELBO reached by the running-mean and MLP baselines with equal steps."""
+    import numpy as np
+    import torch
+    V, H0, H1, B, S, BH = 784, 200, 200, 1024, 16, 100
+    data = sbn_data(V=V, H0=H0, H1=H1)
+    inf = _sbn_inference(data, B, S, "mlp")
+    chunk = 10
+    for _ in range(max(1, args.warmup // chunk + 1)):
+        inf.steps(chunk)
+    torch.cuda.synchronize()
+    K = max(args.steps // chunk, 1) * chunk
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        a.record()
+        for _ in range(K // chunk):
+            inf.steps(chunk)
+        b.record()
+        b.synchronize()
+    ms = a.elapsed_time(b) / K
+    R = S * B
+    flops = 4.0 * R * ((H0 + 1) * H1 + (H1 + 1) * H0 + (H0 + 1) * V) + \
+        4.0 * B * (V + 1) * (H0 + BH)
+    peak, src = _peak_3xtf32()
+    ach = flops / (ms / 1e3) / 1e12
+    # gradient variance at the trained parameters, one frozen minibatch
+    inf._sbn.gather = False
+    nq = (V + 1) * H0 + (H0 + 1) * H1
+    gvar = {}
+    for mode, name in ((0, "none"), (1, "mean"), (2, "mlp")):
+        inf._cfg.baseline = mode
+        gs = []
+        for k in range(24):
+            inf.seed = 7000 + k
+            gs.append(inf.score_gradients()[1][:nq].double())
+        gvar[name] = float(torch.stack(gs).var(dim=0).sum())
+    inf._cfg.baseline = 2
+    # ELBO after equal training with the running-mean and the MLP baseline
+    elbo = {}
+    for name in ("mean", "mlp"):
+        run = _sbn_inference(data, B, S, name, seed=1)
+        losses = []
+        for i in range(args.sbn_compare_steps // chunk):
+            run.steps(chunk)
+            if i >= args.sbn_compare_steps // chunk - 10:
+                losses.append(run._read_state().loss)
+        elbo[name] = -float(np.mean(losses)) / B
+    st = inf._read_state()
+    from edward_gb300 import _lib
+    launches = _lib.load().edg_sbn_launches_per_step(inf._cfg, B, 1)
+    line = {"metric": "ScoreKLqp ELBO-grad evals/s (sigmoid belief network 784-200-200, S=16, "
+                      "B=1024, learned MLP baseline)",
+            "value": 1e3 / ms, "unit": "evals/s", "n_gpus": 1, "steps": K,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "sbn_score_V784_H200_H200_S16_B1024_mlp100",
+                       "params": inf._P, "baseline_params": int(inf._bparams.numel()),
+                       "launch": f"CUDA graph of {chunk} steps",
+                       "l2_flush": "inputs larger than L2 (sample-row buffers %.0f MB per step)"
+                                   % (4.0 * R * (V + 3 * H0 + 2 * H1) / 1e6)},
+            "gpu_launches": K * (1 + launches),
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                         "frac": ach / peak, "traffic": None,
+                         "kernel": "whole step (SIMT bgemm + row kernels + baseline)",
+                         "peak_source": src, "algorithmic_flops_per_step": flops},
+            "q_grad_variance": gvar,
+            "elbo_per_row_after_%d_steps" % args.sbn_compare_steps: elbo,
+            "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -592,7 +698,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--hier-instances", type=int, default=2048)
-    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn"],
+    ap.add_argument("--sbn-compare-steps", type=int, default=1000)
+    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -605,6 +712,8 @@ def main():
         return run_klqp(args)
     if args.workload == "bnn":
         return run_bnn(args)
+    if args.workload == "sbn":
+        return run_sbn(args)
     return run_gpu(args)
 
 

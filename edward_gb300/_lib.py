@@ -115,6 +115,7 @@ _SIGS = {
     "edg_sbn_num_params": (c_int32, [c_int32, c_int32, c_int32]),
     "edg_sbn_baseline_num_params": (c_int32, [c_int32, c_int32]),
     "edg_sbn_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgSBN), c_int32]),
+    "edg_sbn_launches_per_step": (c_int32, [ctypes.POINTER(EdgSBN), c_int32, c_int32]),
     "edg_sbn_score_step": (c_int32, [ctypes.POINTER(EdgSBN), ctypes.POINTER(EdgOpt),
                                      ctypes.POINTER(EdgOpt), c_void_p, c_int32, c_void_p,
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

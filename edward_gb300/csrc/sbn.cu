@@ -20,7 +20,7 @@
 //   sample1   z1, log q(z1|z0), log p(z1); Lq1 <- z1 - sigmoid(Lq1)
 //   Lp1       = Z1a Wp1;  rows: log p(z0|z1), Lp1 <- z0 - sigmoid(Lp1)
 //   Lp0       = Z0a Wp0;  rows: log p(x|z0),  Lp0 <- x - sigmoid(Lp0)
-//   [MLP baseline forward  b(x) = c + sigma * (tanh(Xa Wb0) Wb1)]
+//   [MLP baseline forward  b(x) = c + sigma * (tanh(Xc Wb0) Wb1), Xc = [2x - 1, 1]]
 //   signal    f[s,b] = log p(x, z) - log q(z | x);  F_s = sum_b f[s,b]
 //   scale     learning signal A: F_s (no baseline: the reference's
 //             estimator, klqp.py:894-904) or f[s,b] - b(x_b) (per row);
@@ -95,11 +95,16 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// Xa[b] = [x_b, 1, 0...]
-__global__ void prep_x_kernel(Dims d, const float* __restrict__ X, float* __restrict__ Xa) {
+// Xa[b] = [x_b, 1, 0...]; Xc[b] = [2 x_b - 1, 1, 0...] (the MLP baseline's
+// centred input) when Xc != NULL.
+__global__ void prep_x_kernel(Dims d, const float* __restrict__ X, float* __restrict__ Xa,
+                              float* __restrict__ Xc) {
   const int b = blockIdx.x;
-  for (int v = threadIdx.x; v < d.ldx; v += blockDim.x)
-    Xa[(int64_t)b * d.ldx + v] = v < d.V ? X[(int64_t)b * d.V + v] : (v == d.V ? 1.0f : 0.0f);
+  for (int v = threadIdx.x; v < d.ldx; v += blockDim.x) {
+    const float x = v < d.V ? X[(int64_t)b * d.V + v] : 0.0f;
+    Xa[(int64_t)b * d.ldx + v] = v < d.V ? x : (v == d.V ? 1.0f : 0.0f);
+    if (Xc) Xc[(int64_t)b * d.ldx + v] = v < d.V ? 2.0f * x - 1.0f : (v == d.V ? 1.0f : 0.0f);
+  }
 }
 
 // z0 for every (sample, row): warp per sample row r = s B + b.
@@ -172,7 +177,7 @@ __global__ void bern_rows_kernel(int R, int n, const float* __restrict__ T, int 
   if (lane == 0) out[r] = acc;
 }
 
-// MLP baseline output o_b = Hb[b] . w1 + b1 (Hb = tanh(Xa Wb0)); sets Hb's ones column.
+// MLP baseline output o_b = Hb[b] . w1 + b1 (Hb = tanh(Xc Wb0)); sets Hb's ones column.
 __global__ void mlp_out_kernel(Dims d, float* __restrict__ Hb, const float* __restrict__ bp,
                                float* __restrict__ out) {
   const int b = blockIdx.x * (kT / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -455,7 +460,7 @@ __global__ void __launch_bounds__(kT) baseline_apply_kernel(BaseArgs a) {
 }
 
 struct Workspace {
-  float *Xa, *Lq0, *Z0a, *Z1a, *R0, *Lq1, *Lp1, *Lp0, *R0q, *terms, *f, *Hb, *mlp_out, *dout, *dHb,
+  float *Xa, *Xc, *Lq0, *Z0a, *Z1a, *R0, *Lq1, *Lp1, *Lp0, *R0q, *terms, *f, *Hb, *mlp_out, *dout, *dHb,
       *G, *GB, *part;
   double *Fs, *bpart;
   unsigned* counters;
@@ -481,7 +486,7 @@ static size_t carve(const Dims& d, int sms, void* base, Workspace* w) {
   }
   const int nb = (d.B + kT / 32 - 1) / (kT / 32);
   const size_t o[] = {
-      take(B * d.ldx * 4),   take(B * d.H0 * 4), take(R * d.ld0 * 4), take(R * d.ld1 * 4),
+      take(B * d.ldx * 4),   take(mlp ? B * d.ldx * 4 : 0), take(B * d.H0 * 4), take(R * d.ld0 * 4), take(R * d.ld1 * 4),
       take(R * d.H0 * 4),    take(R * d.H1 * 4), take(R * d.H0 * 4),  take(R * d.V * 4),
       take(B * d.H0 * 4),    take(5 * R * 4),    take(R * 4),
       take(mlp ? B * d.ldh * 4 : 0), take(B * 4), take(B * 4), take(mlp ? B * d.BH * 4 : 0),
@@ -489,13 +494,14 @@ static size_t carve(const Dims& d, int sms, void* base, Workspace* w) {
       take(d.S * 8),         take((size_t)nb * 3 * 8), take(64)};
   if (w && base) {
     char* c = reinterpret_cast<char*>(base);
-    float** fp[] = {&w->Xa, &w->Lq0, &w->Z0a, &w->Z1a, &w->R0, &w->Lq1, &w->Lp1, &w->Lp0,
-                    &w->R0q, &w->terms, &w->f, &w->Hb, &w->mlp_out, &w->dout, &w->dHb, &w->G,
-                    &w->GB, &w->part};
-    for (int i = 0; i < 18; ++i) *fp[i] = reinterpret_cast<float*>(c + o[i]);
-    w->Fs = reinterpret_cast<double*>(c + o[18]);
-    w->bpart = reinterpret_cast<double*>(c + o[19]);
-    w->counters = reinterpret_cast<unsigned*>(c + o[20]);
+    float** fp[] = {&w->Xa, &w->Xc, &w->Lq0, &w->Z0a, &w->Z1a, &w->R0, &w->Lq1, &w->Lp1,
+                    &w->Lp0, &w->R0q, &w->terms, &w->f, &w->Hb, &w->mlp_out, &w->dout, &w->dHb,
+                    &w->G, &w->GB, &w->part};
+    constexpr int nf = sizeof(fp) / sizeof(fp[0]);
+    for (int i = 0; i < nf; ++i) *fp[i] = reinterpret_cast<float*>(c + o[i]);
+    w->Fs = reinterpret_cast<double*>(c + o[nf]);
+    w->bpart = reinterpret_cast<double*>(c + o[nf + 1]);
+    w->counters = reinterpret_cast<unsigned*>(c + o[nf + 2]);
   }
   return off;
 }
@@ -549,6 +555,23 @@ extern "C" int32_t edg_sbn_baseline_num_params(int32_t V, int32_t BH) {
   return (int32_t)make_dims(&c, 1).PB;
 }
 
+extern "C" int32_t edg_sbn_launches_per_step(const edg_sbn_t* cfg, int32_t B, int32_t apply) {
+  if (check_cfg(cfg, B) != EDG_OK) return -1;
+  const Dims d = make_dims(cfg, B);
+  const int sms = num_sms();
+  auto tn = [&](int M, int N, int K) { return choose_splits(M, N, K, sms) > 1 ? 2 : 1; };
+  int n = 9 + 2 + 1;  // prep .. bern_rows(x), signal, scale
+  if (d.mode == EDG_BASELINE_MLP) n += 2;
+  n += tn(d.V + 1, d.H0, d.B) + tn(d.H0 + 1, d.H1, d.R) + tn(d.H1 + 1, d.H0, d.R) +
+       tn(d.H0 + 1, d.V, d.R);
+  n += 1;  // finalize
+  if (apply && d.mode != EDG_BASELINE_NONE) {
+    n += 2;
+    if (d.mode == EDG_BASELINE_MLP) n += tn(d.V + 1, d.BH, d.B) + tn(d.BH + 1, 1, d.B);
+  }
+  return n;
+}
+
 extern "C" size_t edg_sbn_workspace_bytes(const edg_sbn_t* cfg, int32_t B) {
   if (check_cfg(cfg, B) != EDG_OK) return 0;
   return carve(make_dims(cfg, B), num_sms(), nullptr, nullptr);
@@ -588,7 +611,7 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
   float* lx = w.terms + 4 * (int64_t)d.R;
   cudaMemsetAsync(w.counters, 0, 64, st);
 
-  prep_x_kernel<<<d.B, 256, 0, st>>>(d, X, w.Xa);
+  prep_x_kernel<<<d.B, 256, 0, st>>>(d, X, w.Xa, mlp ? w.Xc : nullptr);
   if ((rc = check_launch("sbn prep_x_kernel"))) return rc;
   // q(z0 | x) logits, shared by all samples
   rc = simt::bgemm<false, false>(w.Xa, theta + d.oq0, w.Lq0, d.B, d.H0, d.V + 1, d.ldx, d.H0,
@@ -617,7 +640,7 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
   if ((rc = check_launch("sbn bern_rows_kernel"))) return rc;
   // MLP baseline forward (uses parameters from earlier steps only)
   if (mlp) {
-    rc = simt::bgemm<false, false>(w.Xa, baseline_params, w.Hb, d.B, d.BH, d.V + 1, d.ldx, d.BH,
+    rc = simt::bgemm<false, false>(w.Xc, baseline_params, w.Hb, d.B, d.BH, d.V + 1, d.ldx, d.BH,
                                    d.ldh, 0, 0, 0, 1, simt::EpiTanh{}, st);
     if (rc) return rc;
     mlp_out_kernel<<<b_grid, kT, 0, st>>>(d, w.Hb, baseline_params, w.mlp_out);
@@ -665,7 +688,7 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
                                                 baseline_params, w.dout, w.dHb, w.bpart);
     if ((rc = check_launch("sbn baseline_grad_kernel"))) return rc;
     if (mlp) {
-      if ((rc = gemm_tn(w.Xa, d.ldx, w.dHb, d.BH, w.GB, d.BH, d.V + 1, d.BH, d.B, w.part, sms, st)))
+      if ((rc = gemm_tn(w.Xc, d.ldx, w.dHb, d.BH, w.GB, d.BH, d.V + 1, d.BH, d.B, w.part, sms, st)))
         return rc;
       if ((rc = gemm_tn(w.Hb, d.ldh, w.dout, 1, w.GB + d.ob1, 1, d.BH + 1, 1, d.B, w.part, sms,
                         st)))

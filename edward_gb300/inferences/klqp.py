@@ -333,9 +333,9 @@ class ScoreKLqp(KLqp):
     ``baseline`` (sigmoid belief network family): ``None`` / ``"none"`` is the
     reference's estimator (no control variate); ``"mean"`` subtracts a running
     mean of the per-row learning signal; ``"mlp"`` subtracts
-    c + sigma * mlp(x), a ``baseline_hidden``-unit tanh network trained online
+    c + sigma * mlp(2x - 1), a ``baseline_hidden``-unit tanh network trained online
     on the (x, learning signal) pairs the estimator produces, with
-    ``baseline_optimizer`` (default Adam, learning rate 1e-3)."""
+    ``baseline_optimizer`` (default Adam, learning rate 1e-2)."""
     _method = SCORE
 
     def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, baseline=None,
@@ -346,7 +346,7 @@ class ScoreKLqp(KLqp):
         if self.baseline not in ("none", "mean", "mlp"):
             raise ValueError(f"baseline must be None, 'mean' or 'mlp'; got {baseline!r}")
         self.baseline_hidden = int(baseline_hidden)
-        self.baseline_optimizer = (train.AdamOptimizer(1e-3) if baseline_optimizer is None
+        self.baseline_optimizer = (train.AdamOptimizer(1e-2) if baseline_optimizer is None
                                    else train.resolve(baseline_optimizer, None))
         if not 0.0 <= baseline_decay < 1.0:
             raise ValueError("baseline_decay must be in [0, 1)")

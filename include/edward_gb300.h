@@ -258,7 +258,7 @@ int edg_minibatch_gather(const float* X, const float* y, int64_t N, int32_t D, i
  * optimizer apply.  The learning signal is
  *   EDG_BASELINE_NONE: the sample's total F_s = sum_b f_sb (the reference);
  *   EDG_BASELINE_MEAN: f_sb - c per row, c a running mean of f;
- *   EDG_BASELINE_MLP:  f_sb - (c + sigma * mlp(x_b)) per row, mlp a
+ *   EDG_BASELINE_MLP:  f_sb - (c + sigma * mlp(2 x_b - 1)) per row, mlp a
  *       V -> baseline_hidden (tanh) -> 1 network trained online (one optimizer
  *       step per call, on the row targets (mean_s f_sb - c) / sigma).
  * Every variant is unbiased (the baseline depends on x and on earlier steps
@@ -280,6 +280,8 @@ int32_t edg_sbn_num_params(int32_t V, int32_t H0, int32_t H1);
 /* MLP baseline parameters: Wb0|bb0 [V+1, BH] then Wb1|bb1 [BH+1, 1]. */
 int32_t edg_sbn_baseline_num_params(int32_t V, int32_t BH);
 size_t edg_sbn_workspace_bytes(const edg_sbn_t* cfg, int32_t B);
+/* Kernel launches one edg_sbn_score_step call makes (for throughput reports). */
+int32_t edg_sbn_launches_per_step(const edg_sbn_t* cfg, int32_t B, int32_t apply);
 /* X [B, V] (0/1 values as floats); prior_logits [H1]; theta [P]; opt_slots [2P];
  * baseline_params [PB] / baseline_slots [2 PB] (MLP baseline only);
  * baseline_stats float[8] (running mean, running scale, update count, the

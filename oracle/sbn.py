@@ -11,7 +11,8 @@ The gradient is ``build_score_loss_and_gradients`` (``edward/inferences/
 klqp.py:840-906``): loss = -mean_s F_s with F_s = sum_b [log p(x_b, z_sb) -
 log q(z_sb | x_b)]; the q-gradient is -mean_s grad(log q(z_s)) * F_s (the
 learning signal is stop-gradient), the p-gradient is grad(loss).  With a
-baseline the learning signal becomes per row, f_sb - b(x_b).
+baseline the learning signal becomes per row, f_sb - b(x_b), with the learned
+b(x) = c + sigma * mlp(2x - 1) (tanh hidden layer).
 
 Parameters are four [in + 1, out] blocks (bias as the last row):
 Wq0 [V+1, H0], Wq1 [H0+1, H1], Wp1 [H1+1, H0], Wp0 [H0+1, V].
@@ -81,9 +82,10 @@ def sample_z(theta, X, u0, u1, V, H0, H1):
 
 
 def mlp_forward(bparams, X, V, BH):
+    """The baseline network on the centred input 2x - 1: (hidden [B, BH], out [B])."""
     w0 = np.asarray(bparams[:(V + 1) * BH], np.float64).reshape(V + 1, BH)
     w1 = np.asarray(bparams[(V + 1) * BH:], np.float64)
-    Hb = np.tanh(aug(np.asarray(X, np.float64)) @ w0)
+    Hb = np.tanh(aug(2.0 * np.asarray(X, np.float64) - 1.0) @ w0)
     return Hb, Hb @ w1[:BH] + w1[BH]
 
 
@@ -159,7 +161,7 @@ def baseline_update(out, X, stats, bparams, bslots, V, BH, mode, decay, lr, beta
         w1 = bparams[(V + 1) * BH:]
         dw1 = aug(Hb).T @ d
         dHb = d[:, None] * w1[None, :BH] * (1.0 - Hb * Hb)
-        dw0 = aug(np.asarray(X, np.float64)).T @ dHb
+        dw0 = aug(2.0 * np.asarray(X, np.float64) - 1.0).T @ dHb
         g = np.concatenate([dw0.reshape(-1), dw1])
         PB = g.size
         m, v = bslots[:PB], bslots[PB:]

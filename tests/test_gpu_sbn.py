@@ -35,7 +35,8 @@ def _draws(rng, S, B, H0, H1):
             (rng.random((S, B, H1)) < 0.5).astype(np.float32))
 
 
-@pytest.mark.parametrize("V,H0,H1,B,S", [(20, 12, 8, 16, 3), (784, 200, 200, 64, 4)])
+@pytest.mark.parametrize("V,H0,H1,B,S", [(20, 12, 8, 16, 3), (784, 200, 200, 64, 4),
+                                          (50, 20, 10, 512, 4)])
 @pytest.mark.parametrize("baseline", [None, "mean", "mlp"])
 def test_sbn_score_gradient_parity_given_draws(cuda, V, H0, H1, B, S, baseline):
     from sbn_model import flat_theta
@@ -76,12 +77,14 @@ def test_sbn_philox_draws_follow_the_bernoulli_rule(cuda):
     close(g.cpu().numpy(), ref["grad"], 2e-5)
 
 
-def test_sbn_training_steps_with_mlp_baseline_match_oracle(cuda):
+@pytest.mark.parametrize("V,H0,H1,B,S", [(24, 10, 8, 16, 4), (300, 12, 8, 1024, 2)])
+def test_sbn_training_steps_with_mlp_baseline_match_oracle(cuda, V, H0, H1, B, S):
     """Three update() calls: model Adam step + the baseline's own regression
-    step and running statistics, all against the oracle chain."""
+    step and running statistics, all against the oracle chain (the second
+    size runs every gradient GEMM split over the rows)."""
     import edward_gb300 as ed
     from sbn_model import flat_theta
-    V, H0, H1, B, S, BH = 24, 10, 8, 16, 4, 16
+    BH = 16
     inf, x_ph, weights, X, pl = _setup(V, H0, H1, B, S, "mlp",
                                        optimizer=ed.train.AdamOptimizer(1e-3))
     th = flat_theta(weights)
@@ -99,7 +102,7 @@ def test_sbn_training_steps_with_mlp_baseline_match_oracle(cuda):
         info = inf.update(feed_dict={x_ph: X})
         assert abs(info["loss"] - ref["loss"]) <= 1e-5 * abs(ref["loss"])
         th = opt.apply(th, ref["grad"], 1e-3)
-        stats, bp, bsl = sbn.baseline_update(ref, X, stats, bp, bsl, V, BH, sbn.MLP, 0.9, 1e-3)
+        stats, bp, bsl = sbn.baseline_update(ref, X, stats, bp, bsl, V, BH, sbn.MLP, 0.9, 1e-2)
         np.testing.assert_allclose(flat_theta(weights), th, rtol=1e-4, atol=2e-5)
         np.testing.assert_allclose(inf._bparams.cpu().numpy(), bp, rtol=1e-4, atol=2e-5)
         np.testing.assert_allclose(inf._bstats.cpu().numpy()[:6], stats[:6], rtol=2e-5, atol=1e-6)
