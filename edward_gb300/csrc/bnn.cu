@@ -3,15 +3,23 @@
 // out = h2 W2 + b2, y ~ Normal(out, noise); q = N(mu, softplus(rho)) on every
 // weight, prior N(0, prior_scale).
 //
+// The flat parameter layout W0 [D,H1], b0, W1 [H1,H2], b1, W2 [H2,1], b2 puts
+// every bias right after its weight matrix, i.e. each layer is one [in+1, out]
+// block.  Activations carry a trailing ones column, so one GEMM gives a
+// layer's pre-activation and one transposed GEMM gives its weight *and* bias
+// gradient, written straight into the per-sample gradient G[s].
+//
 // One step = one minibatch ELBO gradient + optimizer apply, as a fixed
 // sequence of launches on one stream (graph-capturable):
-//   sample   theta_s = mu + sigma * eps_s (Philox), eps kept for the rho gradient
-//   F1, F2   batched GEMMs with fused bias + tanh epilogues
-//   head     out, residual, log-lik, dW2/db2 and dH2 = dout w2 (1 - h2^2) (in place of h2)
-//   B1       dW1_s = h1_s^T dH2_s          (written straight into the per-sample gradient)
-//   B2       dH1 = (dH2 W1^T)(1 - h1^2)    (in place of h1)
-//   B3       dW0_s = X^T dH1_s
-//   colsums  db1, db0
+//   sample   theta_s = mu + sigma * eps_s (Philox), eps kept for the rho gradient;
+//            Xa = [X, 1] and the ones columns of H1a / H2a
+//   F1, F2   H1a = tanh(Xa W0a), H2a = tanh(H1a W1a)    (batched over samples)
+//   head     out, residual, FP64 log-lik partials, dout = scale (y - out) / noise^2
+//   G2       [dW2; db2] = H2a^T dout
+//   adj2     dH2 = dout w2 (1 - h2^2)                  (in place of h2)
+//   B1       [dW1; db1] = H1a^T dH2
+//   B2       dH1 = (dH2 W1^T)(1 - h1^2)                (in place of h1)
+//   B3       [dW0; db0] = Xa^T dH1
 //   finalize sum over samples, KL, loss, gradients w.r.t. (mu, rho), optimizer
 // Hidden activations exist only for the current minibatch (S x M), are
 // recomputed every step and are overwritten by their adjoints.
@@ -26,7 +34,7 @@ namespace bnn {
 
 constexpr int kT = 256;
 using simt::bgemm;
-using simt::EpiBiasTanh;
+using simt::EpiTanh;
 using simt::EpiIdentity;
 using simt::EpiTanhGrad;
 
@@ -64,78 +72,113 @@ __global__ void sample_kernel(const float* __restrict__ mu, const float* __restr
   theta[i] = mu[p] + softplusf(rho[p]) * e;
 }
 
+// ------------------------------------------------------------ activations
+struct Act {
+  int M, ldx, ld1, ld2;
+};
+
+__host__ __device__ inline Act make_act(const Layout& L, int M) {
+  Act a;
+  a.M = M;
+  a.ldx = round_up(L.D + 1, 4);
+  a.ld1 = round_up(L.H1 + 1, 4);
+  a.ld2 = round_up(L.H2 + 1, 4);
+  return a;
+}
+
+// Xa = [X, 1, 0...]; the ones column (and zero padding) of every row of H1a, H2a.
+__global__ void prep_kernel(Layout L, Act a, int S, const float* __restrict__ X,
+                            float* __restrict__ Xa, float* __restrict__ H1a,
+                            float* __restrict__ H2a) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < (int64_t)a.M * a.ldx; i += nth) {
+    const int m = (int)(i / a.ldx), d = (int)(i % a.ldx);
+    Xa[i] = d < L.D ? X[(int64_t)m * L.D + d] : (d == L.D ? 1.0f : 0.0f);
+  }
+  const int p1 = a.ld1 - L.H1, p2 = a.ld2 - L.H2;
+  for (int64_t i = tid; i < (int64_t)S * a.M * (p1 + p2); i += nth) {
+    const int64_t r = i / (p1 + p2);
+    const int c = (int)(i % (p1 + p2));
+    if (c < p1) H1a[r * a.ld1 + L.H1 + c] = c == 0 ? 1.0f : 0.0f;
+    else H2a[r * a.ld2 + L.H2 + (c - p1)] = c == p1 ? 1.0f : 0.0f;
+  }
+}
+
 // ------------------------------------------------------------ output layer
-// One block per sample: out, residual, FP64 log-lik, dW2, db2 and
-// dH2 = dout * w2 * (1 - h2^2) written over h2.
-__global__ void __launch_bounds__(kT) head_kernel(Layout L, int M, const float* __restrict__ y,
-                                                  const float* __restrict__ theta, float* H2,
-                                                  float* __restrict__ G, double* ll_out,
-                                                  float noise, float dscale) {
-  extern __shared__ __align__(16) float sm[];
-  float* w2 = sm;             // [H2]
-  float* dout = sm + L.H2;    // [M]
+constexpr int kHeadRows = 32;  // rows per block (4 per warp)
+
+// out = h2 . w2 + b2, residual, dout = scale * res / noise^2 and per-block
+// FP64 partial sums of the unscaled log-likelihood; grid (M / kHeadRows, S).
+__global__ void __launch_bounds__(kT) head_kernel(Layout L, Act a, const float* __restrict__ y,
+                                                  const float* __restrict__ theta,
+                                                  const float* __restrict__ H2a,
+                                                  float* __restrict__ dout,
+                                                  double* __restrict__ ll_part, float noise,
+                                                  float dscale) {
   __shared__ double red[kT / 32];
-  const int s = blockIdx.x;
-  const float* th = theta + (int64_t)s * L.P;
-  float* Hs = H2 + (int64_t)s * M * L.H2;
-  for (int k = threadIdx.x; k < L.H2; k += kT) w2[k] = th[L.oW2 + k];
-  __syncthreads();
-  const float b2 = th[L.ob2];
+  const int s = blockIdx.y;
+  const float* w2 = theta + (int64_t)s * L.P + L.oW2;
+  const float b2 = w2[L.H2];
   const float inv_var = 1.0f / (noise * noise);
   const float lnorm = logf(noise) + (float)kHalfLog2Pi;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Kahan kl;
-  for (int m = warp; m < M; m += kT / 32) {
+  double acc = 0.0;
+  for (int i = warp; i < kHeadRows; i += kT / 32) {
+    const int m = blockIdx.x * kHeadRows + i;
+    if (m >= a.M) break;
+    const float* h = H2a + ((int64_t)s * a.M + m) * a.ld2;
     float v = 0.0f;
-    for (int k = lane; k < L.H2; k += 32) v = fmaf(Hs[(int64_t)m * L.H2 + k], w2[k], v);
+    for (int k = lane; k < L.H2; k += 32) v = fmaf(h[k], __ldg(w2 + k), v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const float res = y[m] - (v + b2);
     if (lane == 0) {
-      dout[m] = dscale * res * inv_var;
-      kl.add(-0.5f * res * res * inv_var - lnorm);
+      dout[(int64_t)s * a.M + m] = dscale * res * inv_var;
+      acc += (double)(-0.5f * res * res * inv_var - lnorm);
     }
   }
-  double lls = lane == 0 ? kl.value() : 0.0;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) lls += __shfl_xor_sync(0xffffffffu, lls, o);
-  if (lane == 0) red[warp] = lls;
+  if (lane == 0) red[warp] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < kT / 32; ++w) t += red[w];
-    ll_out[s] = t * (double)dscale;
-  }
-  float* Gs = G + (int64_t)s * L.P;
-  // dW2[k] = sum_m h2[m][k] dout[m]; then h2 <- dH2
-  for (int k = threadIdx.x; k < L.H2; k += kT) {
-    float a = 0.0f;
-    for (int m = 0; m < M; ++m) a = fmaf(Hs[(int64_t)m * L.H2 + k], dout[m], a);
-    Gs[L.oW2 + k] = a;
-  }
-  if (threadIdx.x == 0) {
-    float a = 0.0f;
-    for (int m = 0; m < M; ++m) a += dout[m];
-    Gs[L.ob2] = a;
-  }
-  __syncthreads();
-  for (int64_t e = threadIdx.x; e < (int64_t)M * L.H2; e += kT) {
-    const int m = (int)(e / L.H2), k = (int)(e % L.H2);
-    const float h = Hs[e];
-    Hs[e] = dout[m] * w2[k] * (1.0f - h * h);
+    ll_part[(int64_t)s * gridDim.x + blockIdx.x] = t;
   }
 }
 
-// G[s][off + h] = sum_m Src[s][m][h]
-__global__ void colsum_kernel(const float* __restrict__ Src, int M, int H, int P, int off,
-                              float* __restrict__ G) {
-  const int s = blockIdx.y;
-  const int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= H) return;
-  const float* p = Src + (int64_t)s * M * H + h;
-  float a = 0.0f;
-  for (int m = 0; m < M; ++m) a += p[(int64_t)m * H];
-  G[(int64_t)s * P + off + h] = a;
+// ll[s] = scale * sum of the head partials of sample s.
+__global__ void __launch_bounds__(kT) ll_reduce_kernel(const double* __restrict__ ll_part,
+                                                       int nparts, float dscale,
+                                                       double* __restrict__ ll) {
+  __shared__ double red[kT / 32];
+  const int s = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += kT) acc += ll_part[(int64_t)s * nparts + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w];
+    ll[s] = t * (double)dscale;
+  }
+}
+
+// dH2 = dout * w2 * (1 - h2^2), written over h2 (columns < H2 only).
+__global__ void adj2_kernel(Layout L, Act a, int S, const float* __restrict__ theta,
+                            const float* __restrict__ dout, float* __restrict__ H2a) {
+  const int64_t n = (int64_t)S * a.M * L.H2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / L.H2;
+    const int k = (int)(i % L.H2);
+    const int s = (int)(r / a.M);
+    float* hp = H2a + r * a.ld2 + k;
+    const float h = *hp;
+    *hp = dout[r] * __ldg(theta + (int64_t)s * L.P + L.oW2 + k) * (1.0f - h * h);
+  }
 }
 
 // ------------------------------------------------------------ finalize
@@ -262,9 +305,11 @@ __global__ void gather_kernel(const float* __restrict__ X, const float* __restri
 }
 
 struct Workspace {
-  float *theta, *eps, *G, *H1, *H2;
-  double *ll, *kl_part;
+  float *theta, *eps, *G, *Xa, *H1, *H2, *dout;
+  double *ll, *ll_part, *kl_part;
 };
+
+static int head_blocks(int M) { return (M + kHeadRows - 1) / kHeadRows; }
 
 static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
   size_t off = 0;
@@ -273,18 +318,25 @@ static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
     off += (bytes + 255) / 256 * 256;
     return o;
   };
+  const Act a = make_act(L, M);
   const size_t o_theta = take((size_t)S * L.P * 4), o_eps = take((size_t)S * L.P * 4);
   const size_t o_G = take((size_t)S * L.P * 4);
-  const size_t o_H1 = take((size_t)S * M * L.H1 * 4), o_H2 = take((size_t)S * M * L.H2 * 4);
-  const size_t o_ll = take((size_t)S * 8), o_kl = take((size_t)((L.P + kT - 1) / kT) * 8);
+  const size_t o_Xa = take((size_t)M * a.ldx * 4);
+  const size_t o_H1 = take((size_t)S * M * a.ld1 * 4), o_H2 = take((size_t)S * M * a.ld2 * 4);
+  const size_t o_dout = take((size_t)S * M * 4);
+  const size_t o_ll = take((size_t)S * 8), o_llp = take((size_t)S * head_blocks(M) * 8);
+  const size_t o_kl = take((size_t)((L.P + kT - 1) / kT) * 8);
   if (w && base) {
     char* b = reinterpret_cast<char*>(base);
     w->theta = reinterpret_cast<float*>(b + o_theta);
     w->eps = reinterpret_cast<float*>(b + o_eps);
     w->G = reinterpret_cast<float*>(b + o_G);
+    w->Xa = reinterpret_cast<float*>(b + o_Xa);
     w->H1 = reinterpret_cast<float*>(b + o_H1);
     w->H2 = reinterpret_cast<float*>(b + o_H2);
+    w->dout = reinterpret_cast<float*>(b + o_dout);
     w->ll = reinterpret_cast<double*>(b + o_ll);
+    w->ll_part = reinterpret_cast<double*>(b + o_llp);
     w->kl_part = reinterpret_cast<double*>(b + o_kl);
   }
   return off;
@@ -292,48 +344,50 @@ static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
 
 // Per-sample scaled log-likelihood ll[s] (FP64) and its gradient G[s] w.r.t.
 // theta[s] for S weight samples over one minibatch: the batched forward pass
-// and the hand-written adjoint.  H1 / H2 [S, M, H] hold the activations and
-// are overwritten by their adjoints.
+// and the hand-written adjoint.
 static int loglik_grad(const Layout& L, int S, int M, const float* X, const float* y,
-                       const float* theta, float* H1, float* H2, float* G, double* ll,
+                       const float* theta, const Workspace& w, float* G, double* ll,
                        float noise, float dscale, cudaStream_t st) {
   int rc;
-  // F1: H1 = tanh(X W0 + b0)
-  rc = bgemm<false, false>(X, theta + L.oW0, H1, M, L.H1, L.D, L.D, L.H1, L.H1, 0, L.P,
-                           (int64_t)M * L.H1, S, EpiBiasTanh{theta + L.ob0, L.P}, st);
+  const Act a = make_act(L, M);
+  const int64_t s1 = (int64_t)M * a.ld1, s2 = (int64_t)M * a.ld2;
+  prep_kernel<<<std::min<int64_t>(((int64_t)S * M + 255) / 256, 4096), 256, 0, st>>>(
+      L, a, S, X, w.Xa, w.H1, w.H2);
+  if ((rc = check_launch("bnn prep_kernel"))) return rc;
+  // F1: H1a = tanh(Xa W0a)
+  rc = bgemm<false, false>(w.Xa, theta + L.oW0, w.H1, M, L.H1, L.D + 1, a.ldx, L.H1, a.ld1, 0,
+                           L.P, s1, S, EpiTanh{}, st);
   if (rc) return rc;
-  // F2: H2 = tanh(H1 W1 + b1)
-  rc = bgemm<false, false>(H1, theta + L.oW1, H2, M, L.H2, L.H1, L.H1, L.H2, L.H2,
-                           (int64_t)M * L.H1, L.P, (int64_t)M * L.H2, S,
-                           EpiBiasTanh{theta + L.ob1, L.P}, st);
+  // F2: H2a = tanh(H1a W1a)
+  rc = bgemm<false, false>(w.H1, theta + L.oW1, w.H2, M, L.H2, L.H1 + 1, a.ld1, L.H2, a.ld2, s1,
+                           L.P, s2, S, EpiTanh{}, st);
   if (rc) return rc;
-  // head: out, ll, dW2, db2, dH2 (over H2)
-  const size_t hsm = (size_t)(L.H2 + M) * 4;
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  EDG_REQUIRE((int)hsm <= optin, EDG_E_UNSUPPORTED, "minibatch of %d rows too large", M);
-  cudaFuncSetAttribute(head_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
-  head_kernel<<<S, kT, hsm, st>>>(L, M, y, theta, H2, G, ll, noise, dscale);
+  const int hb = head_blocks(M);
+  head_kernel<<<dim3(hb, S), kT, 0, st>>>(L, a, y, theta, w.H2, w.dout, w.ll_part, noise, dscale);
   if ((rc = check_launch("bnn head_kernel"))) return rc;
-  // B1: dW1 = H1^T dH2  -> G[:, oW1]
-  rc = bgemm<true, false>(H1, H2, G + L.oW1, L.H1, L.H2, M, L.H1, L.H2, L.H2,
-                          (int64_t)M * L.H1, (int64_t)M * L.H2, L.P, S, EpiIdentity{}, st);
+  ll_reduce_kernel<<<S, kT, 0, st>>>(w.ll_part, hb, dscale, ll);
+  if ((rc = check_launch("bnn ll_reduce_kernel"))) return rc;
+  // G2: [dW2; db2] = H2a^T dout
+  rc = bgemm<true, false>(w.H2, w.dout, G + L.oW2, L.H2 + 1, 1, M, a.ld2, 1, 1, s2, M, L.P, S,
+                          EpiIdentity{}, st);
   if (rc) return rc;
-  colsum_kernel<<<dim3((L.H2 + 127) / 128, S), 128, 0, st>>>(H2, M, L.H2, L.P, L.ob1, G);
-  if ((rc = check_launch("bnn colsum"))) return rc;
-  // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of H1
-  rc = bgemm<false, true>(H2, theta + L.oW1, H1, M, L.H1, L.H2, L.H2, L.H2, L.H1,
-                          (int64_t)M * L.H2, L.P, (int64_t)M * L.H1, S,
-                          EpiTanhGrad{H1, (int64_t)M * L.H1, L.H1}, st);
+  {
+    const int64_t n = (int64_t)S * M * L.H2;
+    adj2_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 8192), 256, 0, st>>>(
+        L, a, S, theta, w.dout, w.H2);
+    if ((rc = check_launch("bnn adj2_kernel"))) return rc;
+  }
+  // B1: [dW1; db1] = H1a^T dH2
+  rc = bgemm<true, false>(w.H1, w.H2, G + L.oW1, L.H1 + 1, L.H2, M, a.ld1, a.ld2, L.H2, s1, s2,
+                          L.P, S, EpiIdentity{}, st);
   if (rc) return rc;
-  // B3: dW0 = X^T dH1 -> G[:, oW0]
-  rc = bgemm<true, false>(X, H1, G + L.oW0, L.D, L.H1, M, L.D, L.H1, L.H1, 0,
-                          (int64_t)M * L.H1, L.P, S, EpiIdentity{}, st);
+  // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of h1
+  rc = bgemm<false, true>(w.H2, theta + L.oW1, w.H1, M, L.H1, L.H2, a.ld2, L.H2, a.ld1, s2, L.P,
+                          s1, S, EpiTanhGrad{w.H1, s1, a.ld1}, st);
   if (rc) return rc;
-  colsum_kernel<<<dim3((L.H1 + 127) / 128, S), 128, 0, st>>>(H1, M, L.H1, L.P, L.ob0, G);
-  if ((rc = check_launch("bnn colsum"))) return rc;
-  return EDG_OK;
+  // B3: [dW0; db0] = Xa^T dH1
+  return bgemm<true, false>(w.Xa, w.H1, G + L.oW0, L.D + 1, L.H1, M, a.ldx, a.ld1, L.H1, 0, s1,
+                            L.P, S, EpiIdentity{}, st);
 }
 
 static int check_cfg(const edg_bnn_t* c, int M) {
@@ -398,8 +452,7 @@ extern "C" int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, con
   sample_kernel<<<(unsigned)((SP + 255) / 256), 256, 0, st>>>(mu, rho, L.P, S, cfg->seed, state,
                                                                eps_override, w.theta, w.eps);
   if ((rc = check_launch("bnn sample_kernel"))) return rc;
-  rc = loglik_grad(L, S, M, X, y, w.theta, w.H1, w.H2, w.G, w.ll, cfg->noise, cfg->data_scale,
-                   st);
+  rc = loglik_grad(L, S, M, X, y, w.theta, w, w.G, w.ll, cfg->noise, cfg->data_scale, st);
   if (rc) return rc;
   FinArgs f;
   f.P = L.P;
@@ -434,6 +487,6 @@ extern "C" int edg_bnn_loglik_grad(const edg_bnn_t* cfg, const float* X, const f
   const size_t need = carve(L, cfg->n_samples, M, workspace, &w);
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
-  return loglik_grad(L, cfg->n_samples, M, X, y, theta, w.H1, w.H2, grad_out, ll_out, cfg->noise,
+  return loglik_grad(L, cfg->n_samples, M, X, y, theta, w, grad_out, ll_out, cfg->noise,
                      cfg->data_scale, (cudaStream_t)stream);
 }
