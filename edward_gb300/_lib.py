@@ -28,6 +28,7 @@ EDG_E_NONFINITE, EDG_E_TIMEOUT, EDG_E_UNSUPPORTED, EDG_E_WORKSPACE = -5, -6, -7,
 LIK_BERNOULLI, LIK_NORMAL = 0, 1
 KLQP_REPARAM_KL, KLQP_REPARAM, KLQP_SCORE = 0, 1, 2
 BASELINE_NONE, BASELINE_MEAN, BASELINE_MLP = 0, 1, 2
+GEMM_TC, GEMM_SIMT = 0, 1
 OPT_ADAM, OPT_SGD, OPT_MOMENTUM, OPT_ADAGRAD, OPT_RMSPROP, OPT_ADADELTA = range(6)
 
 
@@ -64,13 +65,13 @@ class EdgHier(ctypes.Structure):
 class EdgBNN(ctypes.Structure):
     _fields_ = [("D", c_int32), ("H1", c_int32), ("H2", c_int32), ("n_samples", c_int32),
                 ("noise", c_float), ("prior_scale", c_float), ("data_scale", c_float),
-                ("method", c_int32), ("seed", c_uint64)]
+                ("method", c_int32), ("gemm_engine", c_int32), ("seed", c_uint64)]
 
 
 class EdgSBN(ctypes.Structure):
     _fields_ = [("V", c_int32), ("H0", c_int32), ("H1", c_int32), ("n_samples", c_int32),
                 ("baseline", c_int32), ("baseline_hidden", c_int32), ("baseline_decay", c_float),
-                ("reserved", c_float), ("seed", c_uint64)]
+                ("gemm_engine", c_int32), ("seed", c_uint64)]
 
 
 class EdgHMC(ctypes.Structure):
@@ -103,6 +104,10 @@ _SIGS = {
                                    c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
                                    c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p]),
+    "edg_gemm_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32]),
+    "edg_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32,
+                           c_int64, c_void_p, c_int32, c_int64, c_void_p, c_int32, c_int64, c_int32,
+                           c_int32, c_void_p, c_size_t, c_void_p]),
     "edg_bnn_num_params": (c_int32, [c_int32, c_int32, c_int32]),
     "edg_bnn_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgBNN), c_int32]),
     "edg_bnn_klqp_step": (c_int32, [ctypes.POINTER(EdgBNN), ctypes.POINTER(EdgOpt), c_void_p,

@@ -27,6 +27,7 @@
 
 #include "edg_common.cuh"
 #include "gemm_simt.cuh"
+#include "gemm_tc.cuh"
 #include "optim.cuh"
 
 namespace edg {
@@ -59,8 +60,10 @@ __host__ __device__ inline Layout make_layout(int D, int H1, int H2) {
   return L;
 }
 
+// theta[s][p] = mu[p] + softplus(rho[p]) eps[s][p]; the rows of theta / eps are
+// ps >= P floats apart (16-byte aligned rows for the tensor-core loads).
 __global__ void sample_kernel(const float* __restrict__ mu, const float* __restrict__ rho, int P,
-                              int S, uint64_t seed, const edg_state_t* state,
+                              int ps, int S, uint64_t seed, const edg_state_t* state,
                               const float* __restrict__ eps_ovr, float* __restrict__ theta,
                               float* __restrict__ eps) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -68,18 +71,20 @@ __global__ void sample_kernel(const float* __restrict__ mu, const float* __restr
   const int s = (int)(i / P), p = (int)(i % P);
   const uint32_t iter = (uint32_t)state->t;
   const float e = eps_ovr ? eps_ovr[i] : philox_normal(seed, 0u, iter, (uint32_t)s, (uint32_t)p);
-  eps[i] = e;
-  theta[i] = mu[p] + softplusf(rho[p]) * e;
+  eps[(int64_t)s * ps + p] = e;
+  theta[(int64_t)s * ps + p] = mu[p] + softplusf(rho[p]) * e;
 }
 
 // ------------------------------------------------------------ activations
 struct Act {
   int M, ldx, ld1, ld2;
+  int ps;  // floats between the parameter rows of consecutive samples (theta, G)
 };
 
-__host__ __device__ inline Act make_act(const Layout& L, int M) {
+__host__ __device__ inline Act make_act(const Layout& L, int M, int ps) {
   Act a;
   a.M = M;
+  a.ps = ps;
   a.ldx = round_up(L.D + 1, 4);
   a.ld1 = round_up(L.H1 + 1, 4);
   a.ld2 = round_up(L.H2 + 1, 4);
@@ -118,7 +123,7 @@ __global__ void __launch_bounds__(kT) head_kernel(Layout L, Act a, const float* 
                                                   float dscale) {
   __shared__ double red[kT / 32];
   const int s = blockIdx.y;
-  const float* w2 = theta + (int64_t)s * L.P + L.oW2;
+  const float* w2 = theta + (int64_t)s * a.ps + L.oW2;
   const float b2 = w2[L.H2];
   const float inv_var = 1.0f / (noise * noise);
   const float lnorm = logf(noise) + (float)kHalfLog2Pi;
@@ -177,13 +182,13 @@ __global__ void adj2_kernel(Layout L, Act a, int S, const float* __restrict__ th
     const int s = (int)(r / a.M);
     float* hp = H2a + r * a.ld2 + k;
     const float h = *hp;
-    *hp = dout[r] * __ldg(theta + (int64_t)s * L.P + L.oW2 + k) * (1.0f - h * h);
+    *hp = dout[r] * __ldg(theta + (int64_t)s * a.ps + L.oW2 + k) * (1.0f - h * h);
   }
 }
 
 // ------------------------------------------------------------ finalize
 struct FinArgs {
-  int P, S;
+  int P, S, ps;
   float prior_scale;
   edg_opt_t opt;
   float* mu;
@@ -212,9 +217,9 @@ __global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
     const float sg = softplusf(rho);
     float sg_mu = 0.0f, sg_sig = 0.0f;
     for (int s = 0; s < a.S; ++s) {
-      const float g = a.G[(int64_t)s * a.P + p];
+      const float g = a.G[(int64_t)s * a.ps + p];
       sg_mu += g;
-      sg_sig += g * a.eps[(int64_t)s * a.P + p];
+      sg_sig += g * a.eps[(int64_t)s * a.ps + p];
     }
     const float invS = 1.0f / (float)a.S;
     const float ps = a.prior_scale;
@@ -231,8 +236,8 @@ __global__ void __launch_bounds__(kT) finalize_kernel(FinArgs a) {
       float zz = 0.0f, zze = 0.0f;
       double lqp = 0.0;
       for (int s = 0; s < a.S; ++s) {
-        const float e = a.eps[(int64_t)s * a.P + p];
-        const float z = a.theta[(int64_t)s * a.P + p];
+        const float e = a.eps[(int64_t)s * a.ps + p];
+        const float z = a.theta[(int64_t)s * a.ps + p];
         zz += z;
         zze += z * e;
         lqp += 0.5 * ((double)(z / ps) * (z / ps) - (double)e * e);
@@ -305,22 +310,34 @@ __global__ void gather_kernel(const float* __restrict__ X, const float* __restri
 }
 
 struct Workspace {
-  float *theta, *eps, *G, *Xa, *H1, *H2, *dout;
+  float *theta, *eps, *G, *Xa, *H1, *H2, *dout, *part;
   double *ll, *ll_part, *kl_part;
 };
 
 static int head_blocks(int M) { return (M + kHeadRows - 1) / kHeadRows; }
 
-static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
+constexpr int kTcChunk = 1024;  // rows per K split of the weight-gradient GEMMs
+
+static int param_stride(const Layout& L) { return round_up(L.P, 4); }
+
+static size_t part_floats(const Layout& L, int S, int M, int engine) {
+  if (engine != EDG_GEMM_TC) return 0;
+  return std::max(tcg::part_floats(L.H1 + 1, L.H2, M, S, kTcChunk),
+                  tcg::part_floats(L.D + 1, L.H1, M, S, kTcChunk));
+}
+
+static size_t carve(const Layout& L, int S, int M, int engine, void* base, Workspace* w) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
     off += (bytes + 255) / 256 * 256;
     return o;
   };
-  const Act a = make_act(L, M);
-  const size_t o_theta = take((size_t)S * L.P * 4), o_eps = take((size_t)S * L.P * 4);
-  const size_t o_G = take((size_t)S * L.P * 4);
+  const int ps = param_stride(L);
+  const Act a = make_act(L, M, ps);
+  const size_t o_theta = take((size_t)S * ps * 4), o_eps = take((size_t)S * ps * 4);
+  const size_t o_G = take((size_t)S * ps * 4);
+  const size_t o_part = take(part_floats(L, S, M, engine) * 4);
   const size_t o_Xa = take((size_t)M * a.ldx * 4);
   const size_t o_H1 = take((size_t)S * M * a.ld1 * 4), o_H2 = take((size_t)S * M * a.ld2 * 4);
   const size_t o_dout = take((size_t)S * M * 4);
@@ -335,6 +352,7 @@ static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
     w->H1 = reinterpret_cast<float*>(b + o_H1);
     w->H2 = reinterpret_cast<float*>(b + o_H2);
     w->dout = reinterpret_cast<float*>(b + o_dout);
+    w->part = reinterpret_cast<float*>(b + o_part);
     w->ll = reinterpret_cast<double*>(b + o_ll);
     w->ll_part = reinterpret_cast<double*>(b + o_llp);
     w->kl_part = reinterpret_cast<double*>(b + o_kl);
@@ -342,25 +360,37 @@ static size_t carve(const Layout& L, int S, int M, void* base, Workspace* w) {
   return off;
 }
 
+// One GEMM on the selected engine: tcgen05 (3xTF32, reductions over the
+// minibatch rows split into kTcChunk-row chunks) or SIMT FP32.
+template <bool TA, bool TB, class Epi>
+static int gemm_on(int engine, const float* A, const float* B, float* C, int M, int N, int K,
+                   int lda, int ldb, int ldc, int64_t sA, int64_t sB, int64_t sC, int batch,
+                   Epi epi, float* part, unsigned* err, cudaStream_t st) {
+  if (engine == EDG_GEMM_TC && N >= 16)
+    return tcg::gemm<TA, TB>(A, B, C, M, N, K, lda, ldb, ldc, sA, sB, sC, batch, epi,
+                             TA ? kTcChunk : 0, part, err, st);
+  return bgemm<TA, TB>(A, B, C, M, N, K, lda, ldb, ldc, sA, sB, sC, batch, epi, st);
+}
+
 // Per-sample scaled log-likelihood ll[s] (FP64) and its gradient G[s] w.r.t.
 // theta[s] for S weight samples over one minibatch: the batched forward pass
-// and the hand-written adjoint.
-static int loglik_grad(const Layout& L, int S, int M, const float* X, const float* y,
-                       const float* theta, const Workspace& w, float* G, double* ll,
-                       float noise, float dscale, cudaStream_t st) {
+// and the hand-written adjoint.  theta / G rows are ps floats apart.
+static int loglik_grad(const Layout& L, int S, int M, int ps, int engine, const float* X,
+                       const float* y, const float* theta, const Workspace& w, float* G,
+                       double* ll, float noise, float dscale, unsigned* err, cudaStream_t st) {
   int rc;
-  const Act a = make_act(L, M);
+  const Act a = make_act(L, M, ps);
   const int64_t s1 = (int64_t)M * a.ld1, s2 = (int64_t)M * a.ld2;
   prep_kernel<<<std::min<int64_t>(((int64_t)S * M + 255) / 256, 4096), 256, 0, st>>>(
       L, a, S, X, w.Xa, w.H1, w.H2);
   if ((rc = check_launch("bnn prep_kernel"))) return rc;
   // F1: H1a = tanh(Xa W0a)
-  rc = bgemm<false, false>(w.Xa, theta + L.oW0, w.H1, M, L.H1, L.D + 1, a.ldx, L.H1, a.ld1, 0,
-                           L.P, s1, S, EpiTanh{}, st);
+  rc = gemm_on<false, false>(engine, w.Xa, theta + L.oW0, w.H1, M, L.H1, L.D + 1, a.ldx, L.H1,
+                             a.ld1, 0, ps, s1, S, EpiTanh{}, w.part, err, st);
   if (rc) return rc;
   // F2: H2a = tanh(H1a W1a)
-  rc = bgemm<false, false>(w.H1, theta + L.oW1, w.H2, M, L.H2, L.H1 + 1, a.ld1, L.H2, a.ld2, s1,
-                           L.P, s2, S, EpiTanh{}, st);
+  rc = gemm_on<false, false>(engine, w.H1, theta + L.oW1, w.H2, M, L.H2, L.H1 + 1, a.ld1, L.H2,
+                             a.ld2, s1, ps, s2, S, EpiTanh{}, w.part, err, st);
   if (rc) return rc;
   const int hb = head_blocks(M);
   head_kernel<<<dim3(hb, S), kT, 0, st>>>(L, a, y, theta, w.H2, w.dout, w.ll_part, noise, dscale);
@@ -368,7 +398,7 @@ static int loglik_grad(const Layout& L, int S, int M, const float* X, const floa
   ll_reduce_kernel<<<S, kT, 0, st>>>(w.ll_part, hb, dscale, ll);
   if ((rc = check_launch("bnn ll_reduce_kernel"))) return rc;
   // G2: [dW2; db2] = H2a^T dout
-  rc = bgemm<true, false>(w.H2, w.dout, G + L.oW2, L.H2 + 1, 1, M, a.ld2, 1, 1, s2, M, L.P, S,
+  rc = bgemm<true, false>(w.H2, w.dout, G + L.oW2, L.H2 + 1, 1, M, a.ld2, 1, 1, s2, M, ps, S,
                           EpiIdentity{}, st);
   if (rc) return rc;
   {
@@ -378,16 +408,16 @@ static int loglik_grad(const Layout& L, int S, int M, const float* X, const floa
     if ((rc = check_launch("bnn adj2_kernel"))) return rc;
   }
   // B1: [dW1; db1] = H1a^T dH2
-  rc = bgemm<true, false>(w.H1, w.H2, G + L.oW1, L.H1 + 1, L.H2, M, a.ld1, a.ld2, L.H2, s1, s2,
-                          L.P, S, EpiIdentity{}, st);
+  rc = gemm_on<true, false>(engine, w.H1, w.H2, G + L.oW1, L.H1 + 1, L.H2, M, a.ld1, a.ld2, L.H2,
+                            s1, s2, ps, S, EpiIdentity{}, w.part, err, st);
   if (rc) return rc;
   // B2: dH1 = (dH2 W1^T)(1 - h1^2), in place of h1
-  rc = bgemm<false, true>(w.H2, theta + L.oW1, w.H1, M, L.H1, L.H2, a.ld2, L.H2, a.ld1, s2, L.P,
-                          s1, S, EpiTanhGrad{w.H1, s1, a.ld1}, st);
+  rc = gemm_on<false, true>(engine, w.H2, theta + L.oW1, w.H1, M, L.H1, L.H2, a.ld2, L.H2, a.ld1,
+                            s2, ps, s1, S, EpiTanhGrad{w.H1, s1, a.ld1}, w.part, err, st);
   if (rc) return rc;
   // B3: [dW0; db0] = Xa^T dH1
-  return bgemm<true, false>(w.Xa, w.H1, G + L.oW0, L.D + 1, L.H1, M, a.ldx, a.ld1, L.H1, 0, s1,
-                            L.P, S, EpiIdentity{}, st);
+  return gemm_on<true, false>(engine, w.Xa, w.H1, G + L.oW0, L.D + 1, L.H1, M, a.ldx, a.ld1, L.H1,
+                              0, s1, ps, S, EpiIdentity{}, w.part, err, st);
 }
 
 static int check_cfg(const edg_bnn_t* c, int M) {
@@ -398,6 +428,8 @@ static int check_cfg(const edg_bnn_t* c, int M) {
               c->n_samples);
   EDG_REQUIRE(c->noise > 0 && c->prior_scale > 0, EDG_E_VALUE,
               "noise and prior_scale must be positive");
+  EDG_REQUIRE(c->gemm_engine == EDG_GEMM_TC || c->gemm_engine == EDG_GEMM_SIMT, EDG_E_VALUE,
+              "unknown gemm_engine %d", c->gemm_engine);
   EDG_REQUIRE(c->method == EDG_KLQP_REPARAM_KL || c->method == EDG_KLQP_REPARAM, EDG_E_UNSUPPORTED,
               "method %d: the Bayesian NN step implements the reparameterisation gradient "
               "with analytic or Monte Carlo KL", c->method);
@@ -420,7 +452,7 @@ extern "C" int32_t edg_bnn_num_params(int32_t D, int32_t H1, int32_t H2) {
 extern "C" size_t edg_bnn_workspace_bytes(const edg_bnn_t* cfg, int32_t M) {
   if (check_cfg(cfg, M) != EDG_OK) return 0;
   const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
-  return carve(L, cfg->n_samples, M, nullptr, nullptr);
+  return carve(L, cfg->n_samples, M, cfg->gemm_engine, nullptr, nullptr);
 }
 
 extern "C" int edg_minibatch_gather(const float* X, const float* y, int64_t N, int32_t D,
@@ -444,18 +476,21 @@ extern "C" int edg_bnn_klqp_step(const edg_bnn_t* cfg, const edg_opt_t* opt, con
   const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
   const int S = cfg->n_samples;
   Workspace w;
-  const size_t need = carve(L, S, M, workspace, &w);
+  const size_t need = carve(L, S, M, cfg->gemm_engine, workspace, &w);
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
   cudaStream_t st = (cudaStream_t)stream;
+  const int ps = param_stride(L);
   const int64_t SP = (int64_t)S * L.P;
-  sample_kernel<<<(unsigned)((SP + 255) / 256), 256, 0, st>>>(mu, rho, L.P, S, cfg->seed, state,
-                                                               eps_override, w.theta, w.eps);
+  sample_kernel<<<(unsigned)((SP + 255) / 256), 256, 0, st>>>(mu, rho, L.P, ps, S, cfg->seed,
+                                                               state, eps_override, w.theta, w.eps);
   if ((rc = check_launch("bnn sample_kernel"))) return rc;
-  rc = loglik_grad(L, S, M, X, y, w.theta, w, w.G, w.ll, cfg->noise, cfg->data_scale, st);
+  rc = loglik_grad(L, S, M, ps, cfg->gemm_engine, X, y, w.theta, w, w.G, w.ll, cfg->noise,
+                   cfg->data_scale, &state->error, st);
   if (rc) return rc;
   FinArgs f;
   f.P = L.P;
+  f.ps = ps;
   f.S = S;
   f.prior_scale = cfg->prior_scale;
   f.opt = *opt;
@@ -484,9 +519,10 @@ extern "C" int edg_bnn_loglik_grad(const edg_bnn_t* cfg, const float* X, const f
   EDG_REQUIRE(X && y && theta && ll_out && grad_out, EDG_E_NULL, "pointers must not be NULL");
   const Layout L = make_layout(cfg->D, cfg->H1, cfg->H2);
   Workspace w;
-  const size_t need = carve(L, cfg->n_samples, M, workspace, &w);
+  const size_t need = carve(L, cfg->n_samples, M, cfg->gemm_engine, workspace, &w);
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
-  return loglik_grad(L, cfg->n_samples, M, X, y, theta, w, grad_out, ll_out, cfg->noise,
-                     cfg->data_scale, (cudaStream_t)stream);
+  // caller layout: theta / grad_out rows are P floats apart
+  return loglik_grad(L, cfg->n_samples, M, L.P, cfg->gemm_engine, X, y, theta, w, grad_out,
+                     ll_out, cfg->noise, cfg->data_scale, nullptr, (cudaStream_t)stream);
 }

@@ -238,11 +238,12 @@ class BNNDevice:
         return self.Xb, self.yb
 
 
-def bnn_config(D, H1, H2, n_samples, noise, prior_scale=1.0, data_scale=1.0, method=0, seed=0):
+def bnn_config(D, H1, H2, n_samples, noise, prior_scale=1.0, data_scale=1.0, method=0, seed=0,
+               engine=0):
     cfg = _lib.EdgBNN()
     cfg.D, cfg.H1, cfg.H2, cfg.n_samples = D, H1, H2, n_samples
     cfg.noise, cfg.prior_scale, cfg.data_scale = noise, prior_scale, data_scale
-    cfg.method, cfg.seed = method, seed
+    cfg.method, cfg.seed, cfg.gemm_engine = method, seed, engine
     return cfg
 
 
@@ -253,7 +254,7 @@ def bnn_loglik_grad(cfg, X, y, theta):
     S, P = theta.shape
     if S != cfg.n_samples:
         cfg = bnn_config(cfg.D, cfg.H1, cfg.H2, S, cfg.noise, cfg.prior_scale, cfg.data_scale,
-                         cfg.method, cfg.seed)
+                         cfg.method, cfg.seed, cfg.gemm_engine)
     lib = _lib.load()
     M = X.shape[0]
     if P != lib.edg_bnn_num_params(cfg.D, cfg.H1, cfg.H2):
@@ -343,3 +344,19 @@ class SBNDevice:
             _lib.call("edg_minibatch_gather_u8", _lib.ptr(self.X_u8), self.N, self.spec.V, self.B,
                       int(self.seed), _lib.ptr(state), _lib.ptr(self.Xb), _lib.stream_ptr())
         return self.Xb
+
+
+def gemm(A, B, M, N, K, ta=False, tb=False, lda=None, ldb=None, batch=1, sA=0, sB=0,
+         engine="tc", kchunk=0):
+    """C[b] = op(A[b]) op(B[b]) through ``edg_gemm`` (FP32 tensors on the GPU,
+    flat or shaped; strides in elements).  Returns C [batch, M, N]."""
+    lda = lda if lda is not None else (M if ta else K)
+    ldb = ldb if ldb is not None else (K if tb else N)
+    eng = {"tc": _lib.GEMM_TC, "simt": _lib.GEMM_SIMT}[engine]
+    C = torch.empty(batch, M, N, dtype=torch.float32, device=A.device)
+    lib = _lib.load()
+    wsb = lib.edg_gemm_workspace_bytes(eng, M, N, K, batch, kchunk)
+    ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=A.device)
+    _lib.call("edg_gemm", eng, int(ta), int(tb), M, N, K, _lib.ptr(A), lda, sA, _lib.ptr(B), ldb,
+              sB, _lib.ptr(C), N, M * N, batch, kchunk, _lib.ptr(ws), wsb, _lib.stream_ptr())
+    return C

@@ -201,6 +201,22 @@ int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg, const edg_o
                       const float* eps_override, float* grad_out, int32_t apply,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------- batched GEMM
+ * C[b] = op(A[b]) op(B[b]) in FP32, the building block of the network steps:
+ * op(A)(m, k) = A[b*sA + m*lda + k] (A[b*sA + k*lda + m] when ta),
+ * op(B)(k, n) = B[b*sB + k*ldb + n] (B[b*sB + n*ldb + k] when tb).
+ * EDG_GEMM_TC: tcgen05 tensor cores with 3xTF32 (operands split hi/lo in
+ * flight, FP32 accumulation); kchunk > 0 splits K into chunks of kchunk rows
+ * summed in FP32 (workspace: edg_gemm_workspace_bytes).  EDG_GEMM_SIMT: FP32
+ * CUDA cores. */
+enum { EDG_GEMM_TC = 0, EDG_GEMM_SIMT = 1 };
+size_t edg_gemm_workspace_bytes(int32_t engine, int32_t M, int32_t N, int32_t K, int32_t batch,
+                                int32_t kchunk);
+int edg_gemm(int32_t engine, int32_t ta, int32_t tb, int32_t M, int32_t N, int32_t K,
+             const float* A, int32_t lda, int64_t sA, const float* B, int32_t ldb, int64_t sB,
+             float* C, int32_t ldc, int64_t sC, int32_t batch, int32_t kchunk, void* workspace,
+             size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------- Bayesian NN
  * KLqp for the regression network h1 = tanh(X W0 + b0), h2 = tanh(h1 W1 + b1),
  * out = h2 W2 + b2, y ~ Normal(out, noise), every weight ~ Normal(0, prior_scale),
@@ -219,6 +235,7 @@ typedef struct {
   float data_scale;      /* minibatch scale N / M (Inference.scale[y]) */
   int32_t method;        /* EDG_KLQP_REPARAM_KL (analytic KL) or EDG_KLQP_REPARAM (Monte Carlo
                             KL, build_reparam_loss_and_gradients, klqp.py:642-704) */
+  int32_t gemm_engine;   /* EDG_GEMM_TC (default) or EDG_GEMM_SIMT */
   uint64_t seed;
 } edg_bnn_t;
 
@@ -272,7 +289,7 @@ typedef struct {
   int32_t baseline;        /* EDG_BASELINE_* */
   int32_t baseline_hidden; /* hidden width of the MLP baseline */
   float baseline_decay;    /* decay of the running mean / scale, in [0, 1) */
-  float reserved;
+  int32_t gemm_engine;     /* EDG_GEMM_TC (default) or EDG_GEMM_SIMT */
   uint64_t seed;
 } edg_sbn_t;
 

@@ -12,11 +12,12 @@ from oracle.klqp import TFAdam
 pytestmark = pytest.mark.gpu
 
 
-def _setup(cuda, D, H1, H2, M, S, noise=0.3, dscale=2.5, prior=1.0, seed=0):
+def _setup(cuda, D, H1, H2, M, S, noise=0.3, dscale=2.5, prior=1.0, seed=0, engine=0):
     from edward_gb300 import _lib
     lib = _lib.load()
     cfg = _lib.EdgBNN()
     cfg.D, cfg.H1, cfg.H2, cfg.n_samples = D, H1, H2, S
+    cfg.gemm_engine = engine
     cfg.noise, cfg.prior_scale, cfg.data_scale, cfg.seed = noise, prior, dscale, 17
     P = lib.edg_bnn_num_params(D, H1, H2)
     assert P == bnn.n_params(D, H1, H2)
@@ -50,10 +51,15 @@ def close(a, b, rtol):
     np.testing.assert_allclose(a, b, rtol=rtol, atol=rtol * np.abs(b).max())
 
 
-@pytest.mark.parametrize("D,H1,H2,M,S", [(5, 24, 20, 70, 3), (32, 256, 256, 300, 4)])
-def test_bnn_loss_and_gradient_parity(cuda, D, H1, H2, M, S):
+ENGINES = pytest.mark.parametrize("engine", [0, 1], ids=["tc", "simt"])
+
+
+@pytest.mark.parametrize("D,H1,H2,M,S", [(5, 24, 20, 70, 3), (32, 256, 256, 300, 4),
+                                         (32, 256, 256, 4096, 2)])
+@ENGINES
+def test_bnn_loss_and_gradient_parity(cuda, D, H1, H2, M, S, engine):
     from edward_gb300 import _lib
-    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S)
+    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S, engine=engine)
     _step(cfg, t, M, ws, apply=False)
     st = _lib.read_state(t["state"])
     loss, gmu, grho = bnn.klqp_loss_and_grads(mu, rho, eps, X, y, cfg.noise, cfg.data_scale,
@@ -64,10 +70,11 @@ def test_bnn_loss_and_gradient_parity(cuda, D, H1, H2, M, S):
     close(g[P:], grho, 2e-5)
 
 
-def test_bnn_gradient_vs_fp64_finite_differences(cuda):
+@ENGINES
+def test_bnn_gradient_vs_fp64_finite_differences(cuda, engine):
     """The hand-written adjoint against FP64 central differences of the loss."""
     D, H1, H2, M, S = 4, 9, 7, 33, 2
-    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S, seed=3)
+    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S, seed=3, engine=engine)
     _step(cfg, t, M, ws, apply=False)
     g = t["grad"].cpu().numpy().astype(np.float64)
     h = 1e-6
@@ -88,11 +95,12 @@ def test_bnn_gradient_vs_fp64_finite_differences(cuda):
         assert abs(fd - g[P + p]) <= 2e-5 * max(1.0, abs(fd)), (p, fd, g[P + p])
 
 
-def test_bnn_adam_steps(cuda):
+@ENGINES
+def test_bnn_adam_steps(cuda, engine):
     """Three fused steps with Adam equal the oracle gradient + TF Adam."""
     from edward_gb300 import _lib
     D, H1, H2, M, S = 6, 16, 12, 64, 2
-    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S, seed=5)
+    cfg, P, (X, y, mu, rho, eps), t, ws = _setup(cuda, D, H1, H2, M, S, seed=5, engine=engine)
     opt = TFAdam(2 * P)
     th = np.concatenate([mu, rho]).astype(np.float64)
     for k in range(3):
@@ -227,7 +235,8 @@ def test_bnn_reparameterization_klqp_monte_carlo_kl(cuda):
     close(grho.cpu().numpy(), r0, 2e-5)
 
 
-def test_bnn_log_lik_autograd_function(cuda):
+@ENGINES
+def test_bnn_log_lik_autograd_function(cuda, engine):
     """The torch.autograd.Function over the hand-written adjoint: backward of a
     weighted sum of per-sample log-likelihoods equals the oracle's gradient."""
     from edward_gb300 import ops
@@ -235,7 +244,7 @@ def test_bnn_log_lik_autograd_function(cuda):
     X, y = bnn.synthetic(M, D, H1, H2, seed=12)
     P = bnn.n_params(D, H1, H2)
     theta = (np.random.default_rng(13).standard_normal((S, P)) * 0.3).astype(np.float32)
-    cfg = ops.bnn_config(D, H1, H2, S, noise=0.4, data_scale=3.0)
+    cfg = ops.bnn_config(D, H1, H2, S, noise=0.4, data_scale=3.0, engine=engine)
     th = torch.tensor(theta, device=cuda, requires_grad=True)
     ll = ops.bnn_log_lik(cfg, torch.as_tensor(X, device=cuda), torch.as_tensor(y, device=cuda), th)
     w = torch.tensor([1.0, -0.5, 2.0], device=cuda)
