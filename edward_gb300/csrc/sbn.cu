@@ -33,6 +33,7 @@
 
 #include "edg_common.cuh"
 #include "gemm_simt.cuh"
+#include "gemm_tc.cuh"
 #include "optim.cuh"
 
 namespace edg {
@@ -42,7 +43,7 @@ constexpr int kT = 256;
 constexpr int kMaxSplits = 32;
 
 struct Dims {
-  int V, H0, H1, S, B, R, BH, mode;
+  int V, H0, H1, S, B, R, BH, mode, engine;
   int ldx, ld0, ld1, ldh, H0p;
   int64_t oq0, oq1, op1, op0, P;  // model parameter blocks
   int64_t ob1, PB;                // baseline: Wb0 block at 0, Wb1 block at ob1
@@ -58,6 +59,7 @@ static Dims make_dims(const edg_sbn_t* c, int B) {
   d.R = c->n_samples * B;
   d.BH = c->baseline_hidden;
   d.mode = c->baseline;
+  d.engine = c->gemm_engine;
   d.ldx = round_up(d.V + 1, 4);
   d.ld0 = round_up(d.H0 + 1, 4);
   d.ld1 = round_up(d.H1 + 1, 4);
@@ -278,9 +280,18 @@ static int choose_splits(int M, int N, int K, int sms) {
   return 1;
 }
 
-// C = A^T B with A [K, M] (lda), B [K, N] (ldb): split-K over the K rows.
-static int gemm_tn(const float* A, int lda, const float* Bm, int ldb, float* C, int ldc, int M,
-                   int N, int K, float* part, int sms, cudaStream_t st) {
+constexpr int kTcChunk = 1024;  // rows per K split on the tensor cores
+
+static bool use_tc(int engine, int N) { return engine == EDG_GEMM_TC && N >= 16; }
+
+// C = A^T B with A [K, M] (lda), B [K, N] (ldb), reduced over the K rows: on the
+// tensor cores in kTcChunk-row chunks, on the SIMT engine split-K for parallelism.
+static int gemm_tn(int engine, const float* A, int lda, const float* Bm, int ldb, float* C,
+                   int ldc, int M, int N, int K, float* part, int sms, unsigned* err,
+                   cudaStream_t st) {
+  if (use_tc(engine, N))
+    return tcg::gemm<true, false>(A, Bm, C, M, N, K, lda, ldb, ldc, 0, 0, 0, 1,
+                                  simt::EpiIdentity{}, kTcChunk, part, err, st);
   const int splits = choose_splits(M, N, K, sms);
   if (splits == 1)
     return simt::bgemm<true, false>(A, Bm, C, M, N, K, lda, ldb, ldc, 0, 0, 0, 1,
@@ -296,9 +307,25 @@ static int gemm_tn(const float* A, int lda, const float* Bm, int ldb, float* C, 
   return check_launch("sbn splitk_reduce_kernel");
 }
 
-static size_t gemm_tn_part_floats(int M, int N, int K, int sms) {
+static size_t gemm_tn_part_floats(int engine, int M, int N, int K, int sms) {
+  if (use_tc(engine, N)) return tcg::part_floats(M, N, K, 1, kTcChunk);
   const int s = choose_splits(M, N, K, sms);
   return s == 1 ? 0 : (size_t)s * M * N;
+}
+
+static int gemm_tn_launches(int engine, int M, int N, int K, int sms) {
+  if (use_tc(engine, N)) return tcg::part_floats(M, N, K, 1, kTcChunk) ? 2 : 1;
+  return choose_splits(M, N, K, sms) > 1 ? 2 : 1;
+}
+
+// C = A B (+ epilogue), A [M, K] (lda), B [K, N] (ldb).
+template <class Epi>
+static int gemm_nn(int engine, const float* A, int lda, const float* Bm, int ldb, float* C,
+                   int ldc, int M, int N, int K, Epi epi, unsigned* err, cudaStream_t st) {
+  if (use_tc(engine, N))
+    return tcg::gemm<false, false>(A, Bm, C, M, N, K, lda, ldb, ldc, 0, 0, 0, 1, epi, 0, nullptr,
+                                   err, st);
+  return simt::bgemm<false, false>(A, Bm, C, M, N, K, lda, ldb, ldc, 0, 0, 0, 1, epi, st);
 }
 
 struct FinArgs {
@@ -476,13 +503,13 @@ static size_t carve(const Dims& d, int sms, void* base, Workspace* w) {
   const int64_t R = d.R, B = d.B;
   const bool mlp = d.mode == EDG_BASELINE_MLP;
   size_t part = 0;
-  part = std::max(part, gemm_tn_part_floats(d.V + 1, d.H0, d.B, sms));
-  part = std::max(part, gemm_tn_part_floats(d.H0 + 1, d.H1, d.R, sms));
-  part = std::max(part, gemm_tn_part_floats(d.H1 + 1, d.H0, d.R, sms));
-  part = std::max(part, gemm_tn_part_floats(d.H0 + 1, d.V, d.R, sms));
+  part = std::max(part, gemm_tn_part_floats(d.engine, d.V + 1, d.H0, d.B, sms));
+  part = std::max(part, gemm_tn_part_floats(d.engine, d.H0 + 1, d.H1, d.R, sms));
+  part = std::max(part, gemm_tn_part_floats(d.engine, d.H1 + 1, d.H0, d.R, sms));
+  part = std::max(part, gemm_tn_part_floats(d.engine, d.H0 + 1, d.V, d.R, sms));
   if (mlp) {
-    part = std::max(part, gemm_tn_part_floats(d.V + 1, d.BH, d.B, sms));
-    part = std::max(part, gemm_tn_part_floats(d.BH + 1, 1, d.B, sms));
+    part = std::max(part, gemm_tn_part_floats(d.engine, d.V + 1, d.BH, d.B, sms));
+    part = std::max(part, gemm_tn_part_floats(d.engine, d.BH + 1, 1, d.B, sms));
   }
   const int nb = (d.B + kT / 32 - 1) / (kT / 32);
   const size_t o[] = {
@@ -519,6 +546,8 @@ static int check_cfg(const edg_sbn_t* c, int B) {
               "the MLP baseline needs baseline_hidden > 0");
   EDG_REQUIRE(c->baseline_decay >= 0.0f && c->baseline_decay < 1.0f, EDG_E_VALUE,
               "baseline_decay must be in [0, 1)");
+  EDG_REQUIRE(c->gemm_engine == EDG_GEMM_TC || c->gemm_engine == EDG_GEMM_SIMT, EDG_E_VALUE,
+              "unknown gemm_engine %d", c->gemm_engine);
   EDG_REQUIRE((int64_t)c->n_samples * B * std::max(c->V, std::max(c->H0, c->H1)) < (1ll << 31),
               EDG_E_SHAPE, "problem too large");
   return EDG_OK;
@@ -559,7 +588,7 @@ extern "C" int32_t edg_sbn_launches_per_step(const edg_sbn_t* cfg, int32_t B, in
   if (check_cfg(cfg, B) != EDG_OK) return -1;
   const Dims d = make_dims(cfg, B);
   const int sms = num_sms();
-  auto tn = [&](int M, int N, int K) { return choose_splits(M, N, K, sms) > 1 ? 2 : 1; };
+  auto tn = [&](int M, int N, int K) { return gemm_tn_launches(d.engine, M, N, K, sms); };
   int n = 9 + 2 + 1;  // prep .. bern_rows(x), signal, scale
   if (d.mode == EDG_BASELINE_MLP) n += 2;
   n += tn(d.V + 1, d.H0, d.B) + tn(d.H0 + 1, d.H1, d.R) + tn(d.H1 + 1, d.H0, d.R) +
@@ -602,6 +631,7 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
   cudaStream_t st = (cudaStream_t)stream;
+  unsigned* err = &state->error;
   const int rows_grid = (d.R + kT / 32 - 1) / (kT / 32);
   const int b_grid = (d.B + kT / 32 - 1) / (kT / 32);
   float* lq0 = w.terms;
@@ -614,34 +644,34 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
   prep_x_kernel<<<d.B, 256, 0, st>>>(d, X, w.Xa, mlp ? w.Xc : nullptr);
   if ((rc = check_launch("sbn prep_x_kernel"))) return rc;
   // q(z0 | x) logits, shared by all samples
-  rc = simt::bgemm<false, false>(w.Xa, theta + d.oq0, w.Lq0, d.B, d.H0, d.V + 1, d.ldx, d.H0,
-                                 d.H0, 0, 0, 0, 1, simt::EpiIdentity{}, st);
+  rc = gemm_nn(d.engine, w.Xa, d.ldx, theta + d.oq0, d.H0, w.Lq0, d.H0, d.B, d.H0, d.V + 1,
+               simt::EpiIdentity{}, err, st);
   if (rc) return rc;
   sample0_kernel<<<rows_grid, kT, 0, st>>>(d, w.Lq0, w.Z0a, w.R0, lq0, cfg->seed, state,
                                            z_override);
   if ((rc = check_launch("sbn sample0_kernel"))) return rc;
-  rc = simt::bgemm<false, false>(w.Z0a, theta + d.oq1, w.Lq1, d.R, d.H1, d.H0 + 1, d.ld0, d.H1,
-                                 d.H1, 0, 0, 0, 1, simt::EpiIdentity{}, st);
+  rc = gemm_nn(d.engine, w.Z0a, d.ld0, theta + d.oq1, d.H1, w.Lq1, d.H1, d.R, d.H1, d.H0 + 1,
+               simt::EpiIdentity{}, err, st);
   if (rc) return rc;
   sample1_kernel<<<rows_grid, kT, 0, st>>>(d, w.Lq1, w.Z1a, prior_logits, lq1, lp1, cfg->seed,
                                            state, z_override);
   if ((rc = check_launch("sbn sample1_kernel"))) return rc;
   // p(z0 | z1)
-  rc = simt::bgemm<false, false>(w.Z1a, theta + d.op1, w.Lp1, d.R, d.H0, d.H1 + 1, d.ld1, d.H0,
-                                 d.H0, 0, 0, 0, 1, simt::EpiIdentity{}, st);
+  rc = gemm_nn(d.engine, w.Z1a, d.ld1, theta + d.op1, d.H0, w.Lp1, d.H0, d.R, d.H0, d.H1 + 1,
+               simt::EpiIdentity{}, err, st);
   if (rc) return rc;
   bern_rows_kernel<<<rows_grid, kT, 0, st>>>(d.R, d.H0, w.Z0a, d.ld0, 0, w.Lp1, d.H0, lp0);
   if ((rc = check_launch("sbn bern_rows_kernel"))) return rc;
   // p(x | z0)
-  rc = simt::bgemm<false, false>(w.Z0a, theta + d.op0, w.Lp0, d.R, d.V, d.H0 + 1, d.ld0, d.V, d.V,
-                                 0, 0, 0, 1, simt::EpiIdentity{}, st);
+  rc = gemm_nn(d.engine, w.Z0a, d.ld0, theta + d.op0, d.V, w.Lp0, d.V, d.R, d.V, d.H0 + 1,
+               simt::EpiIdentity{}, err, st);
   if (rc) return rc;
   bern_rows_kernel<<<rows_grid, kT, 0, st>>>(d.R, d.V, w.Xa, d.ldx, d.B, w.Lp0, d.V, lx);
   if ((rc = check_launch("sbn bern_rows_kernel"))) return rc;
   // MLP baseline forward (uses parameters from earlier steps only)
   if (mlp) {
-    rc = simt::bgemm<false, false>(w.Xc, baseline_params, w.Hb, d.B, d.BH, d.V + 1, d.ldx, d.BH,
-                                   d.ldh, 0, 0, 0, 1, simt::EpiTanh{}, st);
+    rc = gemm_nn(d.engine, w.Xc, d.ldx, baseline_params, d.BH, w.Hb, d.ldh, d.B, d.BH, d.V + 1,
+                 simt::EpiTanh{}, err, st);
     if (rc) return rc;
     mlp_out_kernel<<<b_grid, kT, 0, st>>>(d, w.Hb, baseline_params, w.mlp_out);
     if ((rc = check_launch("sbn mlp_out_kernel"))) return rc;
@@ -659,17 +689,18 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
     cudaMemcpyAsync(signal_out, w.f, (size_t)d.R * 4, cudaMemcpyDeviceToDevice, st);
   }
   // gradients (weight and bias blocks at once)
-  if ((rc = gemm_tn(w.Xa, d.ldx, w.R0q, d.H0, w.G + d.oq0, d.H0, d.V + 1, d.H0, d.B, w.part, sms,
-                    st)))
+  const int e = d.engine;
+  if ((rc = gemm_tn(e, w.Xa, d.ldx, w.R0q, d.H0, w.G + d.oq0, d.H0, d.V + 1, d.H0, d.B, w.part,
+                    sms, err, st)))
     return rc;
-  if ((rc = gemm_tn(w.Z0a, d.ld0, w.Lq1, d.H1, w.G + d.oq1, d.H1, d.H0 + 1, d.H1, d.R, w.part, sms,
-                    st)))
+  if ((rc = gemm_tn(e, w.Z0a, d.ld0, w.Lq1, d.H1, w.G + d.oq1, d.H1, d.H0 + 1, d.H1, d.R, w.part,
+                    sms, err, st)))
     return rc;
-  if ((rc = gemm_tn(w.Z1a, d.ld1, w.Lp1, d.H0, w.G + d.op1, d.H0, d.H1 + 1, d.H0, d.R, w.part, sms,
-                    st)))
+  if ((rc = gemm_tn(e, w.Z1a, d.ld1, w.Lp1, d.H0, w.G + d.op1, d.H0, d.H1 + 1, d.H0, d.R, w.part,
+                    sms, err, st)))
     return rc;
-  if ((rc = gemm_tn(w.Z0a, d.ld0, w.Lp0, d.V, w.G + d.op0, d.V, d.H0 + 1, d.V, d.R, w.part, sms,
-                    st)))
+  if ((rc = gemm_tn(e, w.Z0a, d.ld0, w.Lp0, d.V, w.G + d.op0, d.V, d.H0 + 1, d.V, d.R, w.part, sms,
+                    err, st)))
     return rc;
   FinArgs f;
   f.d = d;
@@ -688,10 +719,11 @@ extern "C" int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt,
                                                 baseline_params, w.dout, w.dHb, w.bpart);
     if ((rc = check_launch("sbn baseline_grad_kernel"))) return rc;
     if (mlp) {
-      if ((rc = gemm_tn(w.Xc, d.ldx, w.dHb, d.BH, w.GB, d.BH, d.V + 1, d.BH, d.B, w.part, sms, st)))
+      if ((rc = gemm_tn(e, w.Xc, d.ldx, w.dHb, d.BH, w.GB, d.BH, d.V + 1, d.BH, d.B, w.part, sms,
+                        err, st)))
         return rc;
-      if ((rc = gemm_tn(w.Hb, d.ldh, w.dout, 1, w.GB + d.ob1, 1, d.BH + 1, 1, d.B, w.part, sms,
-                        st)))
+      if ((rc = gemm_tn(e, w.Hb, d.ldh, w.dout, 1, w.GB + d.ob1, 1, d.BH + 1, 1, d.B, w.part, sms,
+                        err, st)))
         return rc;
     }
     BaseArgs ba;

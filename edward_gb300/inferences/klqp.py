@@ -43,12 +43,18 @@ class KLqp(VariationalInference):
             latent_vars = d
         super().__init__(latent_vars, data)
 
-    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, *args, **kwargs):
+    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, gemm_engine="tc",
+                   *args, **kwargs):
         """``n_samples`` / ``kl_scaling`` as in ``klqp.py:86-113``.  ``n_minibatch``
-        (Bayesian NN family, data bound to arrays): each step draws that many
+        (network families, data bound to arrays): each step draws that many
         rows uniformly with replacement on the device instead of using the
-        whole data set; ``scale`` for the observed variable then defaults to
-        N / n_minibatch."""
+        whole data set; for the Bayesian NN ``scale`` for the observed variable
+        then defaults to N / n_minibatch.  ``gemm_engine`` (network families):
+        ``"tc"`` runs the layer GEMMs on the tensor cores (tcgen05, 3xTF32),
+        ``"simt"`` on the FP32 CUDA cores."""
+        if gemm_engine not in ("tc", "simt"):
+            raise ValueError(f"gemm_engine must be 'tc' or 'simt'; got {gemm_engine!r}")
+        self.gemm_engine = _lib.GEMM_TC if gemm_engine == "tc" else _lib.GEMM_SIMT
         if kl_scaling is None:
             kl_scaling = {}
         if n_samples <= 0:
@@ -182,6 +188,7 @@ class KLqp(VariationalInference):
         cfg.noise, cfg.prior_scale = spec.noise, spec.prior_scale
         cfg.data_scale = float(dscale.reshape(-1)[0])
         cfg.method = self._method_id
+        cfg.gemm_engine = self.gemm_engine
         cfg.seed = next_seed()
         self._bnn.seed = next_seed()
         self._cfg = cfg
@@ -219,6 +226,7 @@ class KLqp(VariationalInference):
         cfg.V, cfg.H0, cfg.H1, cfg.n_samples = V, H0, H1, self.n_samples
         cfg.baseline, cfg.baseline_hidden = mode, self.baseline_hidden
         cfg.baseline_decay = self.baseline_decay
+        cfg.gemm_engine = self.gemm_engine
         cfg.seed = next_seed()
         self._cfg = cfg
         self._opt = self.optimizer.to_c()
@@ -338,8 +346,8 @@ class ScoreKLqp(KLqp):
     ``baseline_optimizer`` (default Adam, learning rate 1e-2)."""
     _method = SCORE
 
-    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, baseline=None,
-                   baseline_hidden=100, baseline_optimizer=None, baseline_decay=0.9,
+    def initialize(self, n_samples=1, kl_scaling=None, n_minibatch=None, gemm_engine="tc",
+                   baseline=None, baseline_hidden=100, baseline_optimizer=None, baseline_decay=0.9,
                    *args, **kwargs):
         from .. import train
         self.baseline = baseline or "none"
@@ -351,7 +359,7 @@ class ScoreKLqp(KLqp):
         if not 0.0 <= baseline_decay < 1.0:
             raise ValueError("baseline_decay must be in [0, 1)")
         self.baseline_decay = float(baseline_decay)
-        return super().initialize(n_samples, kl_scaling, n_minibatch, *args, **kwargs)
+        return super().initialize(n_samples, kl_scaling, n_minibatch, gemm_engine, *args, **kwargs)
 
     def _validate(self):
         super()._validate()

@@ -6,7 +6,6 @@ import pytest
 import torch
 
 from oracle import sbn
-from oracle.klqp import TFAdam
 
 pytestmark = pytest.mark.gpu
 
@@ -38,9 +37,10 @@ def _draws(rng, S, B, H0, H1):
 @pytest.mark.parametrize("V,H0,H1,B,S", [(20, 12, 8, 16, 3), (784, 200, 200, 64, 4),
                                           (50, 20, 10, 512, 4)])
 @pytest.mark.parametrize("baseline", [None, "mean", "mlp"])
-def test_sbn_score_gradient_parity_given_draws(cuda, V, H0, H1, B, S, baseline):
+@pytest.mark.parametrize("engine", ["tc", "simt"])
+def test_sbn_score_gradient_parity_given_draws(cuda, V, H0, H1, B, S, baseline, engine):
     from sbn_model import flat_theta
-    inf, x_ph, weights, X, pl = _setup(V, H0, H1, B, S, baseline)
+    inf, x_ph, weights, X, pl = _setup(V, H0, H1, B, S, baseline, gemm_engine=engine)
     inf._feed({x_ph: X})
     stats, bp = None, None
     if baseline is not None:        # a baseline that has seen earlier steps
@@ -77,35 +77,41 @@ def test_sbn_philox_draws_follow_the_bernoulli_rule(cuda):
     close(g.cpu().numpy(), ref["grad"], 2e-5)
 
 
-@pytest.mark.parametrize("V,H0,H1,B,S", [(24, 10, 8, 16, 4), (300, 12, 8, 1024, 2)])
+@pytest.mark.parametrize("V,H0,H1,B,S", [(24, 10, 8, 16, 4), (300, 12, 8, 1024, 2),
+                                          (784, 200, 200, 32, 4)])
 def test_sbn_training_steps_with_mlp_baseline_match_oracle(cuda, V, H0, H1, B, S):
-    """Three update() calls: model Adam step + the baseline's own regression
-    step and running statistics, all against the oracle chain (the second
-    size runs every gradient GEMM split over the rows)."""
+    """Three training steps, each checked as a transition from the device's
+    state before it: the model step (plain gradient descent, so the parameter
+    change is lr times the gradient), the MLP baseline's own Adam step and the
+    running statistics, against the oracle (the second size splits every
+    gradient GEMM over the rows).  The draws are given: a Bernoulli draw
+    u < sigmoid(l) flips when u is within the logits' rounding error of its
+    threshold, which among ~10^5 draws happens; the Philox draw rule has its
+    own test at a size where no draw is that close."""
     import edward_gb300 as ed
     from sbn_model import flat_theta
     BH = 16
+    lr = 0.05
     inf, x_ph, weights, X, pl = _setup(V, H0, H1, B, S, "mlp",
-                                       optimizer=ed.train.AdamOptimizer(1e-3))
-    th = flat_theta(weights)
-    P = th.size
-    opt = TFAdam(P)
-    stats = np.array([0.0, 1.0, 0.0, 0.9, 0.999, 0, 0, 0])
-    bp = inf._bparams.cpu().numpy().astype(np.float64)
-    bsl = np.zeros(2 * bp.size)
+                                       optimizer=ed.train.GradientDescentOptimizer(lr))
+    inf._feed({x_ph: X})
+    rng = np.random.default_rng(11)
     for t in range(3):
-        u0, u1 = sbn.draw_uniforms(inf.seed, t, S, B, H0, H1)
-        z0, z1, (p0, p1) = sbn.sample_z(th, X, u0, u1, V, H0, H1)
-        assert min(np.abs(u0 - p0[None]).min(), np.abs(u1 - p1).min()) > 1e-6
-        ref = sbn.score_step(th, X, pl, z0, z1, V, H0, H1, mode=sbn.MLP, stats=stats,
-                             bparams=bp, BH=BH)
-        info = inf.update(feed_dict={x_ph: X})
-        assert abs(info["loss"] - ref["loss"]) <= 1e-5 * abs(ref["loss"])
-        th = opt.apply(th, ref["grad"], 1e-3)
-        stats, bp, bsl = sbn.baseline_update(ref, X, stats, bp, bsl, V, BH, sbn.MLP, 0.9, 1e-2)
-        np.testing.assert_allclose(flat_theta(weights), th, rtol=1e-4, atol=2e-5)
-        np.testing.assert_allclose(inf._bparams.cpu().numpy(), bp, rtol=1e-4, atol=2e-5)
-        np.testing.assert_allclose(inf._bstats.cpu().numpy()[:6], stats[:6], rtol=2e-5, atol=1e-6)
+        th = flat_theta(weights)
+        stats = inf._bstats.cpu().numpy().astype(np.float64)
+        bp = inf._bparams.cpu().numpy().astype(np.float64)
+        bsl = inf._bslots.cpu().numpy().astype(np.float64)
+        z0, z1 = _draws(rng, S, B, H0, H1)
+        ref = sbn.score_step(th, X, pl, z0.astype(np.float64), z1.astype(np.float64), V, H0, H1,
+                             mode=sbn.MLP, stats=stats, bparams=bp, BH=BH)
+        zo = torch.cat([torch.as_tensor(z0).reshape(-1), torch.as_tensor(z1).reshape(-1)]).to(cuda)
+        inf._step(apply=True, eps=zo)
+        loss = inf._read_state().loss
+        assert abs(loss - ref["loss"]) <= 1e-5 * abs(ref["loss"])
+        close(flat_theta(weights) - th, -lr * ref["grad"], 2e-5)
+        stats1, bp1, _ = sbn.baseline_update(ref, X, stats, bp, bsl, V, BH, sbn.MLP, 0.9, 1e-2)
+        np.testing.assert_allclose(inf._bparams.cpu().numpy(), bp1, rtol=1e-4, atol=2e-5)
+        np.testing.assert_allclose(inf._bstats.cpu().numpy()[:6], stats1[:6], rtol=2e-5, atol=1e-6)
     assert inf.t == 3
 
 
