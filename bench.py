@@ -568,13 +568,13 @@ def run_bnn(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "bnn_klqp_N100000_D32_H256_H256_S64_M4096", "params": P,
-                       "launch": f"CUDA graph of {chunk} steps (gather + 12 launches each)",
+                       "launch": f"CUDA graph of {chunk} steps (gather + 13 launches each)",
                        "l2_flush": "inputs larger than L2 (activations %.0f MB per step)"
                                    % (act_bytes / 1e6)},
-            "gpu_launches": K * 13,
+            "gpu_launches": K * 14,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                          "frac": ach / peak, "traffic": None,
-                         "kernel": "whole step (SIMT bgemm + head + adjoint + finalize)",
+                         "kernel": "whole step (tcgen05 3xTF32 GEMMs + fused head/adjoint + finalize)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
             "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)

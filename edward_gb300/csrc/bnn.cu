@@ -14,9 +14,9 @@
 //   sample   theta_s = mu + sigma * eps_s (Philox), eps kept for the rho gradient;
 //            Xa = [X, 1] and the ones columns of H1a / H2a
 //   F1, F2   H1a = tanh(Xa W0a), H2a = tanh(H1a W1a)    (batched over samples)
-//   head     out, residual, FP64 log-lik partials, dout = scale (y - out) / noise^2
-//   G2       [dW2; db2] = H2a^T dout
-//   adj2     dH2 = dout w2 (1 - h2^2)                  (in place of h2)
+//   head     one pass over h2: out, residual, FP64 log-lik partials,
+//            dout = scale (y - out) / noise^2, dH2 = dout w2 (1 - h2^2) in place
+//            of h2 and per-block partials of [dW2; db2] = sum_m [h2; 1] dout
 //   B1       [dW1; db1] = H1a^T dH2
 //   B2       dH1 = (dH2 W1^T)(1 - h1^2)                (in place of h1)
 //   B3       [dW0; db0] = Xa^T dH1
@@ -113,34 +113,45 @@ __global__ void prep_kernel(Layout L, Act a, int S, const float* __restrict__ X,
 // ------------------------------------------------------------ output layer
 constexpr int kHeadRows = 32;  // rows per block (4 per warp)
 
-// out = h2 . w2 + b2, residual, dout = scale * res / noise^2 and per-block
-// FP64 partial sums of the unscaled log-likelihood; grid (M / kHeadRows, S).
-__global__ void __launch_bounds__(kT) head_kernel(Layout L, Act a, const float* __restrict__ y,
-                                                  const float* __restrict__ theta,
-                                                  const float* __restrict__ H2a,
-                                                  float* __restrict__ dout,
-                                                  double* __restrict__ ll_part, float noise,
-                                                  float dscale) {
+// One pass over a block of kHeadRows rows of sample s (grid (M / kHeadRows, S)):
+// out = h2 . w2 + b2, residual, dout = scale * res / noise^2, then
+// dH2 = dout w2 (1 - h2^2) written over h2, per-block partials of
+// [dW2; db2] = sum_m [h2_m; 1] dout_m (wpart[blk][s][0..H2]) and of the
+// unscaled FP64 log-likelihood (ll_part[s][blk]).  Requires H2 < 1024.
+__global__ void __launch_bounds__(kT) head_adj_kernel(Layout L, Act a, const float* __restrict__ y,
+                                                      const float* __restrict__ theta, float* H2a,
+                                                      float* __restrict__ wpart,
+                                                      double* __restrict__ ll_part, float noise,
+                                                      float dscale) {
+  extern __shared__ float s_part[];  // [kT / 32][H2 + 1]
   __shared__ double red[kT / 32];
-  const int s = blockIdx.y;
+  const int s = blockIdx.y, nblk = gridDim.x;
   const float* w2 = theta + (int64_t)s * a.ps + L.oW2;
   const float b2 = w2[L.H2];
   const float inv_var = 1.0f / (noise * noise);
   const float lnorm = logf(noise) + (float)kHalfLog2Pi;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* my = s_part + warp * (L.H2 + 1);
+  for (int k = lane; k <= L.H2; k += 32) my[k] = 0.0f;
   double acc = 0.0;
   for (int i = warp; i < kHeadRows; i += kT / 32) {
     const int m = blockIdx.x * kHeadRows + i;
     if (m >= a.M) break;
-    const float* h = H2a + ((int64_t)s * a.M + m) * a.ld2;
+    float* h = H2a + ((int64_t)s * a.M + m) * a.ld2;
     float v = 0.0f;
     for (int k = lane; k < L.H2; k += 32) v = fmaf(h[k], __ldg(w2 + k), v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     const float res = y[m] - (v + b2);
+    const float d = dscale * res * inv_var;
     if (lane == 0) {
-      dout[(int64_t)s * a.M + m] = dscale * res * inv_var;
       acc += (double)(-0.5f * res * res * inv_var - lnorm);
+      my[L.H2] += d;
+    }
+    for (int k = lane; k < L.H2; k += 32) {
+      const float hk = h[k];
+      my[k] = fmaf(hk, d, my[k]);
+      h[k] = d * __ldg(w2 + k) * (1.0f - hk * hk);
     }
   }
   if (lane == 0) red[warp] = acc;
@@ -148,7 +159,13 @@ __global__ void __launch_bounds__(kT) head_kernel(Layout L, Act a, const float* 
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < kT / 32; ++w) t += red[w];
-    ll_part[(int64_t)s * gridDim.x + blockIdx.x] = t;
+    ll_part[(int64_t)s * nblk + blockIdx.x] = t;
+  }
+  float* out = wpart + ((int64_t)blockIdx.x * gridDim.y + s) * (L.H2 + 1);
+  for (int k = threadIdx.x; k <= L.H2; k += kT) {
+    float t = 0.0f;
+    for (int w = 0; w < kT / 32; ++w) t += s_part[w * (L.H2 + 1) + k];
+    out[k] = t;
   }
 }
 
@@ -168,21 +185,6 @@ __global__ void __launch_bounds__(kT) ll_reduce_kernel(const double* __restrict_
     double t = 0.0;
     for (int w = 0; w < kT / 32; ++w) t += red[w];
     ll[s] = t * (double)dscale;
-  }
-}
-
-// dH2 = dout * w2 * (1 - h2^2), written over h2 (columns < H2 only).
-__global__ void adj2_kernel(Layout L, Act a, int S, const float* __restrict__ theta,
-                            const float* __restrict__ dout, float* __restrict__ H2a) {
-  const int64_t n = (int64_t)S * a.M * L.H2;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / L.H2;
-    const int k = (int)(i % L.H2);
-    const int s = (int)(r / a.M);
-    float* hp = H2a + r * a.ld2 + k;
-    const float h = *hp;
-    *hp = dout[r] * __ldg(theta + (int64_t)s * a.ps + L.oW2 + k) * (1.0f - h * h);
   }
 }
 
@@ -310,7 +312,7 @@ __global__ void gather_kernel(const float* __restrict__ X, const float* __restri
 }
 
 struct Workspace {
-  float *theta, *eps, *G, *Xa, *H1, *H2, *dout, *part;
+  float *theta, *eps, *G, *Xa, *H1, *H2, *wpart, *part;
   double *ll, *ll_part, *kl_part;
 };
 
@@ -340,7 +342,7 @@ static size_t carve(const Layout& L, int S, int M, int engine, void* base, Works
   const size_t o_part = take(part_floats(L, S, M, engine) * 4);
   const size_t o_Xa = take((size_t)M * a.ldx * 4);
   const size_t o_H1 = take((size_t)S * M * a.ld1 * 4), o_H2 = take((size_t)S * M * a.ld2 * 4);
-  const size_t o_dout = take((size_t)S * M * 4);
+  const size_t o_wpart = take((size_t)head_blocks(M) * S * (L.H2 + 1) * 4);
   const size_t o_ll = take((size_t)S * 8), o_llp = take((size_t)S * head_blocks(M) * 8);
   const size_t o_kl = take((size_t)((L.P + kT - 1) / kT) * 8);
   if (w && base) {
@@ -351,7 +353,7 @@ static size_t carve(const Layout& L, int S, int M, int engine, void* base, Works
     w->Xa = reinterpret_cast<float*>(b + o_Xa);
     w->H1 = reinterpret_cast<float*>(b + o_H1);
     w->H2 = reinterpret_cast<float*>(b + o_H2);
-    w->dout = reinterpret_cast<float*>(b + o_dout);
+    w->wpart = reinterpret_cast<float*>(b + o_wpart);
     w->part = reinterpret_cast<float*>(b + o_part);
     w->ll = reinterpret_cast<double*>(b + o_ll);
     w->ll_part = reinterpret_cast<double*>(b + o_llp);
@@ -393,20 +395,14 @@ static int loglik_grad(const Layout& L, int S, int M, int ps, int engine, const 
                              a.ld2, s1, ps, s2, S, EpiTanh{}, w.part, err, st);
   if (rc) return rc;
   const int hb = head_blocks(M);
-  head_kernel<<<dim3(hb, S), kT, 0, st>>>(L, a, y, theta, w.H2, w.dout, w.ll_part, noise, dscale);
-  if ((rc = check_launch("bnn head_kernel"))) return rc;
+  head_adj_kernel<<<dim3(hb, S), kT, (kT / 32) * (L.H2 + 1) * sizeof(float), st>>>(
+      L, a, y, theta, w.H2, w.wpart, w.ll_part, noise, dscale);
+  if ((rc = check_launch("bnn head_adj_kernel"))) return rc;
   ll_reduce_kernel<<<S, kT, 0, st>>>(w.ll_part, hb, dscale, ll);
   if ((rc = check_launch("bnn ll_reduce_kernel"))) return rc;
-  // G2: [dW2; db2] = H2a^T dout
-  rc = bgemm<true, false>(w.H2, w.dout, G + L.oW2, L.H2 + 1, 1, M, a.ld2, 1, 1, s2, M, ps, S,
-                          EpiIdentity{}, st);
-  if (rc) return rc;
-  {
-    const int64_t n = (int64_t)S * M * L.H2;
-    adj2_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 8192), 256, 0, st>>>(
-        L, a, S, theta, w.dout, w.H2);
-    if ((rc = check_launch("bnn adj2_kernel"))) return rc;
-  }
+  // [dW2; db2] = sum of the per-block partials
+  if ((rc = tcg::sum_partials(w.wpart, hb, S, 1, L.H2 + 1, G + L.oW2, L.H2 + 1, ps, st)))
+    return rc;
   // B1: [dW1; db1] = H1a^T dH2
   rc = gemm_on<true, false>(engine, w.H1, w.H2, G + L.oW1, L.H1 + 1, L.H2, M, a.ld1, a.ld2, L.H2,
                             s1, s2, ps, S, EpiIdentity{}, w.part, err, st);
@@ -434,6 +430,7 @@ static int check_cfg(const edg_bnn_t* c, int M) {
               "method %d: the Bayesian NN step implements the reparameterisation gradient "
               "with analytic or Monte Carlo KL", c->method);
   const int64_t P = (int64_t)make_layout(c->D, c->H1, c->H2).P;
+  EDG_REQUIRE(c->H2 < 1024, EDG_E_SHAPE, "the second hidden layer is limited to 1023 units");
   EDG_REQUIRE(P * c->n_samples < (1ll << 31) && (int64_t)c->n_samples * M * c->H1 < (1ll << 40),
               EDG_E_SHAPE, "problem too large");
   return EDG_OK;

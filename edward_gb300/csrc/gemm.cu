@@ -1,9 +1,39 @@
 // Batched FP32 GEMM entry point over the two GEMM engines used by the
 // network steps (tensor-core 3xTF32 and SIMT FP32), for tests and callers
 // that need the building block on its own.
+#define EDG_GEMM_TC_IMPL
 #include "edg_common.cuh"
 #include "gemm_simt.cuh"
 #include "gemm_tc.cuh"
+
+namespace edg {
+namespace tcg {
+
+// The tensor-core GEMM kernels live in this translation unit only (their
+// launch attributes are set once per kernel here); the network steps call the
+// instantiations below.
+#define EDG_TC_GEMM(TA, TB, EPI)                                                               \
+  template int gemm<TA, TB, EPI>(const float*, const float*, float*, int, int, int, int, int, \
+                                 int, int64_t, int64_t, int64_t, int, EPI, int, float*,       \
+                                 unsigned*, cudaStream_t);
+EDG_TC_GEMM(false, false, simt::EpiIdentity)
+EDG_TC_GEMM(false, false, simt::EpiTanh)
+EDG_TC_GEMM(true, false, simt::EpiIdentity)
+EDG_TC_GEMM(false, true, simt::EpiIdentity)
+EDG_TC_GEMM(false, true, simt::EpiTanhGrad)
+EDG_TC_GEMM(true, true, simt::EpiIdentity)
+#undef EDG_TC_GEMM
+
+int sum_partials(const float* part, int splits, int batch, int M, int N, float* C, int ldc,
+                 int64_t sC, cudaStream_t st) {
+  const int64_t total = (int64_t)M * N * batch;
+  splitk_sum_kernel<<<(int)std::min<int64_t>((total + 255) / 256, 8 * sm_count()), 256, 0, st>>>(
+      part, splits, batch, M, N, C, ldc, sC, simt::EpiIdentity{});
+  return check_launch("splitk_sum_kernel");
+}
+
+}  // namespace tcg
+}  // namespace edg
 
 using namespace edg;
 

@@ -30,11 +30,43 @@
 // EDG_E_TIMEOUT in *err and runs to completion.
 #pragma once
 
+#include <cstddef>
+#include <cstdint>
+
 #include <algorithm>
 
 #include "edg_common.cuh"
 #include "tc_common.cuh"
 
+namespace edg {
+namespace tcg {
+
+constexpr int kBK = 16;  // K rows per pipeline stage
+
+// Partial-sum floats gemm() needs for this problem (0 without a K split).
+inline size_t part_floats(int M, int N, int K, int batch, int kchunk) {
+  const int splits = kchunk > 0 ? (K + kchunk - 1) / kchunk : 1;
+  return splits > 1 ? (size_t)splits * batch * M * N : 0;
+}
+
+// C[b] = epi(op(A[b]) op(B[b])) on the tensor cores.  kchunk > 0 splits K into
+// chunks of kchunk rows (rounded up to a multiple of 16) whose partials are
+// summed in FP32 from `part` (part_floats() floats); err (device, may be NULL)
+// receives EDG_E_TIMEOUT if a bounded wait gave up.  Instantiated in gemm.cu
+// for the (TA, TB, Epi) combinations the library uses.
+template <bool TA, bool TB, class Epi>
+int gemm(const float* A, const float* B, float* C, int M, int N, int K, int lda, int ldb, int ldc,
+         int64_t sA, int64_t sB, int64_t sC, int batch, Epi epi, int kchunk, float* part,
+         unsigned* err, cudaStream_t st);
+
+// C[b][m][n] (+)= sum over splits of part[s][b][m][n] (C row stride ldc, batch stride sC).
+int sum_partials(const float* part, int splits, int batch, int M, int N, float* C, int ldc,
+                 int64_t sC, cudaStream_t st);
+
+}  // namespace tcg
+}  // namespace edg
+
+#ifdef EDG_GEMM_TC_IMPL
 namespace edg {
 namespace tcg {
 
@@ -114,39 +146,51 @@ __device__ __forceinline__ float4 load_mn4(const Operand& o, const float* base, 
   return v;
 }
 
-// One operand tile (R rows x BK) of one stage: producer thread tp of kProdThreads.
+// One operand tile (R rows x BK) of one stage is fetched into four float4
+// registers per producer thread and then split and stored, so that the
+// global loads of the next stage are in flight while this one is stored.
+// K-contiguous source: float4 chunk c = tp + 256 i holds row c / 4, K group c % 4.
+// MN-contiguous source: task tp (< R) loads the 4 x 4 block of rows
+// 4 (tp % (R / 4)) .. + 3 and K group tp / (R / 4), transposed when stored.
 template <int R>
-__device__ __forceinline__ void load_tile(const Operand& o, const float* base, int r0, int k0,
-                                          int K, uint32_t hi, uint32_t lo, int tp) {
+__device__ __forceinline__ void fetch_tile(const Operand& o, const float* base, int r0, int k0,
+                                           int K, int tp, float4 (&r)[4]) {
   if (o.kcontig) {
-    // R * BK / 4 float4 chunks; chunk c: row c / 4, K group c % 4
-    constexpr int kChunks = R * BK / 4;
+    constexpr int kPer = R * BK / 4 / kProdThreads;  // 2 (R = 128) or 4 (R = 256)
 #pragma unroll
-    for (int c = tp; c < kChunks; c += kProdThreads) {
-      const int row = c >> 2, kg = c & 3;
-      const float4 v = load_k4(o, base, r0 + row, k0 + 4 * kg, K);
-      const uint32_t off = soff(row, 4 * kg);
-      st_split4(hi + off, lo + off, v);
+    for (int i = 0; i < kPer; ++i) {
+      const int c = tp + i * kProdThreads;
+      r[i] = load_k4(o, base, r0 + (c >> 2), k0 + 4 * (c & 3), K);
     }
-  } else {
-    // (R / 4) row groups x 4 K groups; each task loads a 4 x 4 block and transposes it
-    constexpr int kTasks = (R / 4) * 4;
+  } else if (tp < R) {
+    const int rg = tp % (R / 4), kg = tp / (R / 4);
 #pragma unroll
-    for (int t = tp; t < kTasks; t += kProdThreads) {
-      const int rg = t % (R / 4), kg = t / (R / 4);
-      float4 v[4];
+    for (int j = 0; j < 4; ++j) r[j] = load_mn4(o, base, r0 + 4 * rg, k0 + 4 * kg + j, K);
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void put_tile(const Operand& o, int tp, const float4 (&r)[4],
+                                         uint32_t hi, uint32_t lo) {
+  if (o.kcontig) {
+    constexpr int kPer = R * BK / 4 / kProdThreads;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) v[j] = load_mn4(o, base, r0 + 4 * rg, k0 + 4 * kg + j, K);
-      const float4 c0 = make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
-      const float4 c1 = make_float4(v[0].y, v[1].y, v[2].y, v[3].y);
-      const float4 c2 = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
-      const float4 c3 = make_float4(v[0].w, v[1].w, v[2].w, v[3].w);
-      const int row = 4 * rg;
-      st_split4(hi + soff(row + 0, 4 * kg), lo + soff(row + 0, 4 * kg), c0);
-      st_split4(hi + soff(row + 1, 4 * kg), lo + soff(row + 1, 4 * kg), c1);
-      st_split4(hi + soff(row + 2, 4 * kg), lo + soff(row + 2, 4 * kg), c2);
-      st_split4(hi + soff(row + 3, 4 * kg), lo + soff(row + 3, 4 * kg), c3);
+    for (int i = 0; i < kPer; ++i) {
+      const int c = tp + i * kProdThreads;
+      const uint32_t off = soff(c >> 2, 4 * (c & 3));
+      st_split4(hi + off, lo + off, r[i]);
     }
+  } else if (tp < R) {
+    const int rg = tp % (R / 4), kg = tp / (R / 4);
+    const int row = 4 * rg;
+    st_split4(hi + soff(row + 0, 4 * kg), lo + soff(row + 0, 4 * kg),
+              make_float4(r[0].x, r[1].x, r[2].x, r[3].x));
+    st_split4(hi + soff(row + 1, 4 * kg), lo + soff(row + 1, 4 * kg),
+              make_float4(r[0].y, r[1].y, r[2].y, r[3].y));
+    st_split4(hi + soff(row + 2, 4 * kg), lo + soff(row + 2, 4 * kg),
+              make_float4(r[0].z, r[1].z, r[2].z, r[3].z));
+    st_split4(hi + soff(row + 3, 4 * kg), lo + soff(row + 3, 4 * kg),
+              make_float4(r[0].w, r[1].w, r[2].w, r[3].w));
   }
 }
 
@@ -220,24 +264,64 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
 
   if (warp < kProdWarps) {
     // ---------------------------------------------------------------- producers
+    // Stages are produced in one flat sequence over this CTA's tiles; the
+    // loads of stage i + 1 are issued before stage i is stored.
     const int tp = threadIdx.x;
-    uint32_t it = 0;
-    for (int64_t t = blockIdx.x; t < p.total && !s_err; t += gridDim.x) {
+    struct Job {
+      int64_t t;
+      int kt, nk, kb, ke, r0a, r0b;
+      const float* Ab;
+      const float* Bb;
+    };
+    auto make_job = [&](int64_t t, Job& j) {
       const Tile x = tile_of(p, t);
-      const int kb = x.ks * p.kchunk, ke = min(p.K, kb + p.kchunk);
-      const int nk = (ke - kb + BK - 1) / BK;
-      const float* Ab = p.A.p + x.b * p.A.sb;
-      const float* Bb = p.B.p + x.b * p.B.sb;
-      for (int kt = 0; kt < nk && !s_err; ++kt, ++it) {
-        const int s = (int)(it % kStages);
-        if (it >= (uint32_t)kStages) mbar_wait(empty(s), ((it / kStages) - 1) & 1, &s_err);
-        const uint32_t st = sbase + s * kStageBytes;
-        const int k0 = kb + kt * BK;
-        load_tile<BM>(p.A, Ab, x.mt * BM, k0, ke, st, st + kABytes, tp);
-        load_tile<BN>(p.B, Bb, x.nt * BN, k0, ke, st + 2 * kABytes, st + 2 * kABytes + kBBytes, tp);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(full(s));
+      j.t = t;
+      j.kt = 0;
+      j.kb = x.ks * p.kchunk;
+      j.ke = min(p.K, j.kb + p.kchunk);
+      j.nk = (j.ke - j.kb + BK - 1) / BK;
+      j.r0a = x.mt * BM;
+      j.r0b = x.nt * BN;
+      j.Ab = p.A.p + x.b * p.A.sb;
+      j.Bb = p.B.p + x.b * p.B.sb;
+    };
+    float4 ca[4], cb[4], na[4], nb[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ca[i] = cb[i] = na[i] = nb[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Job cur;
+    bool have = blockIdx.x < p.total;
+    if (have) {
+      make_job(blockIdx.x, cur);
+      fetch_tile<BM>(p.A, cur.Ab, cur.r0a, cur.kb, cur.ke, tp, ca);
+      fetch_tile<BN>(p.B, cur.Bb, cur.r0b, cur.kb, cur.ke, tp, cb);
+    }
+    for (uint32_t it = 0; have && !s_err; ++it) {
+      Job nxt = cur;
+      bool have_next = true;
+      if (++nxt.kt == cur.nk) {
+        const int64_t t2 = cur.t + gridDim.x;
+        have_next = t2 < p.total;
+        if (have_next) make_job(t2, nxt);
       }
+      if (have_next) {
+        const int k0 = nxt.kb + nxt.kt * BK;
+        fetch_tile<BM>(p.A, nxt.Ab, nxt.r0a, k0, nxt.ke, tp, na);
+        fetch_tile<BN>(p.B, nxt.Bb, nxt.r0b, k0, nxt.ke, tp, nb);
+      }
+      const int s = (int)(it % kStages);
+      if (it >= (uint32_t)kStages) mbar_wait(empty(s), ((it / kStages) - 1) & 1, &s_err);
+      const uint32_t st = sbase + s * kStageBytes;
+      put_tile<BM>(p.A, tp, ca, st, st + kABytes);
+      put_tile<BN>(p.B, tp, cb, st + 2 * kABytes, st + 2 * kABytes + kBBytes);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(full(s));
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        ca[i] = na[i];
+        cb[i] = nb[i];
+      }
+      cur = nxt;
+      have = have_next;
     }
   } else if (warp == kMmaWarp) {
     // ---------------------------------------------------------------- MMA issuer
@@ -369,14 +453,6 @@ inline bool aligned16(const void* p, int ld, int64_t sb) {
   return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (ld & 3) == 0 && (sb & 3) == 0;
 }
 
-// Partial-sum floats gemm() needs for this problem (0 without a K split).
-inline size_t part_floats(int M, int N, int K, int batch, int kchunk) {
-  const int splits = kchunk > 0 ? (K + kchunk - 1) / kchunk : 1;
-  return splits > 1 ? (size_t)splits * batch * M * N : 0;
-}
-
-// Host launcher.  kchunk > 0 splits K into chunks of kchunk rows (multiple of
-// BK), reduced by splitk_sum_kernel from `part` (part_floats() floats).
 template <bool TA, bool TB, class Epi>
 int gemm(const float* A, const float* B, float* C, int M, int N, int K, int lda, int ldb, int ldc,
          int64_t sA, int64_t sB, int64_t sC, int batch, Epi epi, int kchunk, float* part,
@@ -405,7 +481,7 @@ int gemm(const float* A, const float* B, float* C, int M, int N, int K, int lda,
     err = reinterpret_cast<unsigned*>(a);
   }
   p.err = err;
-  static bool attr_set = false;
+  static bool attr_set = false;  // one kernel per Epi, owned by this translation unit
   if (!attr_set) {
     cudaFuncSetAttribute(gemm_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSmemBytes);
@@ -423,3 +499,5 @@ int gemm(const float* A, const float* B, float* C, int M, int N, int K, int lda,
 
 }  // namespace tcg
 }  // namespace edg
+
+#endif  // EDG_GEMM_TC_IMPL
