@@ -8,16 +8,17 @@
 // (small terms first) accumulated in FP32 in tensor memory.
 //
 // Persistent kernel, one CTA per SM, 416 threads:
-//   warps 0-7   producers: global -> registers (float4), hi/lo split, st.shared
-//               into the canonical K-major no-swizzle layout of both operands
-//               (K-contiguous sources store one 16-byte core-matrix row per
-//               float4; MN-contiguous sources are transposed 4 x 4 in registers);
+//   warps 0-7   producers: cp.async of 16-byte chunks into a per-thread raw
+//               ring (3 stages in flight), then hi/lo split and st.shared into
+//               the canonical K-major no-swizzle layout of both operands
+//               (K-contiguous sources give one 16-byte core-matrix row per
+//               chunk; MN-contiguous sources are transposed 4 x 4 in registers);
 //   warps 8-11  epilogue: tcgen05.ld of the accumulator (row m = TMEM lane),
 //               epilogue functor, stores to C;
 //   warp 12     TMEM owner and MMA issuer (one elected lane).
-// Tiles are 128 (M) x 256 (N) x 16 (K) with 3 shared-memory stages and two
-// TMEM accumulators (2 x 256 columns), so the epilogue of one tile overlaps the
-// main loop of the next.  The core-matrix strides (LBO = 160 B between K groups,
+// Tiles are 128 (M) x 256 (N) x 16 (K) with 2 split (hi/lo) shared-memory
+// stages, 3 raw stages and two TMEM accumulators (2 x 256 columns), so the
+// epilogue of one tile overlaps the main loop of the next.  The core-matrix strides (LBO = 160 B between K groups,
 // SBO = 656 B between 8-row groups) make both producer store patterns free of
 // shared-memory bank conflicts.
 //
@@ -72,7 +73,7 @@ namespace tcg {
 
 using namespace ptx;
 
-constexpr int BM = 128, BN = 256, BK = 16, kStages = 3;
+constexpr int BM = 128, BN = 256, BK = 16, kStages = 2, kRaw = 3;
 constexpr int kProdWarps = 8, kEpiWarps = 4;
 constexpr int kProdThreads = kProdWarps * 32;
 constexpr int kThreads = (kProdWarps + kEpiWarps + 1) * 32;
@@ -81,8 +82,13 @@ constexpr uint32_t kLBO = 160, kSBO = 656;
 constexpr uint32_t kABytes = (BM / 8) * kSBO;  // one plane (hi or lo) of the A tile
 constexpr uint32_t kBBytes = (BN / 8) * kSBO;
 constexpr uint32_t kStageBytes = 2 * kABytes + 2 * kBBytes;
+// Raw (unsplit) copies in flight: per slot, 8 16-byte chunks per producer thread
+// ([chunk][thread], so that a warp's chunk i is one contiguous 512-byte run).
+constexpr uint32_t kRawSlot = 8u * kProdThreads * 16u;
+constexpr uint32_t kRawBase = kStages * kStageBytes;
+constexpr uint32_t kBarBase = kRawBase + kRaw * kRawSlot;
 constexpr uint32_t kTmemCols = 2 * BN;
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 256;
+constexpr size_t kSmemBytes = (size_t)kBarBase + 256;
 
 static_assert(kABytes % 16 == 0 && kBBytes % 16 == 0, "16-byte aligned planes");
 
@@ -118,70 +124,101 @@ struct Operand {
   bool vec;    // float4 loads allowed (16-byte aligned base, ld and batch stride)
 };
 
-// Loads a float4 along K (K-contiguous source) at (row, k..k+3), masked.
-__device__ __forceinline__ float4 load_k4(const Operand& o, const float* base, int row, int k,
-                                          int K) {
-  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (row >= o.rows || k >= K) return v;
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ float4 ld_shared4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+
+// 16 bytes of a K-contiguous source at (row, k .. k + 3) into dst; elements
+// outside the rows or beyond K are zero-filled.
+__device__ __forceinline__ void copy_k4(const Operand& o, const float* base, int row, int k, int K,
+                                        uint32_t dst) {
+  const int nv = row < o.rows ? max(0, min(4, K - k)) : 0;
   const float* q = base + (int64_t)row * o.ld + k;
-  if (o.vec && k + 3 < K) return __ldg(reinterpret_cast<const float4*>(q));
-  v.x = __ldg(q);
-  if (k + 1 < K) v.y = __ldg(q + 1);
-  if (k + 2 < K) v.z = __ldg(q + 2);
-  if (k + 3 < K) v.w = __ldg(q + 3);
-  return v;
-}
-
-// Loads a float4 along the row dimension (MN-contiguous source) at (row..row+3, k), masked.
-__device__ __forceinline__ float4 load_mn4(const Operand& o, const float* base, int row, int k,
-                                           int K) {
-  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (row >= o.rows || k >= K) return v;
-  const float* q = base + (int64_t)k * o.ld + row;
-  if (o.vec && row + 3 < o.rows) return __ldg(reinterpret_cast<const float4*>(q));
-  v.x = __ldg(q);
-  if (row + 1 < o.rows) v.y = __ldg(q + 1);
-  if (row + 2 < o.rows) v.z = __ldg(q + 2);
-  if (row + 3 < o.rows) v.w = __ldg(q + 3);
-  return v;
-}
-
-// One operand tile (R rows x BK) of one stage is fetched into four float4
-// registers per producer thread and then split and stored, so that the
-// global loads of the next stage are in flight while this one is stored.
-// K-contiguous source: float4 chunk c = tp + 256 i holds row c / 4, K group c % 4.
-// MN-contiguous source: task tp (< R) loads the 4 x 4 block of rows
-// 4 (tp % (R / 4)) .. + 3 and K group tp / (R / 4), transposed when stored.
-template <int R>
-__device__ __forceinline__ void fetch_tile(const Operand& o, const float* base, int r0, int k0,
-                                           int K, int tp, float4 (&r)[4]) {
-  if (o.kcontig) {
-    constexpr int kPer = R * BK / 4 / kProdThreads;  // 2 (R = 128) or 4 (R = 256)
+  if (o.vec) {
+    cp_async16(dst, nv ? q : base, 4u * nv);
+  } else {
 #pragma unroll
-    for (int i = 0; i < kPer; ++i) {
-      const int c = tp + i * kProdThreads;
-      r[i] = load_k4(o, base, r0 + (c >> 2), k0 + 4 * (c & 3), K);
-    }
-  } else if (tp < R) {
-    const int rg = tp % (R / 4), kg = tp / (R / 4);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) r[j] = load_mn4(o, base, r0 + 4 * rg, k0 + 4 * kg + j, K);
+    for (int e = 0; e < 4; ++e) cp_async4(dst + 4 * e, e < nv ? q + e : base, e < nv ? 4u : 0u);
   }
 }
 
+// 16 bytes of an MN-contiguous source at (rows row .. row + 3, k) into dst.
+__device__ __forceinline__ void copy_mn4(const Operand& o, const float* base, int row, int k, int K,
+                                         uint32_t dst) {
+  const int nr = k < K ? max(0, min(4, o.rows - row)) : 0;
+  const float* q = base + (int64_t)k * o.ld + row;
+  if (o.vec) {
+    cp_async16(dst, nr ? q : base, 4u * nr);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) cp_async4(dst + 4 * e, e < nr ? q + e : base, e < nr ? 4u : 0u);
+  }
+}
+
+// Raw copy of one operand tile (R rows x BK) of one stage: this thread's chunks
+// go to raw + (c0 + i) * kProdThreads * 16 + tp * 16.
+// K-contiguous source: chunk i is float4 number tp + 256 i (row / 4, K group % 4).
+// MN-contiguous source: thread tp < R owns the 4 x 4 block of rows
+// 4 (tp % (R / 4)) .. + 3 and K group tp / (R / 4); chunk j = K row j of it.
 template <int R>
-__device__ __forceinline__ void put_tile(const Operand& o, int tp, const float4 (&r)[4],
-                                         uint32_t hi, uint32_t lo) {
+__device__ __forceinline__ void fetch_tile(const Operand& o, const float* base, int r0, int k0,
+                                           int K, int tp, uint32_t raw, int c0) {
   if (o.kcontig) {
     constexpr int kPer = R * BK / 4 / kProdThreads;
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
       const int c = tp + i * kProdThreads;
-      const uint32_t off = soff(c >> 2, 4 * (c & 3));
-      st_split4(hi + off, lo + off, r[i]);
+      copy_k4(o, base, r0 + (c >> 2), k0 + 4 * (c & 3), K,
+              raw + (uint32_t)((c0 + i) * kProdThreads + tp) * 16u);
     }
   } else if (tp < R) {
     const int rg = tp % (R / 4), kg = tp / (R / 4);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      copy_mn4(o, base, r0 + 4 * rg, k0 + 4 * kg + j, K,
+               raw + (uint32_t)((c0 + j) * kProdThreads + tp) * 16u);
+  }
+}
+
+// Splits this thread's raw chunks of one operand tile into the hi / lo planes.
+template <int R>
+__device__ __forceinline__ void convert_tile(const Operand& o, int tp, uint32_t raw, int c0,
+                                             uint32_t hi, uint32_t lo) {
+  if (o.kcontig) {
+    constexpr int kPer = R * BK / 4 / kProdThreads;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int c = tp + i * kProdThreads;
+      const float4 v = ld_shared4(raw + (uint32_t)((c0 + i) * kProdThreads + tp) * 16u);
+      const uint32_t off = soff(c >> 2, 4 * (c & 3));
+      st_split4(hi + off, lo + off, v);
+    }
+  } else if (tp < R) {
+    const int rg = tp % (R / 4), kg = tp / (R / 4);
+    float4 r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      r[j] = ld_shared4(raw + (uint32_t)((c0 + j) * kProdThreads + tp) * 16u);
     const int row = 4 * rg;
     st_split4(hi + soff(row + 0, 4 * kg), lo + soff(row + 0, 4 * kg),
               make_float4(r[0].x, r[1].x, r[2].x, r[3].x));
@@ -226,14 +263,14 @@ template <class Epi>
 __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const uint32_t sbase = smem_u32(smem);
-  const uint32_t bar0 = sbase + kStages * kStageBytes;
+  const uint32_t bar0 = sbase + kBarBase;
   // barriers: full[kStages], empty[kStages], accfull[2], accempty[2], drain
   auto full = [&](int s) { return bar0 + 8u * s; };
   auto empty = [&](int s) { return bar0 + 8u * (kStages + s); };
   auto accfull = [&](int i) { return bar0 + 8u * (2 * kStages + i); };
   auto accempty = [&](int i) { return bar0 + 8u * (2 * kStages + 2 + i); };
   const uint32_t drain = bar0 + 8u * (2 * kStages + 4);
-  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(smem + kStages * kStageBytes + 128);
+  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(smem + kBarBase + 128);
   __shared__ volatile int s_err;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -252,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
   }
   if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     sbase + kStages * kStageBytes + 128),
+                     sbase + kBarBase + 128),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -264,16 +301,21 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
 
   if (warp < kProdWarps) {
     // ---------------------------------------------------------------- producers
-    // Stages are produced in one flat sequence over this CTA's tiles; the
-    // loads of stage i + 1 are issued before stage i is stored.
+    // Stages form one flat sequence over this CTA's tiles.  Each thread keeps
+    // kRaw - 1 stages of its own raw 16-byte chunks in flight (cp.async), and
+    // converts a stage once its own copies have landed -- no barrier between
+    // copy and conversion, since every thread converts exactly what it copied.
     const int tp = threadIdx.x;
     struct Job {
       int64_t t;
       int kt, nk, kb, ke, r0a, r0b;
       const float* Ab;
       const float* Bb;
+      bool valid;
     };
-    auto make_job = [&](int64_t t, Job& j) {
+    auto start_tile = [&](int64_t t, Job& j) {
+      j.valid = t < p.total;
+      if (!j.valid) return;
       const Tile x = tile_of(p, t);
       j.t = t;
       j.kt = 0;
@@ -285,44 +327,35 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
       j.Ab = p.A.p + x.b * p.A.sb;
       j.Bb = p.B.p + x.b * p.B.sb;
     };
-    float4 ca[4], cb[4], na[4], nb[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) ca[i] = cb[i] = na[i] = nb[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    Job cur;
-    bool have = blockIdx.x < p.total;
-    if (have) {
-      make_job(blockIdx.x, cur);
-      fetch_tile<BM>(p.A, cur.Ab, cur.r0a, cur.kb, cur.ke, tp, ca);
-      fetch_tile<BN>(p.B, cur.Bb, cur.r0b, cur.kb, cur.ke, tp, cb);
-    }
-    for (uint32_t it = 0; have && !s_err; ++it) {
-      Job nxt = cur;
-      bool have_next = true;
-      if (++nxt.kt == cur.nk) {
-        const int64_t t2 = cur.t + gridDim.x;
-        have_next = t2 < p.total;
-        if (have_next) make_job(t2, nxt);
+    Job f;
+    start_tile(blockIdx.x, f);
+    uint32_t nfetched = 0;
+    auto fetch_next = [&]() {
+      if (f.valid) {
+        const uint32_t raw = sbase + kRawBase + (nfetched % kRaw) * kRawSlot;
+        const int k0 = f.kb + f.kt * BK;
+        fetch_tile<BM>(p.A, f.Ab, f.r0a, k0, f.ke, tp, raw, 0);
+        fetch_tile<BN>(p.B, f.Bb, f.r0b, k0, f.ke, tp, raw, 4);
+        ++nfetched;
+        if (++f.kt == f.nk) start_tile(f.t + gridDim.x, f);
       }
-      if (have_next) {
-        const int k0 = nxt.kb + nxt.kt * BK;
-        fetch_tile<BM>(p.A, nxt.Ab, nxt.r0a, k0, nxt.ke, tp, na);
-        fetch_tile<BN>(p.B, nxt.Bb, nxt.r0b, k0, nxt.ke, tp, nb);
-      }
-      const int s = (int)(it % kStages);
-      if (it >= (uint32_t)kStages) mbar_wait(empty(s), ((it / kStages) - 1) & 1, &s_err);
+      cp_async_commit();
+    };
+#pragma unroll 1
+    for (int i = 0; i < kRaw - 1; ++i) fetch_next();
+    for (uint32_t c = 0; c < nfetched && !s_err; ++c) {
+      fetch_next();
+      cp_async_wait<kRaw - 1>();
+      const int s = (int)(c % kStages);
+      if (c >= (uint32_t)kStages) mbar_wait(empty(s), ((c / kStages) - 1) & 1, &s_err);
+      const uint32_t raw = sbase + kRawBase + (c % kRaw) * kRawSlot;
       const uint32_t st = sbase + s * kStageBytes;
-      put_tile<BM>(p.A, tp, ca, st, st + kABytes);
-      put_tile<BN>(p.B, tp, cb, st + 2 * kABytes, st + 2 * kABytes + kBBytes);
+      convert_tile<BM>(p.A, tp, raw, 0, st, st + kABytes);
+      convert_tile<BN>(p.B, tp, raw, 4, st + 2 * kABytes, st + 2 * kABytes + kBBytes);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full(s));
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        ca[i] = na[i];
-        cb[i] = nb[i];
-      }
-      cur = nxt;
-      have = have_next;
     }
+    cp_async_wait<0>();
   } else if (warp == kMmaWarp) {
     // ---------------------------------------------------------------- MMA issuer
     constexpr uint32_t idesc = idesc_tf32(BM, BN);
