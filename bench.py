@@ -644,14 +644,15 @@ def run_sbn(args):
     inf._sbn.gather = False
     nq = (V + 1) * H0 + (H0 + 1) * H1
     gvar = {}
-    for mode, name in ((0, "none"), (1, "mean"), (2, "mlp")):
-        inf._cfg.baseline = mode
+    for mode, rb, name in ((0, 0, "none"), (0, 1, "rao_blackwell"), (1, 0, "mean"),
+                           (2, 0, "mlp")):
+        inf._cfg.baseline, inf._cfg.rao_blackwell = mode, rb
         gs = []
         for k in range(24):
             inf.seed = 7000 + k
             gs.append(inf.score_gradients()[1][:nq].double())
         gvar[name] = float(torch.stack(gs).var(dim=0).sum())
-    inf._cfg.baseline = 2
+    inf._cfg.baseline, inf._cfg.rao_blackwell = 2, 0
     # ELBO after equal training with the running-mean and the MLP baseline
     elbo = {}
     for name in ("mean", "mlp"):

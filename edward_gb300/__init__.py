@@ -16,5 +16,5 @@ from . import layers, models, train
 from .expr import (Variable, placeholder, dot, matmul, tanh, sigmoid, softplus, reshape, cast,
                    zeros, ones)
 from .inferences import (Inference, VariationalInference, KLqp, ReparameterizationKLqp,
-                         ReparameterizationKLKLqp, ScoreKLqp, MonteCarlo, HMC)
+                         ReparameterizationKLKLqp, ScoreKLqp, ScoreRBKLqp, MonteCarlo, HMC)
 from .util import set_seed, Progbar

@@ -71,7 +71,8 @@ class EdgBNN(ctypes.Structure):
 class EdgSBN(ctypes.Structure):
     _fields_ = [("V", c_int32), ("H0", c_int32), ("H1", c_int32), ("n_samples", c_int32),
                 ("baseline", c_int32), ("baseline_hidden", c_int32), ("baseline_decay", c_float),
-                ("gemm_engine", c_int32), ("seed", c_uint64)]
+                ("gemm_engine", c_int32), ("seed", c_uint64), ("rao_blackwell", c_int32),
+                ("reserved", c_int32)]
 
 
 class EdgHMC(ctypes.Structure):

@@ -43,7 +43,7 @@ constexpr int kT = 256;
 constexpr int kMaxSplits = 32;
 
 struct Dims {
-  int V, H0, H1, S, B, R, BH, mode, engine;
+  int V, H0, H1, S, B, R, BH, mode, engine, rb;
   int ldx, ld0, ld1, ldh, H0p;
   int64_t oq0, oq1, op1, op0, P;  // model parameter blocks
   int64_t ob1, PB;                // baseline: Wb0 block at 0, Wb1 block at ob1
@@ -60,6 +60,7 @@ static Dims make_dims(const edg_sbn_t* c, int B) {
   d.BH = c->baseline_hidden;
   d.mode = c->baseline;
   d.engine = c->gemm_engine;
+  d.rb = c->rao_blackwell;
   d.ldx = round_up(d.V + 1, 4);
   d.ld0 = round_up(d.H0 + 1, 4);
   d.ld1 = round_up(d.H1 + 1, 4);
@@ -194,7 +195,8 @@ __global__ void mlp_out_kernel(Dims d, float* __restrict__ Hb, const float* __re
   }
 }
 
-// f[s,b] = log p(z1) + log p(z0|z1) + log p(x|z0) - log q(z0|x) - log q(z1|z0); F_s = sum_b.
+// f[s,b] = log p(z1) + log p(z0|z1) + log p(x|z0) - log q(z0|x) - log q(z1|z0);
+// Fs[s] = sum_b f[s,b] and Fs[S + s] = sum_b log p(x_b | z0_sb).
 __global__ void __launch_bounds__(kT) signal_kernel(Dims d, const float* __restrict__ terms,
                                                     float* __restrict__ f, double* __restrict__ Fs) {
   __shared__ double red[kT / 32];
@@ -204,35 +206,50 @@ __global__ void __launch_bounds__(kT) signal_kernel(Dims d, const float* __restr
   const float* lp1 = terms + 2 * (int64_t)d.R;
   const float* lp0 = terms + 3 * (int64_t)d.R;
   const float* lx = terms + 4 * (int64_t)d.R;
-  double acc = 0.0;
+  __shared__ double redx[kT / 32];
+  double acc = 0.0, accx = 0.0;
   for (int b = threadIdx.x; b < d.B; b += kT) {
     const int r = s * d.B + b;
     const float v = (lp1[r] + lp0[r] + lx[r]) - (lq0[r] + lq1[r]);
     f[r] = v;
     acc += v;
+    accx += lx[r];
   }
   acc = warp_sum_d(acc);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  accx = warp_sum_d(accx);
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = acc;
+    redx[threadIdx.x >> 5] = accx;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kT / 32; ++w) t += red[w];
+    double t = 0.0, tx = 0.0;
+    for (int w = 0; w < kT / 32; ++w) {
+      t += red[w];
+      tx += redx[w];
+    }
     Fs[s] = t;
+    Fs[d.S + s] = tx;
   }
 }
 
-// Learning signal of sample row r.
+// Learning signal of sample row r for the parameters of q(z0 | x) (layer 0) or
+// q(z1 | z0) (layer 1).  Rao-Blackwellised (ScoreRBKLqp, klqp.py:1110-1139): the
+// signal of a q factor keeps the log densities in the Markov blanket of its
+// latent layer -- everything for q(z0 | x), everything but log p(x | z0) for
+// q(z1 | z0).
 __device__ __forceinline__ float signal_of(const Dims& d, int r, const float* f, const double* Fs,
-                                           const float* stats, const float* mlp_out) {
+                                           const float* stats, const float* mlp_out, int layer) {
   const int s = r / d.B, b = r % d.B;
-  if (d.mode == EDG_BASELINE_NONE) return (float)Fs[s];
+  if (d.mode == EDG_BASELINE_NONE)
+    return (d.rb && layer == 1) ? (float)(Fs[s] - Fs[d.S + s]) : (float)Fs[s];
   if (stats[ST_COUNT] <= 0.0f) return f[r];
   const float base = d.mode == EDG_BASELINE_MEAN ? stats[ST_C]
                                                  : stats[ST_C] + stats[ST_SIGMA] * mlp_out[b];
   return f[r] - base;
 }
 
-// Lq1[r] *= A(r);  R0q[b][j] = sum_s A(s B + b) R0[s B + b][j];  A_out[r] = A(r).
+// Lq1[r] *= A1(r);  R0q[b][j] = sum_s A0(s B + b) R0[s B + b][j];  A_out[r] = A0(r).
 __global__ void scale_kernel(Dims d, const float* __restrict__ f, const double* __restrict__ Fs,
                              const float* __restrict__ stats, const float* __restrict__ mlp_out,
                              float* __restrict__ Lq1, const float* __restrict__ R0,
@@ -242,16 +259,15 @@ __global__ void scale_kernel(Dims d, const float* __restrict__ f, const double* 
        i += (int64_t)gridDim.x * kT) {
     if (i < n1) {
       const int r = (int)(i / d.H1);
-      const float A = signal_of(d, r, f, Fs, stats, mlp_out);
-      Lq1[i] *= A;
-      if (A_out && i % d.H1 == 0) A_out[r] = A;
+      Lq1[i] *= signal_of(d, r, f, Fs, stats, mlp_out, 1);
+      if (A_out && i % d.H1 == 0) A_out[r] = signal_of(d, r, f, Fs, stats, mlp_out, 0);
     } else {
       const int64_t e = i - n1;
       const int b = (int)(e / d.H0), j = (int)(e % d.H0);
       float acc = 0.0f;
       for (int s = 0; s < d.S; ++s) {
         const int r = s * d.B + b;
-        acc = fmaf(signal_of(d, r, f, Fs, stats, mlp_out), R0[(int64_t)r * d.H0 + j], acc);
+        acc = fmaf(signal_of(d, r, f, Fs, stats, mlp_out, 0), R0[(int64_t)r * d.H0 + j], acc);
       }
       R0q[e] = acc;
     }
@@ -518,7 +534,7 @@ static size_t carve(const Dims& d, int sms, void* base, Workspace* w) {
       take(B * d.H0 * 4),    take(5 * R * 4),    take(R * 4),
       take(mlp ? B * d.ldh * 4 : 0), take(B * 4), take(B * 4), take(mlp ? B * d.BH * 4 : 0),
       take(d.P * 4),         take(mlp ? d.PB * 4 : 0), take(part * 4),
-      take(d.S * 8),         take((size_t)nb * 3 * 8), take(64)};
+      take(2 * d.S * 8),         take((size_t)nb * 3 * 8), take(64)};
   if (w && base) {
     char* c = reinterpret_cast<char*>(base);
     float** fp[] = {&w->Xa, &w->Xc, &w->Lq0, &w->Z0a, &w->Z1a, &w->R0, &w->Lq1, &w->Lp1,
@@ -548,6 +564,8 @@ static int check_cfg(const edg_sbn_t* c, int B) {
               "baseline_decay must be in [0, 1)");
   EDG_REQUIRE(c->gemm_engine == EDG_GEMM_TC || c->gemm_engine == EDG_GEMM_SIMT, EDG_E_VALUE,
               "unknown gemm_engine %d", c->gemm_engine);
+  EDG_REQUIRE(!c->rao_blackwell || c->baseline == EDG_BASELINE_NONE, EDG_E_UNSUPPORTED,
+              "the Rao-Blackwellised estimator takes no baseline");
   EDG_REQUIRE((int64_t)c->n_samples * B * std::max(c->V, std::max(c->H0, c->H1)) < (1ll << 31),
               EDG_E_SHAPE, "problem too large");
   return EDG_OK;

@@ -21,6 +21,7 @@ from .variational_inference import VariationalInference
 _CONTINUOUS = ("01", "nonnegative", "simplex", "real", "multivariate_real")
 
 AUTO, REPARAM_KL, REPARAM, SCORE = None, _lib.KLQP_REPARAM_KL, _lib.KLQP_REPARAM, _lib.KLQP_SCORE
+SCORE_RB = "score_rb"
 
 
 class KLqp(VariationalInference):
@@ -77,22 +78,27 @@ class KLqp(VariationalInference):
             return self._method
         if is_reparameterizable:
             return REPARAM_KL if is_analytic_kl else REPARAM
-        return "score_rb"
+        return SCORE_RB
 
     def _validate(self):
         method = self._choose_method()
-        if method == "score_rb":
-            raise NotImplementedError(
-                "Rao-Blackwellised score gradients (ScoreRBKLqp) are not implemented; "
-                "use ed.ScoreKLqp for models with discrete latent variables")
-        self._method_id = method
         latents = list(self.latent_vars.keys())
-        if method == SCORE and all(not q.reparameterizable for q in self.latent_vars.values()):
+        discrete = all(not q.reparameterizable for q in self.latent_vars.values())
+        self._rao_blackwell = method == SCORE_RB
+        if method == SCORE_RB and not discrete:
+            raise NotImplementedError(
+                "Rao-Blackwellised score gradients are implemented for the sigmoid belief "
+                "network family")
+        self._method_id = SCORE if method == SCORE_RB else method
+        if self._method_id == SCORE and discrete:
             self._spec = compile_sbn(self.latent_vars, self.data)
             self._family = "sbn"
             if self.kl_scaling or self.scale:
                 raise NotImplementedError("scale / kl_scaling for the sigmoid belief network")
+            if self._rao_blackwell and getattr(self, "baseline", "none") != "none":
+                raise NotImplementedError("ScoreRBKLqp takes no baseline")
             return
+        method = self._method_id
         try:
             self._spec = compile_glm(latents, self.data)
             self._family = "glm"
@@ -220,6 +226,10 @@ class KLqp(VariationalInference):
         self._sbn = SBNDevice(spec, dev, self.n_minibatch)
         self._sbn.seed = next_seed()
         self._prior = torch.as_tensor(spec.prior_logits, device=dev)
+        from .. import train
+        if not hasattr(self, "baseline"):        # KLqp / ScoreRBKLqp: no control variate
+            self.baseline, self.baseline_hidden, self.baseline_decay = "none", 1, 0.9
+            self.baseline_optimizer = train.AdamOptimizer(1e-2)
         mode = {"none": _lib.BASELINE_NONE, "mean": _lib.BASELINE_MEAN,
                 "mlp": _lib.BASELINE_MLP}[self.baseline]
         cfg = _lib.EdgSBN()
@@ -227,6 +237,7 @@ class KLqp(VariationalInference):
         cfg.baseline, cfg.baseline_hidden = mode, self.baseline_hidden
         cfg.baseline_decay = self.baseline_decay
         cfg.gemm_engine = self.gemm_engine
+        cfg.rao_blackwell = 1 if self._rao_blackwell else 0
         cfg.seed = next_seed()
         self._cfg = cfg
         self._opt = self.optimizer.to_c()
@@ -315,6 +326,26 @@ class KLqp(VariationalInference):
         g = self._grad.detach().clone()
         return float(st.loss), g[:P], g[P:]
 
+    def score_gradients(self, z=None, signal=False):
+        """(loss, grad [P]) at the current parameters without applying the
+        optimizer (sigmoid belief network); ``z`` = (z0 [S, B, H0], z1 [S, B, H1])
+        overrides the draws; ``signal=True`` also returns f [S, B] and the
+        learning signal [S, B]."""
+        if self._family != "sbn":
+            raise NotImplementedError("score_gradients is for the sigmoid belief network")
+        zo = None
+        if z is not None:
+            zo = torch.cat([torch.as_tensor(np.asarray(a, np.float32)).reshape(-1) for a in z])
+            zo = zo.to(self._device)
+        S, B = self.n_samples, self._sbn.B
+        sig = torch.empty(2 * S * B, dtype=torch.float32, device=self._device) if signal else None
+        self._step(apply=False, eps=zo, grad_out=self._grad, signal_out=sig)
+        st = self._read_state()
+        out = (float(st.loss), self._grad.detach().clone())
+        if signal:
+            out += (sig[:S * B].view(S, B).clone(), sig[S * B:].view(S, B).clone())
+        return out
+
     @property
     def seed(self):
         return int(self._cfg.seed)
@@ -366,22 +397,11 @@ class ScoreKLqp(KLqp):
         if self._family != "sbn" and self.baseline != "none":
             raise NotImplementedError("baselines are implemented for the sigmoid belief network")
 
-    def score_gradients(self, z=None, signal=False):
-        """(loss, grad [P]) at the current parameters without applying the
-        optimizer (sigmoid belief network); ``z`` = (z0 [S, B, H0], z1 [S, B, H1])
-        overrides the draws; ``signal=True`` also returns f [S, B] and the
-        learning signal [S, B]."""
-        if self._family != "sbn":
-            raise NotImplementedError("score_gradients is for the sigmoid belief network")
-        zo = None
-        if z is not None:
-            zo = torch.cat([torch.as_tensor(np.asarray(a, np.float32)).reshape(-1) for a in z])
-            zo = zo.to(self._device)
-        S, B = self.n_samples, self._sbn.B
-        sig = torch.empty(2 * S * B, dtype=torch.float32, device=self._device) if signal else None
-        self._step(apply=False, eps=zo, grad_out=self._grad, signal_out=sig)
-        st = self._read_state()
-        out = (float(st.loss), self._grad.detach().clone())
-        if signal:
-            out += (sig[:S * B].view(S, B).clone(), sig[S * B:].view(S, B).clone())
-        return out
+
+class ScoreRBKLqp(KLqp):
+    """Score-function gradient with Rao-Blackwellisation across stochastic nodes
+    (``klqp.py:572-639``, ``build_score_rb_loss_and_gradients`` 1058-1152): each
+    variational factor's learning signal keeps only the log densities in the
+    Markov blanket of its latent variable.  ``ed.KLqp`` dispatches here for
+    non-reparameterisable (discrete) latent variables (``klqp.py:153-163``)."""
+    _method = SCORE_RB

@@ -291,6 +291,11 @@ typedef struct {
   float baseline_decay;    /* decay of the running mean / scale, in [0, 1) */
   int32_t gemm_engine;     /* EDG_GEMM_TC (default) or EDG_GEMM_SIMT */
   uint64_t seed;
+  int32_t rao_blackwell;   /* 1: ScoreRBKLqp (build_score_rb_loss_and_gradients,
+                              klqp.py:1058-1152): q(z1 | z0)'s signal drops log p(x | z0),
+                              the one density outside its Markov blanket; baseline must be
+                              EDG_BASELINE_NONE */
+  int32_t reserved;
 } edg_sbn_t;
 
 int32_t edg_sbn_num_params(int32_t V, int32_t H0, int32_t H1);

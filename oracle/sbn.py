@@ -90,10 +90,14 @@ def mlp_forward(bparams, X, V, BH):
 
 
 def score_step(theta, X, prior_logits, z0, z1, V, H0, H1, mode=NONE, stats=None,
-               bparams=None, BH=0):
+               bparams=None, BH=0, rb=False):
     """One score-function gradient at fixed draws.  Returns a dict with loss,
-    grad [P] (w.r.t. theta), f [S, B], A [S, B] (the learning signal used),
-    F [S] and (MLP mode) Hb, mlp_out."""
+    grad [P] (w.r.t. theta), f [S, B], A [S, B] (the learning signal used for
+    q(z0 | x)), F [S] and (MLP mode) Hb, mlp_out.  ``rb``: the Rao-Blackwellised
+    estimator of ``build_score_rb_loss_and_gradients`` (``klqp.py:1058-1152``):
+    the Markov blanket of z1 in p is {z1, z0} and in q {qz1, qz0}, so q(z1 | z0)'s
+    signal is F_s - sum_b log p(x_b | z0_sb); q(z0 | x)'s blanket covers every
+    factor (q(z1 | z0) descends from its parameters), so its signal stays F_s."""
     theta = np.asarray(theta, np.float64)
     X = np.asarray(X, np.float64)
     pl = np.asarray(prior_logits, np.float64)
@@ -132,8 +136,13 @@ def score_step(theta, X, prior_logits, z0, z1, V, H0, H1, mode=NONE, stats=None,
         Hb, o = mlp_forward(bparams, X, V, BH)
         out.update(Hb=Hb, mlp_out=o)
     out["A"] = np.array(A)
+    A1 = A
+    if rb:
+        if mode != NONE:
+            raise ValueError("the Rao-Blackwellised estimator takes no baseline")
+        A1 = np.broadcast_to((F - lx.sum(axis=1))[:, None], f.shape)
     gq0 = Xa.T @ (A[..., None] * R0).sum(axis=0)
-    gq1 = np.einsum("sbi,sbj->ij", Z0a, A[..., None] * R1)
+    gq1 = np.einsum("sbi,sbj->ij", Z0a, A1[..., None] * R1)
     gp1 = np.einsum("sbi,sbj->ij", Z1a, Rp1)
     gp0 = np.einsum("sbi,sbj->ij", Z0a, Rx)
     out["grad"] = -np.concatenate([g.reshape(-1) for g in (gq0, gq1, gp1, gp0)]) / S

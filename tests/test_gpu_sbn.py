@@ -59,6 +59,31 @@ def test_sbn_score_gradient_parity_given_draws(cuda, V, H0, H1, B, S, baseline, 
     close(g.cpu().numpy(), ref["grad"], 2e-5)
 
 
+@pytest.mark.parametrize("V,H0,H1,B,S", [(20, 12, 8, 16, 3), (784, 200, 200, 64, 4),
+                                          (50, 20, 10, 512, 4)])
+@pytest.mark.parametrize("engine", ["tc", "simt"])
+def test_sbn_rao_blackwell_parity_given_draws(cuda, V, H0, H1, B, S, engine):
+    """ed.KLqp on the network dispatches to the Rao-Blackwellised score
+    estimator (klqp.py:153-163, 1058-1152); gradients against the oracle."""
+    import edward_gb300 as ed
+    from sbn_model import example_sbn, flat_theta
+    ed.set_seed(0)
+    lv, xr, x_ph, weights = example_sbn(V, H0, H1, B, prior_logit=0.2)
+    rng = np.random.default_rng(0)
+    for w in weights:
+        w.assign(w.numpy() + rng.standard_normal(w.shape).astype(np.float32) * 0.3)
+    inf = ed.KLqp(lv, data={xr: x_ph})
+    inf.initialize(n_samples=S, n_print=0, gemm_engine=engine)
+    X = (rng.random((B, V)) < 0.4).astype(np.float32)
+    inf._feed({x_ph: X})
+    z0, z1 = _draws(np.random.default_rng(3), S, B, H0, H1)
+    loss, g = inf.score_gradients(z=(z0, z1))
+    ref = sbn.score_step(flat_theta(weights), X, np.full(H1, 0.2), z0.astype(np.float64),
+                         z1.astype(np.float64), V, H0, H1, rb=True)
+    assert abs(loss - ref["loss"]) <= 1e-5 * abs(ref["loss"])
+    close(g.cpu().numpy(), ref["grad"], 2e-5)
+
+
 def test_sbn_philox_draws_follow_the_bernoulli_rule(cuda):
     """Without overrides z = u < sigmoid(logit) with u from Philox stream 3;
     the oracle repeats the draw (no u within 1e-5 of its threshold here)."""

@@ -284,12 +284,16 @@ def test_compile_sbn_rejects_other_networks():
 
 
 def test_sbn_dispatch_on_host():
-    """KLqp on discrete latents wants ScoreRBKLqp (not implemented: says so);
-    ScoreKLqp compiles the network and then needs the GPU."""
+    """KLqp on discrete latents dispatches to the Rao-Blackwellised score
+    estimator (klqp.py:153-163), ScoreKLqp to the plain one; both compile the
+    network on the host and then need the GPU."""
     from sbn_model import example_sbn
     lv, xr, x_ph, _ = example_sbn(6, 3, 2, 4)
-    with pytest.raises(NotImplementedError, match="ScoreKLqp"):
-        ed.KLqp(lv, data={xr: x_ph}).initialize()
+    for cls in (ed.KLqp, ed.ScoreRBKLqp):
+        inf = cls(lv, data={xr: x_ph})
+        with pytest.raises(RuntimeError):
+            inf.initialize(n_samples=2)
+        assert inf._family == "sbn" and inf._rao_blackwell
     inf = ed.ScoreKLqp(lv, data={xr: x_ph})
     with pytest.raises(ValueError):
         inf.initialize(baseline="median")

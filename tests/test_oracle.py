@@ -199,6 +199,37 @@ def test_sbn_score_gradient_matches_finite_differences():
             assert abs(fd - out["grad"][p]) <= 1e-6 * max(1.0, abs(fd))
 
 
+def test_sbn_rao_blackwell_gradient():
+    """ScoreRB (klqp.py:1110-1139): q(z1 | z0)'s surrogate weights its log
+    density by F_s - sum_b log p(x_b | z0) (its Markov blanket); q(z0 | x)'s and
+    the model's gradients are those of the plain estimator."""
+    from oracle import sbn
+    V, H0, H1, S = 3, 2, 2, 3
+    rng, th, X, pl = _tiny_sbn(4)
+    z0, z1, _ = sbn.sample_z(th, X, rng.random((S, 2, H0)), rng.random((S, 2, H1)), V, H0, H1)
+    plain = sbn.score_step(th, X, pl, z0, z1, V, H0, H1)
+    rb = sbn.score_step(th, X, pl, z0, z1, V, H0, H1, rb=True)
+    nq0 = (V + 1) * H0
+    nq = nq0 + (H0 + 1) * H1
+    np.testing.assert_allclose(rb["grad"][:nq0], plain["grad"][:nq0])
+    np.testing.assert_allclose(rb["grad"][nq:], plain["grad"][nq:])
+    Wq0, Wq1, Wp1, Wp0 = sbn.unpack(th, V, H0, H1)
+    lx = sbn.bern_logp(X[None], sbn.aug(z0) @ Wp0).sum(-1).sum(-1)
+    A1 = plain["F"] - lx
+
+    def surrogate(t):
+        W1 = sbn.unpack(t, V, H0, H1)[1]
+        lq1 = sbn.bern_logp(z1, sbn.aug(z0) @ W1).sum(-1).sum(-1)
+        return -(lq1 * A1).sum() / S
+
+    for p in range(nq0, nq):
+        a, b = th.copy(), th.copy()
+        a[p] += 1e-6
+        b[p] -= 1e-6
+        fd = (surrogate(a) - surrogate(b)) / 2e-6
+        assert abs(fd - rb["grad"][p]) <= 1e-6 * max(1.0, abs(fd))
+
+
 def test_sbn_estimators_are_unbiased_against_exact_enumeration():
     """The reference estimator and both per-row baselines average to the
     exact ELBO gradient (enumeration over every z) within Monte Carlo error,
@@ -211,14 +242,18 @@ def test_sbn_estimators_are_unbiased_against_exact_enumeration():
     z0, z1, _ = sbn.sample_z(th, X, rng.random((n, B, H0)), rng.random((n, B, H1)), V, H0, H1)
     bp = rng.standard_normal(sbn.n_baseline_params(V, BH)) * 0.3
     var = {}
-    for mode, stats in ((sbn.NONE, None), (sbn.MEAN, np.array([-5.0, 1, 3, .9, .999, 0, 0, 0])),
-                        (sbn.MLP, np.array([-5.0, 2.0, 3, .9, .999, 0, 0, 0]))):
+    for mode, stats, rb in ((sbn.NONE, None, False),
+                            (sbn.MEAN, np.array([-5.0, 1, 3, .9, .999, 0, 0, 0]), False),
+                            (sbn.MLP, np.array([-5.0, 2.0, 3, .9, .999, 0, 0, 0]), False),
+                            (sbn.NONE, None, True)):
         gs = np.array([sbn.score_step(th, X, pl, z0[k::nb], z1[k::nb], V, H0, H1, mode=mode,
-                                      stats=stats, bparams=bp, BH=BH)["grad"] for k in range(nb)])
+                                      stats=stats, bparams=bp, BH=BH, rb=rb)["grad"]
+                       for k in range(nb)])
         se = gs.std(axis=0) / np.sqrt(nb)
         assert np.all(np.abs(gs.mean(axis=0) - g_exact) < 5 * se + 1e-9)
-        var[mode] = gs.var(axis=0).sum()
-    assert var[sbn.MEAN] < var[sbn.NONE]
+        var[(mode, rb)] = gs.var(axis=0).sum()
+    assert var[(sbn.MEAN, False)] < var[(sbn.NONE, False)]
+    assert var[(sbn.NONE, True)] <= var[(sbn.NONE, False)]
 
 
 def test_sbn_baseline_regression_gradient():
