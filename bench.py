@@ -688,6 +688,51 @@ def run_sbn(args):
     return 0
 
 
+def run_sgld(args):
+    """SGLD (edward/inferences/sgld.py) on the 10,000 x 50 logistic regression with
+    4,096 chains: one batched log-joint gradient + update per iteration."""
+    import numpy as np
+    import torch
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Empirical, Normal
+    X, y, _ = make_data()
+    C = 4096
+    w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
+    b = Normal(loc=0.0, scale=1.0)
+    yv = Bernoulli(logits=ed.dot(X, w) + b)
+    T = args.steps + args.warmup
+    qw = Empirical(ed.Variable(np.zeros((T, C, N_FEAT), np.float32)), n_chains=C)
+    qb = Empirical(ed.Variable(np.zeros((T, C), np.float32)), n_chains=C)
+    inf = ed.SGLD({w: qw, b: qb}, data={yv: y}, n_chains=C)
+    inf.initialize(step_size=1e-4, n_print=0)
+    inf.run_iterations(args.warmup)
+    torch.cuda.synchronize()
+    a, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        a.record()
+        inf.run_iterations(args.steps)
+        b2.record()
+        b2.synchronize()
+    ms = a.elapsed_time(b2) / args.steps
+    P = N_FEAT + 1
+    flops = 4.0 * N_ROWS * P * C
+    line = {"metric": "SGLD chain-iterations/s (Bayesian logistic regression, batched chains)",
+            "value": C / (ms / 1e3), "unit": "chain-iterations/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "sgld_logreg_N10000_D50_C4096", "chains": C,
+                       "l2_flush": "none (X is 2 MB, L2-resident)"},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "fp32", "achieved": flops / (ms / 1e3) / 1e12,
+                         "unit": "TFLOP/s", "traffic": None, "peak": None,
+                         "kernel": "glm_partial_kernel + glm_reduce_kernel + sgmcmc update (SIMT)",
+                         "algorithmic_flops_per_step": flops},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -700,7 +745,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--hier-instances", type=int, default=2048)
     ap.add_argument("--sbn-compare-steps", type=int, default=1000)
-    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn"],
+    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn", "sgld"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -715,6 +760,8 @@ def main():
         return run_bnn(args)
     if args.workload == "sbn":
         return run_sbn(args)
+    if args.workload == "sgld":
+        return run_sgld(args)
     return run_gpu(args)
 
 

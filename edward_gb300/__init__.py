@@ -16,5 +16,6 @@ from . import layers, models, train
 from .expr import (Variable, placeholder, dot, matmul, tanh, sigmoid, softplus, reshape, cast,
                    zeros, ones)
 from .inferences import (Inference, VariationalInference, KLqp, ReparameterizationKLqp,
-                         ReparameterizationKLKLqp, ScoreKLqp, ScoreRBKLqp, MonteCarlo, HMC)
+                         ReparameterizationKLKLqp, ScoreKLqp, ScoreRBKLqp, MonteCarlo, HMC,
+                         SGLD, SGHMC)
 from .util import set_seed, Progbar

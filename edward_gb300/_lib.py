@@ -29,6 +29,7 @@ LIK_BERNOULLI, LIK_NORMAL = 0, 1
 KLQP_REPARAM_KL, KLQP_REPARAM, KLQP_SCORE = 0, 1, 2
 BASELINE_NONE, BASELINE_MEAN, BASELINE_MLP = 0, 1, 2
 GEMM_TC, GEMM_SIMT = 0, 1
+SGMCMC_SGLD, SGMCMC_SGHMC = 0, 1
 OPT_ADAM, OPT_SGD, OPT_MOMENTUM, OPT_ADAGRAD, OPT_RMSPROP, OPT_ADADELTA = range(6)
 
 
@@ -73,6 +74,11 @@ class EdgSBN(ctypes.Structure):
                 ("baseline", c_int32), ("baseline_hidden", c_int32), ("baseline_decay", c_float),
                 ("gemm_engine", c_int32), ("seed", c_uint64), ("rao_blackwell", c_int32),
                 ("reserved", c_int32)]
+
+
+class EdgSGMCMC(ctypes.Structure):
+    _fields_ = [("method", c_int32), ("step_size", c_float), ("friction", c_float),
+                ("data_scale", c_float), ("seed", c_uint64)]
 
 
 class EdgHMC(ctypes.Structure):
@@ -129,6 +135,10 @@ _SIGS = {
                                      c_void_p]),
     "edg_minibatch_gather_u8": (c_int32, [c_void_p, c_int64, c_int32, c_int32, c_uint64, c_void_p,
                                           c_void_p, c_void_p]),
+    "edg_sgmcmc_glm_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgGLM), c_int32]),
+    "edg_sgmcmc_glm_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgSGMCMC), c_int32,
+                                     c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_int64, c_void_p, c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

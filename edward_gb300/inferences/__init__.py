@@ -5,3 +5,4 @@ from .klqp import (KLqp, ReparameterizationKLqp, ReparameterizationKLKLqp, Score
                    ScoreRBKLqp)
 from .monte_carlo import MonteCarlo
 from .hmc import HMC
+from .sgmcmc import SGLD, SGHMC

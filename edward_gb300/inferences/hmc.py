@@ -70,23 +70,9 @@ class HMC(MonteCarlo):
             return self._build_hier()
         spec = self._spec
         self._glm = GLMDevice(spec, self._device)
-        C = self.n_chains or 1
-        self.C = C
-        T = self.n_iter
+        C = self._bind_glm_store(spec)
         P = spec.P
         dev = self._device
-        self._samples = torch.zeros(T, C, P, dtype=torch.float32, device=dev)
-        for blk in spec.blocks:
-            qz = self.latent_vars[blk.rv]
-            var = qz.params_var
-            src = var.value.to(dev).reshape(qz.n, C, blk.size)[:T]
-            self._samples[:, :, blk.offset:blk.offset + blk.size] = src
-            view = self._samples[:, :, blk.offset:blk.offset + blk.size]
-            shape = (T, C) + tuple(blk.shape) if qz.n_chains else (T,) + tuple(blk.shape)
-            var._value = view.view(shape)
-            var.shape = tuple(shape)
-            qz.n = T
-        self._z = self._samples[0].clone()
         self._g = torch.zeros(C, P, dtype=torch.float32, device=dev)
         self._lj = torch.zeros(C, dtype=torch.float64, device=dev)
         self._cache_valid = 0

@@ -45,6 +45,29 @@ class MonteCarlo(Inference):
     def _validate(self):
         """Host-only model checks run before any device work."""
 
+    def _bind_glm_store(self, spec):
+        """One device sample store [T, C, P] for all latents of a compiled GLM;
+        every Empirical's params Variable becomes a strided view of it (its
+        initial values are copied in), and the chain state starts at
+        params[0].  Returns the number of chains C."""
+        C = self.n_chains or 1
+        self.C = C
+        T = self.n_iter
+        dev = self._device
+        self._samples = torch.zeros(T, C, spec.P, dtype=torch.float32, device=dev)
+        for blk in spec.blocks:
+            qz = self.latent_vars[blk.rv]
+            var = qz.params_var
+            src = var.value.to(dev).reshape(qz.n, C, blk.size)[:T]
+            self._samples[:, :, blk.offset:blk.offset + blk.size] = src
+            view = self._samples[:, :, blk.offset:blk.offset + blk.size]
+            shape = (T, C) + tuple(blk.shape) if qz.n_chains else (T,) + tuple(blk.shape)
+            var._value = view.view(shape)
+            var.shape = tuple(shape)
+            qz.n = T
+        self._z = self._samples[0].clone()
+        return C
+
     def build_update(self):
         raise NotImplementedError()
 

@@ -1,0 +1,128 @@
+"""Stochastic-gradient MCMC: ``SGLD`` (``edward/inferences/sgld.py:19-88``) and
+``SGHMC`` (``edward/inferences/sghmc.py:19-102``) for the GLM family.
+
+Same surface as the reference (``Empirical`` stores, ``initialize(step_size)``
+and ``initialize(step_size, friction)``, ``update`` / ``run``, ``n_accept``);
+the log joint uses ``scale`` as the reference's ``_log_joint`` does.  Each
+iteration is one batched log-joint gradient over all C chains plus a fused
+update kernel (``edg_sgmcmc_glm_run``).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..compile import compile_glm
+from ..ops import GLMDevice
+from ..util import next_seed
+from .monte_carlo import MonteCarlo
+
+
+class _SGMCMC(MonteCarlo):
+    _method = None
+
+    def _validate(self):
+        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        for z in self.latent_vars:
+            if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
+                raise NotImplementedError(
+                    f"latent support '{z.support}' for stochastic-gradient MCMC")
+        C = self.n_chains or 1
+        for qz in self.latent_vars.values():
+            if (qz.n_chains or 1) != C:
+                raise ValueError("every Empirical must hold the same number of chains")
+        if any(z in self.scale for z in self.latent_vars):
+            raise NotImplementedError("scale on latent variables")
+        dscale = np.asarray(self.scale.get(self._spec.observed, 1.0), np.float32)
+        if dscale.size != 1:
+            raise NotImplementedError("per-row data scale is not supported; pass a scalar")
+        self._data_scale = float(dscale.reshape(-1)[0])
+
+    def build_update(self):
+        spec = self._spec
+        dev = self._device
+        self._glm = GLMDevice(spec, dev)
+        C = self._bind_glm_store(spec)
+        self._v = torch.zeros(C, spec.P, dtype=torch.float32, device=dev)
+        self._n_accept = torch.zeros(C, dtype=torch.int32, device=dev)
+        cfg = _lib.EdgSGMCMC()
+        cfg.method = self._method
+        cfg.step_size = float(self.step_size)
+        cfg.friction = float(getattr(self, "friction", 0.0))
+        cfg.data_scale = self._data_scale
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        lib = _lib.load()
+        self._ws_bytes = lib.edg_sgmcmc_glm_workspace_bytes(self._glm.ref(), C)
+        self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
+        self.train = self.update
+        return self.train
+
+    def _launch(self, n_iter, noise=None):
+        _lib.call("edg_sgmcmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                  int(n_iter), _lib.ptr(self._z), _lib.ptr(self._v), _lib.ptr(self._n_accept),
+                  _lib.ptr(self._state), _lib.ptr(self._samples), self._samples.shape[0],
+                  _lib.ptr(noise), _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+
+    def update(self, feed_dict=None):
+        """One iteration for every chain; returns ``{'t', 'accept_rate'}``
+        (every proposal is kept, as in the reference)."""
+        if feed_dict:
+            raise NotImplementedError("feed_dict is not supported for this model family")
+        self._launch(1)
+        t = self.t
+        acc = float(self._n_accept.sum().item()) / (max(t, 1) * self._n_accept.numel())
+        return {"t": t, "accept_rate": acc}
+
+    def _run_loop(self):
+        chunk = self.n_print if self.n_print else self.n_iter
+        done = 0
+        while done < self.n_iter:
+            k = min(chunk, self.n_iter - done)
+            self._launch(k)
+            done += k
+            t = self.t
+            acc = float(self._n_accept.sum().item()) / (max(t, 1) * self._n_accept.numel())
+            self.print_progress({"t": t, "accept_rate": acc})
+
+    def run_iterations(self, k, noise=None):
+        """k iterations without host synchronisation; ``noise`` [k, C, P]
+        overrides the Philox draws."""
+        if noise is not None:
+            noise = torch.as_tensor(noise, dtype=torch.float32, device=self._device).contiguous()
+        self._launch(k, noise)
+
+    @property
+    def n_accept(self):
+        if self._n_accept.numel() == 1:
+            return int(self._n_accept[0].item())
+        return self._n_accept
+
+    def reset(self):
+        super().reset()
+        self._n_accept.zero_()
+        self._z.copy_(self._samples[0])
+        self._v.zero_()
+
+
+class SGLD(_SGMCMC):
+    """Stochastic gradient Langevin dynamics (``sgld.py:52-88``):
+    lr = step_size / (t + 1)^0.55, z <- z + lr/2 grad log p + N(0, lr)."""
+    _method = _lib.SGMCMC_SGLD
+
+    def initialize(self, step_size=0.25, *args, **kwargs):
+        self.step_size = step_size
+        return super().initialize(*args, **kwargs)
+
+
+class SGHMC(_SGMCMC):
+    """Stochastic gradient Hamiltonian Monte Carlo (``sghmc.py:58-102``):
+    lr = step_size * 0.01, z <- z + v, v <- (1 - friction/2) v + lr grad log p
+    + N(0, lr * friction)."""
+    _method = _lib.SGMCMC_SGHMC
+
+    def initialize(self, step_size=0.25, friction=0.1, *args, **kwargs):
+        self.step_size = step_size
+        self.friction = friction
+        return super().initialize(*args, **kwargs)

@@ -321,6 +321,30 @@ int edg_sbn_score_step(const edg_sbn_t* cfg, const edg_opt_t* opt, const edg_opt
 int edg_minibatch_gather_u8(const uint8_t* X, int64_t N, int32_t V, int32_t B, uint64_t seed,
                             const edg_state_t* state, float* Xb, void* stream);
 
+/* ---------------------------------------------------------------- SG-MCMC
+ * n_iter iterations of SGLD (edward/inferences/sgld.py:52-88) or SGHMC
+ * (sghmc.py:58-102) for C independent chains over a GLM: per iteration the
+ * gradient of log p(z) + data_scale * log p(y | z) at every chain's state, then
+ *   SGLD   lr = step_size / (t + 1)^0.55; z += lr/2 grad + sqrt(lr) e
+ *   SGHMC  lr = step_size * 0.01; z += v; v = (1 - friction/2) v + lr grad + sqrt(lr friction) e
+ * with t = state->t (advanced by one per iteration), e ~ N(0, 1) from Philox
+ * stream 5 at iteration t, counter row c, element p (or noise_override
+ * [n_iter, C, P]).  The new state goes to samples[t] ([T_cap, C, P], NULL to
+ * skip) and n_accept[c] += 1 every iteration, as in the reference. */
+enum { EDG_SGMCMC_SGLD = 0, EDG_SGMCMC_SGHMC = 1 };
+typedef struct {
+  int32_t method;   /* EDG_SGMCMC_* */
+  float step_size;
+  float friction;   /* SGHMC */
+  float data_scale; /* Inference.scale of the observed variable */
+  uint64_t seed;
+} edg_sgmcmc_t;
+size_t edg_sgmcmc_glm_workspace_bytes(const edg_glm_t* model, int32_t C);
+int edg_sgmcmc_glm_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32_t C, int32_t n_iter,
+                       float* z, float* v, int32_t* n_accept, edg_state_t* state, float* samples,
+                       int64_t T_cap, const float* noise_override, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and

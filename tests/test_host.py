@@ -301,3 +301,17 @@ def test_sbn_dispatch_on_host():
     with pytest.raises(RuntimeError):
         inf.initialize(n_samples=2, baseline="mlp")
     assert inf._family == "sbn"
+
+
+def test_sgmcmc_validates_on_host():
+    """SGLD / SGHMC compile the GLM on the host, then need the GPU."""
+    from edward_gb300.models import Empirical
+    X = np.zeros((10, 3), np.float32)
+    w = Normal(loc=ed.zeros(3), scale=ed.ones(3))
+    y = Bernoulli(logits=ed.dot(X, w))
+    for cls in (ed.SGLD, ed.SGHMC):
+        inf = cls({w: Empirical(ed.Variable(np.zeros((5, 3), np.float32)))},
+                  data={y: np.zeros(10, np.float32)})
+        with pytest.raises(RuntimeError):
+            inf.initialize(step_size=0.1)
+        assert inf._spec.P == 3
