@@ -17,5 +17,5 @@ from .expr import (Variable, placeholder, dot, matmul, tanh, sigmoid, softplus, 
                    zeros, ones)
 from .inferences import (Inference, VariationalInference, KLqp, ReparameterizationKLqp,
                          ReparameterizationKLKLqp, ScoreKLqp, ScoreRBKLqp, MonteCarlo, HMC,
-                         SGLD, SGHMC)
+                         SGLD, SGHMC, MetropolisHastings)
 from .util import set_seed, Progbar

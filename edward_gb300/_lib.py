@@ -81,6 +81,10 @@ class EdgSGMCMC(ctypes.Structure):
                 ("data_scale", c_float), ("seed", c_uint64)]
 
 
+class EdgMH(ctypes.Structure):
+    _fields_ = [("proposal_loc", c_void_p), ("proposal_scale", c_void_p), ("seed", c_uint64)]
+
+
 class EdgHMC(ctypes.Structure):
     _fields_ = [("step_size", c_float), ("n_steps", c_int32), ("seed", c_uint64),
                 ("chains_per_block", c_int32), ("cluster_size", c_int32)]
@@ -139,6 +143,11 @@ _SIGS = {
     "edg_sgmcmc_glm_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgSGMCMC), c_int32,
                                      c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                      c_int64, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "edg_mh_glm_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgGLM), c_int32]),
+    "edg_mh_glm_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgMH), c_int32, c_int32,
+                                 c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                                 c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                                 c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

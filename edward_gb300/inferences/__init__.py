@@ -5,4 +5,4 @@ from .klqp import (KLqp, ReparameterizationKLqp, ReparameterizationKLKLqp, Score
                    ScoreRBKLqp)
 from .monte_carlo import MonteCarlo
 from .hmc import HMC
-from .sgmcmc import SGLD, SGHMC
+from .sgmcmc import SGLD, SGHMC, MetropolisHastings

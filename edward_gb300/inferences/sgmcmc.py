@@ -126,3 +126,92 @@ class SGHMC(_SGMCMC):
         self.step_size = step_size
         self.friction = friction
         return super().initialize(*args, **kwargs)
+
+
+class MetropolisHastings(MonteCarlo):
+    """Metropolis-Hastings (``edward/inferences/metropolis_hastings.py:19-156``)
+    with the reference's surface: ``MetropolisHastings(latent_vars,
+    proposal_vars, data)``.  Proposals for the GLM family are Normal random
+    walks ``Normal(loc=z, scale=s)`` or independence proposals
+    ``Normal(loc=m, scale=s)`` (constant m, s), per latent."""
+
+    def __init__(self, latent_vars, proposal_vars, data=None, n_chains=None):
+        from ..inferences.inference import check_latent_vars
+        check_latent_vars(proposal_vars)
+        self.proposal_vars = proposal_vars
+        super().__init__(latent_vars, data, n_chains=n_chains)
+
+    def _validate(self):
+        from ..compile import _const_param
+        from ..models import Normal
+        self._spec = compile_glm(list(self.latent_vars.keys()), self.data)
+        C = self.n_chains or 1
+        for qz in self.latent_vars.values():
+            if (qz.n_chains or 1) != C:
+                raise ValueError("every Empirical must hold the same number of chains")
+        P = self._spec.P
+        loc = np.zeros(P, np.float32)
+        scale = np.ones(P, np.float32)
+        walk = None
+        for blk in self._spec.blocks:
+            g = self.proposal_vars.get(blk.rv)
+            if not isinstance(g, Normal):
+                raise NotImplementedError(
+                    f"the proposal of {blk.rv.name} must be a Normal random variable")
+            is_walk = g.loc is blk.rv
+            if walk is None:
+                walk = is_walk
+            elif walk != is_walk:
+                raise NotImplementedError("mixing random-walk and independence proposals")
+            sl = slice(blk.offset, blk.offset + blk.size)
+            scale[sl] = np.broadcast_to(_const_param(g.scale, "proposal scale", {}),
+                                        blk.shape).reshape(-1)
+            if not is_walk:
+                loc[sl] = np.broadcast_to(_const_param(g.loc, "proposal loc", {}),
+                                          blk.shape).reshape(-1)
+        if np.any(scale <= 0):
+            raise ValueError("proposal scales must be positive")
+        self._walk, self._prop_loc, self._prop_scale = walk, loc, scale
+
+    def build_update(self):
+        spec = self._spec
+        dev = self._device
+        self._glm = GLMDevice(spec, dev)
+        C = self._bind_glm_store(spec)
+        self._lj = torch.zeros(C, dtype=torch.float64, device=dev)
+        self._cache_valid = 0
+        self._n_accept = torch.zeros(C, dtype=torch.int32, device=dev)
+        self._loc_t = torch.as_tensor(self._prop_loc, device=dev)
+        self._scale_t = torch.as_tensor(self._prop_scale, device=dev)
+        cfg = _lib.EdgMH()
+        cfg.proposal_loc = None if self._walk else self._loc_t.data_ptr()
+        cfg.proposal_scale = self._scale_t.data_ptr()
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        lib = _lib.load()
+        self._ws_bytes = lib.edg_mh_glm_workspace_bytes(self._glm.ref(), C)
+        self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
+        self.train = self.update
+        return self.train
+
+    def _launch(self, n_iter, e_override=None, u_override=None, ratio_out=None):
+        _lib.call("edg_mh_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                  int(n_iter), _lib.ptr(self._z), _lib.ptr(self._lj), self._cache_valid,
+                  _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
+                  self._samples.shape[0], _lib.ptr(e_override), _lib.ptr(u_override),
+                  _lib.ptr(ratio_out), _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+        self._cache_valid = 1
+
+    update = _SGMCMC.update
+    _run_loop = _SGMCMC._run_loop
+    n_accept = _SGMCMC.n_accept
+
+    def run_iterations(self, k, e_override=None, u_override=None, ratio_out=None):
+        """k iterations without host synchronisation (optional draws / ratios)."""
+        self._launch(k, e_override, u_override, ratio_out)
+
+    def reset(self):
+        MonteCarlo.reset(self)
+        self._n_accept.zero_()
+        self._z.copy_(self._samples[0])
+        self._cache_valid = 0

@@ -345,6 +345,28 @@ int edg_sgmcmc_glm_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32_t 
                        int64_t T_cap, const float* noise_override, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------- Metropolis-Hastings
+ * n_iter iterations of MetropolisHastings (edward/inferences/metropolis_hastings.py:64-156)
+ * for C chains over a GLM with Normal proposals: random walk z' = z + s e
+ * (proposal_loc = NULL) or independence z' = m + s e (proposal_loc = m [P]);
+ * ratio = log p(x, z') - log p(x, z) - log g(z' | z) + log g(z | z') (FP64),
+ * accept if log u < ratio.  e: Philox stream 6 at iteration t = state->t,
+ * counter row c, element p (or e_override [n_iter, C, P]); u: stream 7, row c
+ * (or u_override [n_iter, C]).  lj [C] caches log p(x, z) (rebuilt when
+ * cache_valid = 0); samples[t] and n_accept as in edg_hmc_glm_run;
+ * ratio_out [n_iter, C] or NULL. */
+typedef struct {
+  const float* proposal_loc;   /* [P] device, or NULL for the random walk */
+  const float* proposal_scale; /* [P] device */
+  uint64_t seed;
+} edg_mh_t;
+size_t edg_mh_glm_workspace_bytes(const edg_glm_t* model, int32_t C);
+int edg_mh_glm_run(const edg_glm_t* model, const edg_mh_t* cfg, int32_t C, int32_t n_iter,
+                   float* z, double* lj, int32_t cache_valid, int32_t* n_accept,
+                   edg_state_t* state, float* samples, int64_t T_cap, const float* e_override,
+                   const double* u_override, double* ratio_out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and

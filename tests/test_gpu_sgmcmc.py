@@ -66,3 +66,62 @@ def test_sgmcmc_normal_normal_posterior(cuda, cls_name, step):
     assert inference.n_accept > 0.1
     inference.reset()
     assert inference.t == 0 and inference.n_accept == 0
+
+
+@pytest.mark.parametrize("walk", [True, False])
+def test_mh_chains_match_oracle(cuda, walk):
+    """Per iteration: the FP64 ratio against the oracle's at the same state and
+    draws, the accept decisions (away from log u = ratio) and the kept states."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Normal
+    from oracle import mh
+    from oracle.philox import normals
+    C, n = 8, 6
+    lv, data, model, z0 = _logreg(ed, C)
+    (w, qw), (b, qb) = lv.items()
+    if walk:
+        props = {w: Normal(loc=w, scale=0.05 * ed.ones(5)), b: Normal(loc=b, scale=0.05)}
+        loc = None
+    else:
+        props = {w: Normal(loc=0.3 * ed.ones(5), scale=0.2 * ed.ones(5)),
+                 b: Normal(loc=0.0, scale=0.2)}
+        loc = np.array([0.3] * 5 + [0.0])
+    scale = np.array([0.05] * 6) if walk else np.array([0.2] * 6)
+    inf = ed.MetropolisHastings(lv, props, data=data, n_chains=C)
+    inf.initialize(n_print=0)
+    z = z0.copy()
+    for t in range(n):
+        ratio = torch.empty(C, dtype=torch.float64, device=cuda)
+        inf.run_iterations(1, ratio_out=ratio)
+        z_ref, acc, r_ref = mh.step(model, z, t, scale, loc, seed=inf._cfg.seed)
+        r = ratio.cpu().numpy()
+        np.testing.assert_allclose(r, r_ref, rtol=0, atol=1e-5 * max(1.0, np.abs(model.log_joint(z)).max()))
+        got = inf._samples[t].cpu().numpy()
+        from oracle.philox import uniforms64
+        logu = np.log(uniforms64(inf._cfg.seed, mh.KIND_UNIFORM, t, C))
+        clear = np.abs(logu - r_ref) > 1e-3
+        np.testing.assert_allclose(got[clear], z_ref[clear], rtol=1e-5, atol=1e-5)
+        z = got.astype(np.float64)      # continue from the device's state
+    assert inf.t == n
+
+
+@pytest.mark.parametrize("proposal", ["prior", "walk"])
+def test_mh_normal_normal_posterior(cuda, proposal):
+    """The reference's check (tests/inferences/metropolishastings_test.py:20-45):
+    the prior as an independence proposal ({mu: mu}), or a random walk
+    N(mu, 0.5); 2,000 iterations, posterior N(0, 1/51)."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Empirical, Normal
+    ed.set_seed(42)
+    x_data = np.zeros(50, np.float32)
+    mu = Normal(loc=0.0, scale=1.0)
+    x = Normal(loc=mu, scale=1.0, sample_shape=50)
+    qmu = Empirical(params=ed.Variable(np.ones(2000, np.float32)))
+    g = mu if proposal == "prior" else Normal(loc=mu, scale=0.5)
+    inference = ed.MetropolisHastings({mu: qmu}, {mu: g}, data={x: x_data})
+    inference.run(n_print=0)
+    assert abs(float(qmu.mean())) < 0.1
+    assert abs(float(qmu.stddev()) - np.sqrt(1 / 51)) < 0.1
+    assert inference.t == 2000 and inference.n_accept > 0.1
+    inference.reset()
+    assert inference.t == 0 and inference.n_accept == 0
