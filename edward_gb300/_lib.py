@@ -30,6 +30,7 @@ KLQP_REPARAM_KL, KLQP_REPARAM, KLQP_SCORE = 0, 1, 2
 BASELINE_NONE, BASELINE_MEAN, BASELINE_MLP = 0, 1, 2
 GEMM_TC, GEMM_SIMT = 0, 1
 SGMCMC_SGLD, SGMCMC_SGHMC = 0, 1
+EXPFAM_BETA, EXPFAM_GAMMA, EXPFAM_DIRICHLET = 0, 1, 2
 OPT_ADAM, OPT_SGD, OPT_MOMENTUM, OPT_ADAGRAD, OPT_RMSPROP, OPT_ADADELTA = range(6)
 
 
@@ -83,6 +84,10 @@ class EdgSGMCMC(ctypes.Structure):
 
 class EdgMH(ctypes.Structure):
     _fields_ = [("proposal_loc", c_void_p), ("proposal_scale", c_void_p), ("seed", c_uint64)]
+
+
+class EdgExpFam(ctypes.Structure):
+    _fields_ = [("family", c_int32), ("K", c_int32), ("prior", c_void_p), ("stats", c_void_p)]
 
 
 class EdgHMC(ctypes.Structure):
@@ -148,6 +153,12 @@ _SIGS = {
                                  c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
                                  c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                  c_void_p]),
+    "edg_expfam_hmc_run": (c_int32, [ctypes.POINTER(EdgExpFam), ctypes.POINTER(EdgHMC), c_int32,
+                                     c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_void_p,
+                                     c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "edg_expfam_klqp_step": (c_int32, [ctypes.POINTER(EdgExpFam), c_int32, c_uint64,
+                                       ctypes.POINTER(EdgOpt), c_void_p, c_void_p, c_void_p,
+                                       c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

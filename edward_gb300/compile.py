@@ -492,3 +492,73 @@ def compile_sbn(latent_vars, data):
         X = np.ascontiguousarray(X if X.dtype == np.uint8 else X.astype(np.float32))
     return SBNSpec(V=V, H0=H0, H1=H1, prior_logits=pl2[0].astype(np.float32), weights=weights,
                    X=X, x_node=x_node, batch=batch, observed=xrv, z0=z0, z1=z1)
+
+
+# ------------------------------------------------------------- constrained latent family
+
+@dataclass
+class ExpFamSpec:
+    """One latent with constrained support and i.i.d. observations of it:
+    Beta + Bernoulli(probs=z), Gamma + Poisson(rate=z), Dirichlet +
+    Categorical(probs=z).  Worked in the unconstrained space of the bijector
+    auto_transform picks for the support (``util/random_variables.py:856-917``):
+    sigmoid, softplus, SoftmaxCentered.  ``K`` is the unconstrained dimension."""
+    family: int
+    K: int
+    prior: np.ndarray
+    stats: np.ndarray
+    z: RandomVariable
+    observed: RandomVariable
+    blocks: List[LatentBlock] = field(default_factory=list)
+
+    @property
+    def P(self):
+        return self.K
+
+
+def compile_expfam(latents, data):
+    from scipy.special import gammaln
+    from .models import Beta, Categorical, Dirichlet, Gamma, Poisson
+    observed, bindings = _split_data(data)
+    if len(latents) != 1 or len(observed) != 1:
+        raise UnsupportedModel("the constrained-latent family has one latent and one observed "
+                               "variable")
+    z = latents[0]
+    (x, xval), = observed.items()
+    if isinstance(xval, (RandomVariable, Node)):
+        xval = const_value(xval, bindings) if isinstance(xval, Node) else None
+        if xval is None:
+            raise UnsupportedModel("observed values must be bound to an array")
+    xv = np.asarray(xval)
+    if isinstance(z, Beta) and isinstance(x, Bernoulli) and x.probs is z:
+        if np.any((xv != 0) & (xv != 1)):
+            raise ValueError("Bernoulli observations must be 0 or 1")
+        a = _const_param(z.concentration1, "Beta concentration1", bindings)
+        b = _const_param(z.concentration0, "Beta concentration0", bindings)
+        n1 = float((xv == 1).sum())
+        fam, K, prior, stats = 0, 1, [float(a), float(b)], [n1, float(xv.size) - n1]
+    elif isinstance(z, Gamma) and isinstance(x, Poisson) and x.rate is z:
+        if np.any(xv < 0) or np.any(xv != np.round(xv)):
+            raise ValueError("Poisson observations must be non-negative integers")
+        a = _const_param(z.concentration, "Gamma concentration", bindings)
+        r = _const_param(z.rate, "Gamma rate", bindings)
+        fam, K = 1, 1
+        prior = [float(a), float(r)]
+        stats = [float(xv.sum()), float(xv.size), float(gammaln(xv.astype(np.float64) + 1).sum())]
+    elif isinstance(z, Dirichlet) and isinstance(x, Categorical) and x.probs is z:
+        alpha = _const_param(z.concentration, "Dirichlet concentration", bindings).reshape(-1)
+        Kc = alpha.size
+        if Kc < 2 or Kc > 33:
+            raise UnsupportedModel("the Dirichlet latent needs 2 to 33 categories")
+        if np.any(xv < 0) or np.any(xv >= Kc) or np.any(xv != np.round(xv)):
+            raise ValueError(f"Categorical observations must be integers in [0, {Kc})")
+        fam, K = 2, Kc - 1
+        prior = list(alpha.astype(float))
+        stats = list(np.bincount(xv.astype(np.int64).reshape(-1), minlength=Kc).astype(float))
+    else:
+        raise UnsupportedModel("not a Beta-Bernoulli, Gamma-Poisson or Dirichlet-Categorical model")
+    if np.any(np.asarray(prior) <= 0):
+        raise ValueError("prior parameters must be positive")
+    spec = ExpFamSpec(fam, K, np.asarray(prior, np.float64), np.asarray(stats, np.float64), z, x)
+    spec.blocks = [LatentBlock(z, 0, K, (K,) if fam == 2 else tuple(z.shape))]
+    return spec

@@ -14,7 +14,7 @@ import numpy as np
 import torch
 
 from .. import _lib, autotune
-from ..compile import UnsupportedModel, compile_glm, compile_hier
+from ..compile import UnsupportedModel, compile_expfam, compile_glm, compile_hier
 from ..ops import GLMDevice, HierDevice
 from ..util import next_seed
 from .monte_carlo import MonteCarlo
@@ -52,8 +52,13 @@ class HMC(MonteCarlo):
                 self._spec = compile_hier(list(self.latent_vars.keys()), self.data)
                 self._family = "hier"
             except UnsupportedModel as e_hier:
-                raise UnsupportedModel(f"model is neither in the GLM family ({e_glm}) nor in "
-                                       f"the hierarchical family ({e_hier})") from None
+                try:
+                    self._spec = compile_expfam(list(self.latent_vars.keys()), self.data)
+                    self._family = "expfam"
+                except UnsupportedModel as e_ef:
+                    raise UnsupportedModel(
+                        f"model is not in the GLM family ({e_glm}), the hierarchical family "
+                        f"({e_hier}) or the constrained-latent family ({e_ef})") from None
         if self._family == "glm":
             for z in self.latent_vars:
                 if getattr(z, "support", "real") not in (None, "real", "multivariate_real"):
@@ -68,6 +73,8 @@ class HMC(MonteCarlo):
     def build_update(self):
         if self._family == "hier":
             return self._build_hier()
+        if self._family == "expfam":
+            return self._build_expfam()
         spec = self._spec
         self._glm = GLMDevice(spec, self._device)
         C = self._bind_glm_store(spec)
@@ -182,7 +189,61 @@ class HMC(MonteCarlo):
         self.train = self.update
         return self.train
 
+    def _build_expfam(self):
+        """Chains of the unconstrained latent u (FP64); the Empirical shows the
+        constrained values (``inference.py:247-253``) while ``params_var``
+        holds u."""
+        spec = self._spec
+        dev = self._device
+        C = self.n_chains or 1
+        self.C = C
+        T, K = self.n_iter, spec.K
+        self._ef_prior = torch.as_tensor(spec.prior, device=dev)
+        self._ef_stats = torch.as_tensor(spec.stats, device=dev)
+        m = _lib.EdgExpFam()
+        m.family, m.K = spec.family, K
+        m.prior, m.stats = self._ef_prior.data_ptr(), self._ef_stats.data_ptr()
+        self._ef = m
+        self._samples = torch.zeros(T, C, K, dtype=torch.float64, device=dev)
+        qz = self.latent_vars[spec.z]
+        init = qz.params_var.value
+        if init[0].numel() == C * K:
+            self._samples[0] = init[0].to(dev, torch.float64).reshape(C, K)
+        lead = (T, C) if self.n_chains else (T,)
+        shape = lead + ((K,) if spec.family == _lib.EXPFAM_DIRICHLET else ())
+        qz.params_var._value = self._samples.view(shape)
+        qz.params_var.shape = shape
+        qz.n = T
+        if spec.family == _lib.EXPFAM_BETA:
+            qz._constrain = torch.sigmoid
+        elif spec.family == _lib.EXPFAM_GAMMA:
+            qz._constrain = torch.nn.functional.softplus
+        else:
+            qz._constrain = lambda u: torch.softmax(
+                torch.cat([u, torch.zeros_like(u[..., :1])], dim=-1), dim=-1)
+        self._z = self._samples[0].clone()
+        self._g = torch.zeros_like(self._z)
+        self._lj = torch.zeros(C, dtype=torch.float64, device=dev)
+        self._cache_valid = 0
+        self._n_accept = torch.zeros(C, dtype=torch.int32, device=dev)
+        cfg = _lib.EdgHMC()
+        cfg.step_size = float(self.step_size)
+        cfg.n_steps = int(self.n_steps)
+        cfg.seed = next_seed()
+        self._cfg = cfg
+        self.engine = "expfam"
+        self.train = self.update
+        return self.train
+
     def _launch(self, n_iter, r_override=None, u_override=None, ratio_out=None):
+        if self.engine == "expfam":
+            _lib.call("edg_expfam_hmc_run", ctypes.byref(self._ef), ctypes.byref(self._cfg),
+                      self.C, int(n_iter), _lib.ptr(self._z), _lib.ptr(self._g),
+                      _lib.ptr(self._lj), self._cache_valid, _lib.ptr(self._n_accept),
+                      _lib.ptr(self._state), _lib.ptr(self._samples), self._samples.shape[0],
+                      _lib.ptr(r_override), _lib.ptr(u_override), _lib.stream_ptr())
+            self._cache_valid = 1
+            return
         if self.engine == "hier":
             _lib.call("edg_hmc_hier_run", self._hier.ref(), ctypes.byref(self._cfg), self.C,
                       int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),

@@ -11,7 +11,8 @@ import numpy as np
 import torch
 
 from .. import _lib
-from ..compile import UnsupportedModel, compile_glm, compile_mlp, compile_sbn, parse_normal_q
+from ..compile import (UnsupportedModel, compile_expfam, compile_glm, compile_mlp, compile_sbn,
+                       parse_normal_q)
 from ..expr import Variable, softplus
 from ..models import Normal, RandomVariable
 from ..ops import BNNDevice, GLMDevice, SBNDevice
@@ -105,9 +106,23 @@ class KLqp(VariationalInference):
         except UnsupportedModel as e_glm:
             try:
                 self._spec = compile_mlp(latents, self.data)
+                self._family = "bnn"
             except UnsupportedModel as e_mlp:
-                raise UnsupportedModel(f"{e_glm} (GLM family); {e_mlp} (Bayesian NN family)")
-            self._family = "bnn"
+                try:
+                    self._spec = compile_expfam(latents, self.data)
+                except UnsupportedModel as e_ef:
+                    raise UnsupportedModel(f"{e_glm} (GLM family); {e_mlp} (Bayesian NN family); "
+                                           f"{e_ef} (constrained-latent family)")
+                self._family = "expfam"
+                if self._method_id not in (REPARAM,):
+                    raise NotImplementedError("the constrained-latent family takes the "
+                                              "reparameterisation gradient with Monte Carlo KL")
+                if not self.auto_transform:
+                    raise NotImplementedError("the constrained-latent family needs "
+                                              "auto_transform=True")
+                for blk in self._spec.blocks:
+                    parse_normal_q(self.latent_vars[blk.rv])
+                return
             if method == SCORE:
                 raise NotImplementedError("ScoreKLqp for the Bayesian NN family")
             if any(np.any(np.asarray(v) != 1.0) for v in self.kl_scaling.values()):
@@ -120,6 +135,8 @@ class KLqp(VariationalInference):
             parse_normal_q(self.latent_vars[blk.rv])
 
     def build_loss_and_gradients(self, var_list):
+        if self._family == "expfam":
+            return self._build_expfam(var_list)
         if self._family == "bnn":
             return self._build_bnn(var_list)
         if self._family == "sbn":
@@ -209,6 +226,31 @@ class KLqp(VariationalInference):
         self._grad = torch.zeros(2 * P, dtype=torch.float32, device=dev)
         return None, [(None, v) for v in q_vars]
 
+    def _build_expfam(self, var_list):
+        spec, dev = self._spec, self._device
+        q_vars = self._bind_q(var_list)
+        K = spec.K
+        self._ef_prior = torch.as_tensor(spec.prior, device=dev)
+        self._ef_stats = torch.as_tensor(spec.stats, device=dev)
+        m = _lib.EdgExpFam()
+        m.family, m.K = spec.family, K
+        m.prior, m.stats = self._ef_prior.data_ptr(), self._ef_stats.data_ptr()
+        self._ef = m
+        self._ef_seed = next_seed()
+        self._slots = torch.zeros(4 * K, dtype=torch.float32, device=dev)
+        self._reset_optimizer()
+        self._opt = self.optimizer.to_c()
+        self._grad = torch.zeros(2 * K, dtype=torch.float32, device=dev)
+        z = spec.z
+        if spec.family == _lib.EXPFAM_BETA:
+            self.transformations = {z: torch.sigmoid}
+        elif spec.family == _lib.EXPFAM_GAMMA:
+            self.transformations = {z: torch.nn.functional.softplus}
+        else:
+            self.transformations = {z: lambda u: torch.softmax(
+                torch.cat([u, torch.zeros_like(u[..., :1])], dim=-1), dim=-1)}
+        return None, [(None, v) for v in q_vars]
+
     def _build_sbn(self, var_list):
         spec, dev = self._spec, self._device
         lib = _lib.load()
@@ -293,6 +335,12 @@ class KLqp(VariationalInference):
 
     def _step(self, apply=True, eps=None, grad_out=None, signal_out=None):
         import ctypes
+        if self._family == "expfam":
+            _lib.call("edg_expfam_klqp_step", ctypes.byref(self._ef), self.n_samples,
+                      self._ef_seed, ctypes.byref(self._opt), _lib.ptr(self._mu),
+                      _lib.ptr(self._rho), _lib.ptr(self._slots), _lib.ptr(self._state),
+                      _lib.ptr(eps), _lib.ptr(grad_out), 1 if apply else 0, _lib.stream_ptr())
+            return
         if self._family == "sbn":
             X = self._sbn.batch(self._state)
             _lib.call("edg_sbn_score_step", ctypes.byref(self._cfg), ctypes.byref(self._opt),

@@ -228,3 +228,103 @@ class PointMass(RandomVariable):
     def __init__(self, params, name=None):
         super().__init__((), name)
         self.params_node = as_node(params)
+
+
+class Beta(RandomVariable):
+    """Beta(concentration1, concentration0) (support '01')."""
+
+    support = "01"
+    reparameterizable = True
+
+    def __init__(self, concentration1=1.0, concentration0=1.0, sample_shape=(), name=None,
+                 value=None):
+        super().__init__(sample_shape, name, value)
+        self.concentration1 = as_node(concentration1)
+        self.concentration0 = as_node(concentration0)
+
+    @property
+    def batch_shape(self):
+        return tuple(np.broadcast_shapes(self.concentration1.shape or (),
+                                         self.concentration0.shape or ()))
+
+    def params(self):
+        return {"concentration1": self.concentration1, "concentration0": self.concentration0}
+
+
+class Gamma(RandomVariable):
+    """Gamma(concentration, rate) (support 'nonnegative')."""
+
+    support = "nonnegative"
+    reparameterizable = True
+
+    def __init__(self, concentration=1.0, rate=1.0, sample_shape=(), name=None, value=None):
+        super().__init__(sample_shape, name, value)
+        self.concentration = as_node(concentration)
+        self.rate = as_node(rate)
+
+    @property
+    def batch_shape(self):
+        return tuple(np.broadcast_shapes(self.concentration.shape or (), self.rate.shape or ()))
+
+    def params(self):
+        return {"concentration": self.concentration, "rate": self.rate}
+
+
+class Dirichlet(RandomVariable):
+    """Dirichlet(concentration [K]) (support 'simplex'; event shape [K])."""
+
+    support = "simplex"
+    reparameterizable = True
+
+    def __init__(self, concentration, sample_shape=(), name=None, value=None):
+        super().__init__(sample_shape, name, value)
+        self.concentration = as_node(concentration)
+
+    @property
+    def event_shape(self):
+        return tuple(self.concentration.shape[-1:]) if self.concentration.shape else ()
+
+    @property
+    def batch_shape(self):
+        return tuple(self.concentration.shape[:-1]) if self.concentration.shape else ()
+
+    def params(self):
+        return {"concentration": self.concentration}
+
+
+class Poisson(RandomVariable):
+    """Poisson(rate) (support 'countable')."""
+
+    support = "countable"
+
+    def __init__(self, rate, sample_shape=(), name=None, value=None):
+        super().__init__(sample_shape, name, value)
+        self.rate = as_node(rate)
+
+    @property
+    def batch_shape(self):
+        return tuple(self.rate.shape or ())
+
+    def params(self):
+        return {"rate": self.rate}
+
+
+class Categorical(RandomVariable):
+    """Categorical(logits or probs [..., K]) (support 'countable')."""
+
+    support = "countable"
+
+    def __init__(self, logits=None, probs=None, sample_shape=(), name=None, value=None):
+        super().__init__(sample_shape, name, value)
+        if (logits is None) == (probs is None):
+            raise ValueError("Categorical needs exactly one of logits or probs")
+        self.logits = as_node(logits) if logits is not None else None
+        self.probs = as_node(probs) if probs is not None else None
+
+    @property
+    def batch_shape(self):
+        n = self.logits if self.logits is not None else self.probs
+        return tuple(n.shape[:-1]) if n.shape else ()
+
+    def params(self):
+        return {"logits": self.logits} if self.logits is not None else {"probs": self.probs}

@@ -367,6 +367,37 @@ int edg_mh_glm_run(const edg_glm_t* model, const edg_mh_t* cfg, int32_t C, int32
                    const double* u_override, double* ratio_out, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------- constrained latent
+ * One latent with a constrained support and i.i.d. observations, worked in the
+ * unconstrained space auto_transform maps it to (inference.py:222-264,
+ * util/random_variables.py:856-917): target log p(x, z(u)) + log|det dz/du|.
+ *   EDG_EXPFAM_BETA       Beta(a, b) prior, Bernoulli(probs=z) data, z = sigmoid(u)
+ *   EDG_EXPFAM_GAMMA      Gamma(a, rate b) prior, Poisson(rate=z) data, z = softplus(u)
+ *   EDG_EXPFAM_DIRICHLET  Dirichlet(alpha) prior, Categorical(probs=z) data,
+ *                         z = softmax([u, 0]) (SoftmaxCentered), u in R^(categories - 1) */
+enum { EDG_EXPFAM_BETA = 0, EDG_EXPFAM_GAMMA = 1, EDG_EXPFAM_DIRICHLET = 2 };
+typedef struct {
+  int32_t family;       /* EDG_EXPFAM_* */
+  int32_t K;            /* unconstrained dimension: 1, or categories - 1 (<= 32) */
+  const double* prior;  /* device: (a, b) | (a, rate) | alpha[K + 1] */
+  const double* stats;  /* device: (n1, n0) | (sum x, N, sum log x!) | counts[K + 1] */
+} edg_expfam_t;
+/* HMC over C chains (FP64 state u [C, K], gradient and log joint caches, the
+ * reference's leapfrog and Metropolis test); Philox streams and overrides as in
+ * edg_hmc_glm_run; samples [T_cap, C, K] (unconstrained) or NULL. */
+int edg_expfam_hmc_run(const edg_expfam_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
+                       double* u, double* grad, double* lj, int32_t cache_valid,
+                       int32_t* n_accept, edg_state_t* state, double* samples, int64_t T_cap,
+                       const double* r_override, const double* u_override, void* stream);
+/* One KLqp step with q(u) = N(mu, softplus(rho)) [K]: reparameterisation gradient
+ * with Monte Carlo KL (klqp.py:642-704), S <= 256 draws (Philox stream 0 at
+ * iteration state->t, or eps_override [S, K]), then the optimizer apply
+ * (opt_slots [4K]); loss in state->loss, gradients in grad_out [2K] or NULL. */
+int edg_expfam_klqp_step(const edg_expfam_t* model, int32_t n_samples, uint64_t seed,
+                         const edg_opt_t* opt, float* mu, float* rho, float* opt_slots,
+                         edg_state_t* state, const float* eps_override, float* grad_out,
+                         int32_t apply, void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and
