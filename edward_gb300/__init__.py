@@ -13,6 +13,7 @@ Usage mirrors ``import edward as ed``::
 __version__ = "1.3.5+gb300.0.1"
 
 from . import layers, models, train
+from .criticisms import copy, evaluate, ppc
 from .expr import (Variable, placeholder, dot, matmul, tanh, sigmoid, softplus, reshape, cast,
                    zeros, ones)
 from .inferences import (Inference, VariationalInference, KLqp, ReparameterizationKLqp,

@@ -31,6 +31,7 @@ BASELINE_NONE, BASELINE_MEAN, BASELINE_MLP = 0, 1, 2
 GEMM_TC, GEMM_SIMT = 0, 1
 SGMCMC_SGLD, SGMCMC_SGHMC = 0, 1
 EXPFAM_BETA, EXPFAM_GAMMA, EXPFAM_DIRICHLET = 0, 1, 2
+PREDICT_MEAN, PREDICT_ETA, PREDICT_SAMPLE = 0, 1, 2
 OPT_ADAM, OPT_SGD, OPT_MOMENTUM, OPT_ADAGRAD, OPT_RMSPROP, OPT_ADADELTA = range(6)
 
 
@@ -159,6 +160,8 @@ _SIGS = {
     "edg_expfam_klqp_step": (c_int32, [ctypes.POINTER(EdgExpFam), c_int32, c_uint64,
                                        ctypes.POINTER(EdgOpt), c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
+    "edg_glm_predict": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_int32, c_int32, c_uint64,
+                                  c_uint32, c_void_p, c_void_p]),
     "edg_hmc_glm_tc_tiles_bytes": (c_size_t, [ctypes.POINTER(EdgGLM)]),
     "edg_hmc_glm_tc_prepare": (c_int32, [ctypes.POINTER(EdgGLM), c_void_p, c_size_t, c_void_p]),
     "edg_hmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgHMC), c_int32,

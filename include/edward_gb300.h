@@ -398,6 +398,18 @@ int edg_expfam_klqp_step(const edg_expfam_t* model, int32_t n_samples, uint64_t 
                          edg_state_t* state, const float* eps_override, float* grad_out,
                          int32_t apply, void* stream);
 
+/* ---------------------------------------------------------------- criticism
+ * Posterior predictive of a GLM for ed.evaluate / ed.ppc (edward/criticisms/
+ * evaluate.py:20-233, ppc.py:13-104), for S parameter vectors Z [S, P] (posterior
+ * draws) over the model's rows X:
+ *   EDG_PREDICT_MEAN    out [N]    = mean_s E[y_n | z_s] (sigmoid(eta) or eta)
+ *   EDG_PREDICT_ETA     out [S, N] = eta
+ *   EDG_PREDICT_SAMPLE  out [S, N] = draws of y_n | z_s (Philox stream 8 at
+ *                       `iteration`, counter row s, element n). */
+enum { EDG_PREDICT_MEAN = 0, EDG_PREDICT_ETA = 1, EDG_PREDICT_SAMPLE = 2 };
+int edg_glm_predict(const edg_glm_t* model, const float* Z, int32_t S, int32_t mode,
+                    uint64_t seed, uint32_t iteration, float* out, void* stream);
+
 /* ---------------------------------------------------------------- HMC
  * n_iter HMC iterations for C independent chains over a GLM in one launch.
  * Replaces HMC.build_update + leapfrog (hmc.py:61-130,195-210) and

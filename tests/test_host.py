@@ -315,3 +315,18 @@ def test_sgmcmc_validates_on_host():
         with pytest.raises(RuntimeError):
             inf.initialize(step_size=0.1)
         assert inf._spec.P == 3
+
+
+def test_criticism_argument_checks():
+    X = np.zeros((4, 2), np.float32)
+    w = Normal(loc=ed.zeros(2), scale=ed.ones(2))
+    y = Bernoulli(logits=ed.dot(X, w))
+    qw = Empirical(ed.Variable(np.zeros((3, 2), np.float32)))
+    y_post = ed.copy(y, {w: qw})
+    assert ed.copy(y, None) is y
+    with pytest.raises(TypeError):
+        ed.evaluate(3, data={y_post: np.zeros(4)})
+    with pytest.raises(TypeError):
+        ed.evaluate("binary_accuracy", data={y_post: np.zeros(4)}, n_samples=2.5)
+    with pytest.raises(TypeError):
+        ed.ppc("not callable", data={y_post: np.zeros(4)})
