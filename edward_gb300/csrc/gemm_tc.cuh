@@ -358,7 +358,9 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
     cp_async_wait<0>();
   } else if (warp == kMmaWarp) {
     // ---------------------------------------------------------------- MMA issuer
+    // the whole warp runs the issue loop; one elected lane issues
     constexpr uint32_t idesc = idesc_tf32(BM, BN);
+    const uint32_t issue = elect_one();
     uint32_t it = 0, tcount = 0;
     for (int64_t t = blockIdx.x; t < p.total && !s_err; t += gridDim.x, ++tcount) {
       const Tile x = tile_of(p, t);
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
         const int s = (int)(it % kStages);
         mbar_wait(full(s), (it / kStages) & 1, &s_err);
         tc_fence_after();
-        if (lane == 0) {
+        {
           const uint32_t st = sbase + s * kStageBytes;
 #pragma unroll
           for (int j = 0; j < BK / 8; ++j) {
@@ -382,19 +384,19 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
             const uint64_t bhi = sdesc(st + 2 * kABytes + ko, kLBO, kSBO);
             const uint64_t blo = sdesc(st + 2 * kABytes + kBBytes + ko, kLBO, kSBO);
             const uint32_t acc0 = (kt > 0 || j > 0) ? 1u : 0u;
-            mma_ss(d, alo, bhi, idesc, acc0);
-            mma_ss(d, ahi, blo, idesc, 1u);
-            mma_ss(d, ahi, bhi, idesc, 1u);
+            mma_ss_if(issue, d, alo, bhi, idesc, acc0);
+            mma_ss_if(issue, d, ahi, blo, idesc, 1u);
+            mma_ss_if(issue, d, ahi, bhi, idesc, 1u);
           }
-          mma_commit(empty(s));
-          if (kt == nk - 1) mma_commit(accfull(ab));
+          mma_commit_if(issue, empty(s));
+          if (kt == nk - 1) mma_commit_if(issue, accfull(ab));
         }
         __syncwarp();
       }
     }
     // every MMA this thread issued has completed before TMEM is released
     // (also after a timeout, when nobody else waited for them)
-    if (lane == 0) mma_commit(drain);
+    mma_commit_if(issue, drain);
     __syncwarp();
     volatile int drain_err = 0;
     mbar_wait(drain, 0, &drain_err);

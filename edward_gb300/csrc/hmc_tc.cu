@@ -120,6 +120,44 @@ __device__ __forceinline__ float residual_fast(int lik, float y, float eta, floa
   return (y - eta) * inv_var;
 }
 
+// Residuals r = d log p(y | eta) / d eta of 8 consecutive rows (eta in v on
+// entry), split into tf32 hi (v) and lo = r - hi (exact; only the tensor core's
+// own rounding of lo, a relative 2^-21 of r, remains).  Rows at or beyond
+// nvalid get r = 0.  LL adds the rows' log-likelihoods to kl.
+template <bool LL, bool BERN>
+__device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float4* yt4,
+                                               int nvalid, float inv_var, float lik_norm,
+                                               Kahan& kl) {
+#pragma unroll
+  for (int k4 = 0; k4 < 2; ++k4) {
+    const float4 y4 = yt4[k4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = 4 * k4 + j;
+      const float yv = j == 0 ? y4.x : j == 1 ? y4.y : j == 2 ? y4.z : y4.w;
+      const float eta = v[k];
+      float r;
+      if (LL) {
+        if (BERN) {
+          const float ex = expf(-fabsf(eta));
+          const float sg = 1.0f / (1.0f + ex);
+          r = yv - (eta >= 0.0f ? sg : ex * sg);
+          if (k < nvalid) kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
+        } else {
+          const float diff = yv - eta;
+          r = diff * inv_var;
+          if (k < nvalid) kl.add(-0.5f * diff * diff * inv_var - lik_norm);
+        }
+      } else {
+        r = residual_fast(BERN ? EDG_LIK_BERNOULLI : EDG_LIK_NORMAL, yv, eta, inv_var);
+      }
+      r = k < nvalid ? r : 0.0f;
+      v[k] = tf32_rna(r);
+      lo[k] = r - v[k];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int PP = a.PP, P = a.P;
@@ -314,7 +352,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       }
       __syncwarp();
     } else if (warp == 1) {
-      if (lane == 0) {
+      // the whole warp runs the issue loop; one elected lane issues
+      {
+        const uint32_t issue = elect_one();
         fence_proxy_async();
         const uint32_t id_f = idesc_tf32(kCT, kNR);
         const uint32_t id_b = idesc_tf32(kCT, PP);
@@ -343,15 +383,15 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
               if (kk < KF) {
-                mma_ss(dt, dz_hi + 16 * kk, xl + 16 * kk, id_f, kk > 0 ? 1u : 0u);
-                mma_ss(dt, dz_lo + 16 * kk, xh + 16 * kk, id_f, 1u);
+                mma_ss_if(issue, dt, dz_hi + 16 * kk, xl + 16 * kk, id_f, kk > 0 ? 1u : 0u);
+                mma_ss_if(issue, dt, dz_lo + 16 * kk, xh + 16 * kk, id_f, 1u);
               }
             }
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk)
-              if (kk < KF) mma_ss(dt, dz_hi + 16 * kk, xh + 16 * kk, id_f, 1u);
-            mma_commit(b_emptyx + 8 * s);  // forward operands consumed
-            mma_commit(b_eta + 8 * b);
+              if (kk < KF) mma_ss_if(issue, dt, dz_hi + 16 * kk, xh + 16 * kk, id_f, 1u);
+            mma_commit_if(issue, b_emptyx + 8 * s);  // forward operands consumed
+            mma_commit_if(issue, b_eta + 8 * b);
           }
           if (i >= 1) {
             const int j = i - 1;
@@ -365,13 +405,13 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
 #pragma unroll
             for (int kk = 0; kk < kNR / 8; ++kk) {
-              mma_ts(dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
-              mma_ts(dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
+              mma_ts_if(issue, dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
+              mma_ts_if(issue, dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
             }
 #pragma unroll
-            for (int kk = 0; kk < kNR / 8; ++kk) mma_ts(dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
-            mma_commit(b_emptyt + 8 * s);
-            mma_commit(b_gfull + 8 * b);
+            for (int kk = 0; kk < kNR / 8; ++kk) mma_ts_if(issue, dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
+            mma_commit_if(issue, b_emptyt + 8 * s);
+            mma_commit_if(issue, b_gfull + 8 * b);
           }
         }
       }
@@ -423,37 +463,30 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         const float4* yt4 =
             reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 4 * qs;
         const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
-        float v[16], lo[16];
-        tmem_ld16(tl + COL_ETA(b) + 16 * qs, v);
+        // two halves of 8 rows: ld eta, residuals, st hi / lo; one compact
+        // loop per (log-likelihood wanted, likelihood), so the leapfrog's inner
+        // evaluations run the short residual-only loop
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          float r = 0.0f;
-          const float4 y4 = yt4[k >> 2];
-          const float yv = (k & 3) == 0 ? y4.x : (k & 3) == 1 ? y4.y : (k & 3) == 2 ? y4.z : y4.w;
-          if (k < nvalid) {
-            const float eta = v[k];
-            if (need_ll) {
-              if (a.lik == EDG_LIK_BERNOULLI) {
-                const float ex = expf(-fabsf(eta));
-                const float sg = 1.0f / (1.0f + ex);
-                r = yv - (eta >= 0.0f ? sg : ex * sg);
-                kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
-              } else {
-                const float diff = yv - eta;
-                r = diff * a.inv_lik_var;
-                kl.add(-0.5f * diff * diff * a.inv_lik_var - a.lik_norm);
-              }
-            } else {
-              r = residual_fast(a.lik, yv, eta, a.inv_lik_var);
-            }
+        for (int h = 0; h < 2; ++h) {
+          float v[8], lo[8];
+          const uint32_t col = 16 * qs + 8 * h;
+          const float4* yh = yt4 + 2 * h;
+          const int nv = nvalid - 8 * h;
+          tmem_ld8(tl + COL_ETA(b) + col, v);
+          if (need_ll) {
+            if (a.lik == EDG_LIK_BERNOULLI)
+              residual_block<true, true>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+            else
+              residual_block<true, false>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+          } else {
+            if (a.lik == EDG_LIK_BERNOULLI)
+              residual_block<false, true>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+            else
+              residual_block<false, false>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
           }
-          // hi = tf32(r); lo = r - hi is exact and only the tensor core's own
-          // rounding of lo (a relative 2^-21 of r) remains
-          v[k] = tf32_rna(r);
-          lo[k] = r - v[k];
+          tmem_st8(tl + COL_RHI(b) + col, v);
+          tmem_st8(tl + COL_RLO(b) + col, lo);
         }
-        tmem_st16(tl + COL_RHI(b) + 16 * qs, v);
-        tmem_st16(tl + COL_RLO(b) + 16 * qs, lo);
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
