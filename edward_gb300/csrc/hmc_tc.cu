@@ -17,10 +17,11 @@
 //     K-major shared-memory layout (hi, lo, transposed hi, transposed lo, y),
 //     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
 //
-// Warp roles (576 threads): warp 0 bulk-copy producers, warp 1 MMA issuer and
-// TMEM owner, warps 2-17 epilogue; between gradient evaluations warps 2-17 are
-// the "owners" that run the leapfrog / Metropolis arithmetic for this CTA's
-// share of the cluster's chains, with the chain state in registers.
+// Warp roles (608 threads): warp 0 bulk-copy producers, warp 1 forward MMA
+// issuer and TMEM owner, warp 18 backward MMA issuer, warps 2-17 epilogue;
+// between gradient evaluations warps 2-17 are the "owners" that run the
+// leapfrog / Metropolis arithmetic for this CTA's share of the cluster's
+// chains, with the chain state in registers.
 //
 // Every mbarrier wait is bounded (~1 s of clock64): on timeout the kernel
 // records EDG_E_TIMEOUT in edg_state_t::error and runs to completion without
@@ -38,7 +39,9 @@ using namespace ptx;
 
 constexpr int kCT = 128;        // chains per cluster = MMA M
 constexpr int kNR = 64;         // rows per X tile = forward N = backward K
-constexpr int kThreads = 576;  // 2 control warps + 16 epilogue warps
+constexpr int kEpiWarps = 16;
+constexpr int kFWarp = 1, kBWarp = 2 + kEpiWarps;  // MMA issuers
+constexpr int kThreads = 32 * (3 + kEpiWarps);     // + the bulk-copy warp
 constexpr uint32_t kTmemCols = 512;
 
 __host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP + 256u; }
@@ -108,7 +111,6 @@ struct TcArgs {
 };
 
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
-constexpr int kEpiWarps = 16;
 
 // Residual of one (row, chain): d log p(y | eta) / d eta.  The accurate form
 // (expf / log1pf) is used when the log-likelihood is also needed.
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   float* Zhi = reinterpret_cast<float*>(smem + 2 * SB);
   float* Zlo = Zhi + kCT * PP;
   uint64_t* bars = reinterpret_cast<uint64_t*>(Zlo + kCT * PP);
-  // bars: fullx[2] fullt[2] emptyx[2] emptyt[2] eta[2] r[2] gfull[2] gfree[2]
+  // bars: fullx[2] fullt[2] emptyx[2] emptyt[2] eta[2] r[2] gfull[2], 2 spare
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 16);
   volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
   __shared__ bool s_last;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const uint32_t b_fullx = smem_u32(bars + 0), b_fullt = smem_u32(bars + 2);
   const uint32_t b_emptyx = smem_u32(bars + 4), b_emptyt = smem_u32(bars + 6);
   const uint32_t b_eta = smem_u32(bars + 8), b_r = smem_u32(bars + 10);
-  const uint32_t b_gfull = smem_u32(bars + 12), b_gfree = smem_u32(bars + 14);
+  const uint32_t b_gfull = smem_u32(bars + 12);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -196,7 +198,6 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       mbar_init(b_eta + 8 * i, 1);
       mbar_init(b_r + 8 * i, kEpiWarps);
       mbar_init(b_gfull + 8 * i, 1);
-      mbar_init(b_gfree + 8 * i, kEpiWarps);
     }
     *err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #define COL_GP(b) (384u + 64u * (b))
 
   // ---- owner mapping (warps 2-17, 512 threads): 4R threads per chain
-  const bool owner = warp >= 2;
+  const bool owner = warp >= 2 && warp < 2 + kEpiWarps;
   const int et = threadIdx.x - 64;
   const int TPC = 4 * (int)R;
   const int CPO = kCT / (int)R;
@@ -351,69 +352,77 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         }
       }
       __syncwarp();
-    } else if (warp == 1) {
-      // the whole warp runs the issue loop; one elected lane issues
-      {
-        const uint32_t issue = elect_one();
-        fence_proxy_async();
-        const uint32_t id_f = idesc_tf32(kCT, kNR);
-        const uint32_t id_b = idesc_tf32(kCT, PP);
-        // Descriptors are built once; a K step of 8 tf32 elements is 256 bytes,
-        // i.e. +16 in the descriptor's start-address field (address >> 4).
-        const uint32_t sbo_k = 32u * PP, sbo_t = 32u * kNR;
-        const uint64_t dz_hi = sdesc(zhi_addr, 128, sbo_k), dz_lo = sdesc(zlo_addr, 128, sbo_k);
-        const uint32_t st0 = smem_u32(stage0), st1 = smem_u32(stage1);
-        const uint64_t dx_hi[2] = {sdesc(st0, 128, sbo_k), sdesc(st1, 128, sbo_k)};
-        const uint64_t dx_lo[2] = {sdesc(st0 + 256u * PP, 128, sbo_k),
-                                   sdesc(st1 + 256u * PP, 128, sbo_k)};
-        const uint64_t dt_hi[2] = {sdesc(st0 + 512u * PP, 128, sbo_t),
-                                   sdesc(st1 + 512u * PP, 128, sbo_t)};
-        const uint64_t dt_lo[2] = {sdesc(st0 + 768u * PP, 128, sbo_t),
-                                   sdesc(st1 + 768u * PP, 128, sbo_t)};
-        const int KF = PP / 8;  // forward K steps (2, 4 or 8)
-        for (int i = 0; i <= nt; ++i) {
-          if (i < nt) {
-            const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
-            mbar_wait(b_fullx + 8 * s, (g >> 1) & 1u, err);
-            tc_fence_after();
-            const uint32_t dt = tbase + COL_ETA(b);
-            const uint64_t xh = s ? dx_hi[1] : dx_hi[0], xl = s ? dx_lo[1] : dx_lo[0];
-            // lo products first (small running sum), hi*hi last: fewer
-            // truncating additions land on a large accumulator
+    } else if (warp == kFWarp) {
+      // forward issuer: the whole warp runs the loop, one elected lane issues
+      const uint32_t issue = elect_one();
+      fence_proxy_async();
+      const uint32_t id_f = idesc_tf32(kCT, kNR);
+      // Descriptors are built once; a K step of 8 tf32 elements is 256 bytes,
+      // i.e. +16 in the descriptor's start-address field (address >> 4).
+      const uint32_t sbo_k = 32u * PP;
+      const uint64_t dz_hi = sdesc(zhi_addr, 128, sbo_k), dz_lo = sdesc(zlo_addr, 128, sbo_k);
+      const uint32_t st0 = smem_u32(stage0), st1 = smem_u32(stage1);
+      const uint64_t dx_hi[2] = {sdesc(st0, 128, sbo_k), sdesc(st1, 128, sbo_k)};
+      const uint64_t dx_lo[2] = {sdesc(st0 + 256u * PP, 128, sbo_k),
+                                 sdesc(st1 + 256u * PP, 128, sbo_k)};
+      const int KF = PP / 8;  // forward K steps (2, 4 or 8)
+      for (int i = 0; i < nt; ++i) {
+        const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
+        mbar_wait(b_fullx + 8 * s, (g >> 1) & 1u, err);
+        // eta buffer b is rewritten: the epilogue has read tile g-2's eta once
+        // all its warps arrived on r for that tile
+        if (g >= 2) mbar_wait(b_r + 8 * b, ((g >> 1) - 1) & 1u, err);
+        tc_fence_after();
+        const uint32_t dt = tbase + COL_ETA(b);
+        const uint64_t xh = s ? dx_hi[1] : dx_hi[0], xl = s ? dx_lo[1] : dx_lo[0];
+        // lo products first (small running sum), hi*hi last: fewer
+        // truncating additions land on a large accumulator
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-              if (kk < KF) {
-                mma_ss_if(issue, dt, dz_hi + 16 * kk, xl + 16 * kk, id_f, kk > 0 ? 1u : 0u);
-                mma_ss_if(issue, dt, dz_lo + 16 * kk, xh + 16 * kk, id_f, 1u);
-              }
-            }
-#pragma unroll
-            for (int kk = 0; kk < 8; ++kk)
-              if (kk < KF) mma_ss_if(issue, dt, dz_hi + 16 * kk, xh + 16 * kk, id_f, 1u);
-            mma_commit_if(issue, b_emptyx + 8 * s);  // forward operands consumed
-            mma_commit_if(issue, b_eta + 8 * b);
-          }
-          if (i >= 1) {
-            const int j = i - 1;
-            const uint32_t g = gt + j, s = g & 1u, b = g & 1u;
-            mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);
-            mbar_wait(b_r + 8 * b, (g >> 1) & 1u, err);
-            if (g >= 2) mbar_wait(b_gfree + 8 * b, ((g >> 1) - 1) & 1u, err);
-            tc_fence_after();
-            const uint32_t dg = tbase + COL_GP(b);
-            const uint32_t rh = tbase + COL_RHI(b), rl = tbase + COL_RLO(b);
-            const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
-#pragma unroll
-            for (int kk = 0; kk < kNR / 8; ++kk) {
-              mma_ts_if(issue, dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
-              mma_ts_if(issue, dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
-            }
-#pragma unroll
-            for (int kk = 0; kk < kNR / 8; ++kk) mma_ts_if(issue, dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
-            mma_commit_if(issue, b_emptyt + 8 * s);
-            mma_commit_if(issue, b_gfull + 8 * b);
+        for (int kk = 0; kk < 8; ++kk) {
+          if (kk < KF) {
+            mma_ss_if(issue, dt, dz_hi + 16 * kk, xl + 16 * kk, id_f, kk > 0 ? 1u : 0u);
+            mma_ss_if(issue, dt, dz_lo + 16 * kk, xh + 16 * kk, id_f, 1u);
           }
         }
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk)
+          if (kk < KF) mma_ss_if(issue, dt, dz_hi + 16 * kk, xh + 16 * kk, id_f, 1u);
+        mma_commit_if(issue, b_emptyx + 8 * s);  // forward operands consumed
+        mma_commit_if(issue, b_eta + 8 * b);
+      }
+      __syncwarp();
+    } else if (warp == kBWarp) {
+      // backward issuer, concurrent with the forward one: each warp's barrier
+      // waits hide behind the other's MMAs in the tensor pipe
+      const uint32_t issue = elect_one();
+      fence_proxy_async();
+      const uint32_t id_b = idesc_tf32(kCT, PP);
+      const uint32_t sbo_t = 32u * kNR;
+      const uint32_t st0 = smem_u32(stage0), st1 = smem_u32(stage1);
+      const uint64_t dt_hi[2] = {sdesc(st0 + 512u * PP, 128, sbo_t),
+                                 sdesc(st1 + 512u * PP, 128, sbo_t)};
+      const uint64_t dt_lo[2] = {sdesc(st0 + 768u * PP, 128, sbo_t),
+                                 sdesc(st1 + 768u * PP, 128, sbo_t)};
+      for (int i = 0; i < nt; ++i) {
+        const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
+        mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);
+        // r of tile g complete also means every epilogue warp has read the
+        // gradient partial of tile g-2 (it does so before arriving on r), so
+        // the partial buffer b is free
+        mbar_wait(b_r + 8 * b, (g >> 1) & 1u, err);
+        tc_fence_after();
+        const uint32_t dg = tbase + COL_GP(b);
+        const uint32_t rh = tbase + COL_RHI(b), rl = tbase + COL_RLO(b);
+        const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
+#pragma unroll
+        for (int kk = 0; kk < kNR / 8; ++kk) {
+          mma_ts_if(issue, dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
+          mma_ts_if(issue, dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
+        }
+#pragma unroll
+        for (int kk = 0; kk < kNR / 8; ++kk) mma_ts_if(issue, dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
+        mma_commit_if(issue, b_emptyt + 8 * s);
+        mma_commit_if(issue, b_gfull + 8 * b);
       }
       __syncwarp();
     } else {
@@ -453,7 +462,6 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(b_gfree + 8 * b);
       };
       for (int i = 0; i < nt; ++i) {
         const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
