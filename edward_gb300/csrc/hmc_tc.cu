@@ -127,16 +127,15 @@ __device__ __forceinline__ float residual_fast(int lik, float y, float eta, floa
 // own rounding of lo, a relative 2^-21 of r, remains).  Rows at or beyond
 // nvalid get r = 0.  LL adds the rows' log-likelihoods to kl.
 template <bool LL, bool BERN>
-__device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float4* yt4,
+__device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float (&y)[8],
                                                int nvalid, float inv_var, float lik_norm,
                                                Kahan& kl) {
 #pragma unroll
   for (int k4 = 0; k4 < 2; ++k4) {
-    const float4 y4 = yt4[k4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int k = 4 * k4 + j;
-      const float yv = j == 0 ? y4.x : j == 1 ? y4.y : j == 2 ? y4.z : y4.w;
+      const float yv = y[k];
       const float eta = v[k];
       float r;
       if (LL) {
@@ -471,16 +470,28 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         const float4* yt4 =
             reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 4 * qs;
         const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
-        // two halves of 8 rows: ld eta, residuals, st hi / lo; one compact
-        // loop per (log-likelihood wanted, likelihood), so the leapfrog's inner
-        // evaluations run the short residual-only loop
+        // eta of 16 rows in one TMEM load, y loaded while it is in flight;
+        // then two halves of 8 rows: residuals, st hi / lo.  One compact loop
+        // per (log-likelihood wanted, likelihood), so the leapfrog's inner
+        // evaluations run the short residual-only loop.
+        float ve[16], ye[16];
+        tmem_ld16_issue(tl + COL_ETA(b) + 16 * qs, ve);
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {
+          const float4 y4 = yt4[k4];
+          ye[4 * k4] = y4.x;
+          ye[4 * k4 + 1] = y4.y;
+          ye[4 * k4 + 2] = y4.z;
+          ye[4 * k4 + 3] = y4.w;
+        }
+        tmem_ld_wait(ve);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          float v[8], lo[8];
+          float lo[8];
+          float (&v)[8] = *reinterpret_cast<float (*)[8]>(&ve[8 * h]);
+          const float (&yh)[8] = *reinterpret_cast<const float (*)[8]>(&ye[8 * h]);
           const uint32_t col = 16 * qs + 8 * h;
-          const float4* yh = yt4 + 2 * h;
           const int nv = nvalid - 8 * h;
-          tmem_ld8(tl + COL_ETA(b) + col, v);
           if (need_ll) {
             if (a.lik == EDG_LIK_BERNOULLI)
               residual_block<true, true>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
