@@ -112,50 +112,69 @@ struct TcArgs {
 
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
 
-// Residual of one (row, chain): d log p(y | eta) / d eta.  The accurate form
-// (expf / log1pf) is used when the log-likelihood is also needed.
-__device__ __forceinline__ float residual_fast(int lik, float y, float eta, float inv_var) {
-  if (lik == EDG_LIK_BERNOULLI) {
-    const float e = __expf(-fminf(fmaxf(eta, -80.0f), 80.0f));
-    return y - __fdividef(1.0f, 1.0f + e);
-  }
-  return (y - eta) * inv_var;
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
 }
 
 // Residuals r = d log p(y | eta) / d eta of 8 consecutive rows (eta in v on
 // entry), split into tf32 hi (v) and lo = r - hi (exact; only the tensor core's
-// own rounding of lo, a relative 2^-21 of r, remains).  Rows at or beyond
-// nvalid get r = 0.  LL adds the rows' log-likelihoods to kl.
+// own rounding of lo, a relative 2^-21 of r, remains).
+//   LL (the evaluation also needs the log-likelihood): accurate expf / log1pf,
+//     rows at or beyond nvalid get r = 0 and add nothing to kl.
+//   otherwise the short form: Bernoulli sigmoid(eta) = 1 / (1 + e^-eta) with
+//     e^-eta = 2^(-eta log2 e) and one reciprocal per PAIR of rows,
+//     1/a = b / (a b), 1/b = a / (a b); e^-eta is capped at e^40 so that a b
+//     stays below 2^116 (sigmoid changes by at most e^-40 absolute).  Rows
+//     beyond N are not masked: their X rows are zero, so their r only ever
+//     multiplies zeros in the backward MMA.
 template <bool LL, bool BERN>
 __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float (&y)[8],
                                                int nvalid, float inv_var, float lik_norm,
                                                Kahan& kl) {
+  float r[8];
+  if (LL) {
 #pragma unroll
-  for (int k4 = 0; k4 < 2; ++k4) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int k = 4 * k4 + j;
-      const float yv = y[k];
-      const float eta = v[k];
-      float r;
-      if (LL) {
-        if (BERN) {
-          const float ex = expf(-fabsf(eta));
-          const float sg = 1.0f / (1.0f + ex);
-          r = yv - (eta >= 0.0f ? sg : ex * sg);
-          if (k < nvalid) kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
-        } else {
-          const float diff = yv - eta;
-          r = diff * inv_var;
-          if (k < nvalid) kl.add(-0.5f * diff * diff * inv_var - lik_norm);
-        }
+    for (int k = 0; k < 8; ++k) {
+      const float yv = y[k], eta = v[k];
+      if (BERN) {
+        const float ex = expf(-fabsf(eta));
+        const float sg = 1.0f / (1.0f + ex);
+        r[k] = yv - (eta >= 0.0f ? sg : ex * sg);
+        if (k < nvalid) kl.add(-(fmaxf(eta, 0.0f) - eta * yv + log1pf(ex)));
       } else {
-        r = residual_fast(BERN ? EDG_LIK_BERNOULLI : EDG_LIK_NORMAL, yv, eta, inv_var);
+        const float diff = yv - eta;
+        r[k] = diff * inv_var;
+        if (k < nvalid) kl.add(-0.5f * diff * diff * inv_var - lik_norm);
       }
-      r = k < nvalid ? r : 0.0f;
-      v[k] = tf32_rna(r);
-      lo[k] = r - v[k];
+      r[k] = k < nvalid ? r[k] : 0.0f;
     }
+  } else if (BERN) {
+    constexpr float kLog2e = 1.4426950408889634f;
+    constexpr float kCap = 57.70780163555854f;  // 40 log2 e
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 1.0f + ex2_approx(fminf(-kLog2e * v[k], kCap));
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) {
+      const float ir = rcp_approx(a[k] * a[k + 1]);
+      r[k] = y[k] - a[k + 1] * ir;
+      r[k + 1] = y[k + 1] - a[k] * ir;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r[k] = (y[k] - v[k]) * inv_var;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[k] = tf32_rna(r[k]);
+    lo[k] = r[k] - v[k];
   }
 }
 
