@@ -288,59 +288,73 @@ def run_e2e(args, inf, X, y, z0, dev):
     and the chain state (z, cached gradient and log joint) from pinned host
     memory, re-lays X for the engine when it needs it, runs one iteration with
     the engine the inference selected, and copies the state and the kept
-    sample back."""
+    sample back.  The step's buffers are packed into one pinned host buffer
+    mirrored by one device buffer, [X | y | state record | z | g | lj |
+    sample], so that each step makes one host->device copy (X .. lj) and one
+    device->host copy (z .. sample); the host copy of the state record
+    (iteration t = 0) is never overwritten, so every step starts at t = 0 while
+    the chain state held on the host advances."""
     import ctypes
     import torch
     from edward_gb300 import _lib
     P = N_FEAT + 1
-    h_X = torch.as_tensor(X).pin_memory()
-    h_y = torch.as_tensor(y).pin_memory()
-    h_z = torch.as_tensor(z0).pin_memory()
-    h_g = torch.zeros(N_CHAINS, P).pin_memory()
-    h_lj = torch.zeros(N_CHAINS, dtype=torch.float64).pin_memory()
-    h_out = torch.zeros(N_CHAINS, P).pin_memory()
-    d_X = torch.empty_like(h_X, device=dev)
-    d_y = torch.empty_like(h_y, device=dev)
-    d_z = torch.empty_like(h_z, device=dev)
-    d_g = torch.empty_like(h_g, device=dev)
-    d_lj = torch.empty_like(h_lj, device=dev)
-    d_s = torch.zeros(1, N_CHAINS, P, device=dev)
-    st = _lib.new_state(dev)
+    sizes = [("X", X.size * 4), ("y", y.size * 4), ("st", ctypes.sizeof(_lib.EdgState)),
+             ("z", N_CHAINS * P * 4), ("g", N_CHAINS * P * 4), ("lj", N_CHAINS * 8),
+             ("s", N_CHAINS * P * 4)]
+    off, o = {}, 0
+    for name, nbytes in sizes:
+        off[name] = (o, nbytes)
+        o += (nbytes + 255) // 256 * 256
+    total = o
+    h_buf = torch.zeros(total, dtype=torch.uint8).pin_memory()
+
+    def hview(name, dtype):
+        o0, nb = off[name]
+        return h_buf[o0:o0 + nb].view(dtype)
+
+    hview("X", torch.float32).copy_(torch.as_tensor(X).reshape(-1))
+    hview("y", torch.float32).copy_(torch.as_tensor(y).reshape(-1))
+    hview("z", torch.float32).copy_(torch.as_tensor(z0).reshape(-1))
+    st0 = _lib.EdgState()
+    st0.beta1_power, st0.beta2_power = 0.9, 0.999
+    hview("st", torch.uint8).copy_(torch.frombuffer(bytearray(bytes(st0)), dtype=torch.uint8))
+    d_buf = torch.empty(total, dtype=torch.uint8, device=dev)
+    base = d_buf.data_ptr()
+
+    def dptr(name):
+        return ctypes.c_void_p(base + off[name][0])
+
+    in_end = off["lj"][0] + off["lj"][1]
+    out_begin = off["z"][0]
+    out_end = off["s"][0] + off["s"][1]
     glm = _lib.EdgGLM()
     glm.X, glm.y, glm.N, glm.D, glm.bias, glm.lik, glm.lik_scale = (
-        d_X.data_ptr(), d_y.data_ptr(), N_ROWS, N_FEAT, 1, 0, 1.0)
+        base + off["X"][0], base + off["y"][0], N_ROWS, N_FEAT, 1, 0, 1.0)
     glm.prior_loc = inf._glm.prior_loc.data_ptr()
     glm.prior_scale = inf._glm.prior_scale.data_ptr()
     cfg = inf._cfg
     stream = torch.cuda.current_stream()
     sp = _lib.stream_ptr(stream)
-    state0 = _lib.new_state(dev)
     lib = _lib.load()
     tc = inf.engine == "tc"
     if tc:
         nb = lib.edg_hmc_glm_tc_tiles_bytes(ctypes.byref(glm))
         tiles = torch.empty(nb, dtype=torch.uint8, device=dev)
+    h_in, d_in = h_buf[:in_end], d_buf[:in_end]
+    h_out, d_out = h_buf[out_begin:out_end], d_buf[out_begin:out_end]
 
     def step(cache_valid):
-        d_X.copy_(h_X, non_blocking=True)
-        d_y.copy_(h_y, non_blocking=True)
-        d_z.copy_(h_z, non_blocking=True)
-        d_g.copy_(h_g, non_blocking=True)
-        d_lj.copy_(h_lj, non_blocking=True)
-        st.copy_(state0)
+        d_in.copy_(h_in, non_blocking=True)
         if tc:
             _lib.call("edg_hmc_glm_tc_prepare", ctypes.byref(glm), _lib.ptr(tiles), nb, sp)
             _lib.call("edg_hmc_glm_tc_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
-                      _lib.ptr(tiles), _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid,
-                      None, _lib.ptr(st), _lib.ptr(d_s), 1, None, None, None, None, sp)
+                      _lib.ptr(tiles), dptr("z"), dptr("g"), dptr("lj"), cache_valid,
+                      None, dptr("st"), dptr("s"), 1, None, None, None, None, sp)
         else:
             _lib.call("edg_hmc_glm_run", ctypes.byref(glm), ctypes.byref(cfg), N_CHAINS, 1,
-                      _lib.ptr(d_z), _lib.ptr(d_g), _lib.ptr(d_lj), cache_valid, None,
-                      _lib.ptr(st), _lib.ptr(d_s), 1, None, None, None, None, sp)
-        h_z.copy_(d_z, non_blocking=True)
-        h_g.copy_(d_g, non_blocking=True)
-        h_lj.copy_(d_lj, non_blocking=True)
-        h_out.copy_(d_s[0], non_blocking=True)
+                      dptr("z"), dptr("g"), dptr("lj"), cache_valid, None,
+                      dptr("st"), dptr("s"), 1, None, None, None, None, sp)
+        h_out.copy_(d_out, non_blocking=True)
         stream.synchronize()
 
     step(0)  # builds the gradient cache for the host-held state
@@ -351,12 +365,11 @@ def run_e2e(args, inf, X, y, z0, dev):
     for _ in range(args.steps):
         step(1)
     dt = time.perf_counter() - t0
-    h2d = h_X.numel() * 4 + h_y.numel() * 4 + h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8
-    d2h = h_z.numel() * 4 + h_g.numel() * 4 + h_lj.numel() * 8 + h_out.numel() * 4
     name = "edg_hmc_glm_tc_prepare + edg_hmc_glm_tc_run" if tc else "edg_hmc_glm_run"
     return {"value": N_CHAINS * N_LEAP * args.steps / dt, "unit": UNIT,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "path": f"{name} (C ABI) with pinned host buffers, wall clock"}
+            "h2d_bytes_per_step": int(in_end), "d2h_bytes_per_step": int(out_end - out_begin),
+            "path": f"{name} (C ABI), one packed pinned host buffer, one copy each way per step, "
+                    "wall clock"}
 
 
 def read_traffic(engine):
