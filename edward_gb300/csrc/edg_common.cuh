@@ -78,6 +78,26 @@ __device__ __forceinline__ float sigmoidf(float x) {
   const float s = 1.0f / (1.0f + e);
   return x >= 0.0f ? s : e * s;
 }
+// The hardware approximations behind the per-row likelihood arithmetic of
+// the hot loops (exp via exp2(x log2 e), log via ln 2 * log2 x).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+
 // Kahan-compensated FP32 accumulation (per-thread partials of the log joint;
 // the cross-thread and cross-block sums are done in FP64).
 struct Kahan {

@@ -112,15 +112,17 @@ __device__ __forceinline__ void issue_tile(const GLMDev& m, float* Xdst, float* 
   }
 }
 
-// Log-likelihood term and residual d/d eta for one (row, vector).
+// Log-likelihood term and residual d/d eta for one (row, vector).  Bernoulli:
+// e = e^-|eta| = 2^(-|eta| log2 e) <= 1 and a = 1 + e give sigmoid(eta) = 1/a
+// (eta >= 0) or e/a and log1p(e) = ln 2 * log2(a) (absolute error ~2e-7).
 __device__ __forceinline__ void lik_term(const GLMDev& m, float y, float eta, float& ll,
                                          float& resid) {
   if (m.lik == EDG_LIK_BERNOULLI) {
-    const float e = expf(-fabsf(eta));
-    const float s = 1.0f / (1.0f + e);
-    const float sig = eta >= 0.0f ? s : e * s;
-    ll = -(fmaxf(eta, 0.0f) - eta * y + log1pf(e));
-    resid = y - sig;
+    const float e = ex2_approx(-kLog2e * fabsf(eta));
+    const float a = 1.0f + e;
+    const float s = rcp_approx(a);
+    ll = -(fmaxf(eta, 0.0f) - eta * y + kLn2 * lg2_approx(a));
+    resid = y - (eta >= 0.0f ? s : e * s);
   } else {
     const float diff = y - eta;
     ll = -0.5f * diff * diff * m.inv_lik_var - m.lik_norm;

@@ -112,21 +112,6 @@ struct TcArgs {
 
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
 
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float rcp_approx(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float lg2_approx(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
 
 // Residuals r = d log p(y | eta) / d eta of 8 consecutive rows (eta in v on
 // entry), split into tf32 hi (v) and lo = r - hi (exact; only the tensor core's
@@ -152,8 +137,6 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
   if (LL) {
     float part = 0.0f;
     if (BERN) {
-      constexpr float kLog2e = 1.4426950408889634f;
-      constexpr float kLn2 = 0.6931471805599453f;
       float e[8], a[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
@@ -184,7 +167,6 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
 #pragma unroll
     for (int k = 0; k < 8; ++k) r[k] = k < nvalid ? r[k] : 0.0f;
   } else if (BERN) {
-    constexpr float kLog2e = 1.4426950408889634f;
     constexpr float kCap = 57.70780163555854f;  // 40 log2 e
     float a[8];
 #pragma unroll
