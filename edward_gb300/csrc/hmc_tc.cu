@@ -278,6 +278,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   // prior loc and precision 1/scale^2 per coordinate (zero beyond P), and this
   // thread's share of the log-density normalising constant
   __shared__ float s_ploc[64], s_pprec[64];
+  __shared__ double s_logu[kCT];  // log of the Metropolis uniform, per chain of this CTA
   for (int d = threadIdx.x; d < PP; d += kThreads) {
     const bool ok = d < P;
     const float sc = ok ? a.prior_scale[d] : 1.0f;
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     if (owner) {
       if (!cache_eval) {
         if (l == 0) {
-          double k = 0.0;
+          float kf = 0.0f;
 #pragma unroll
           for (int i = 0; i < kMaxEPT; ++i) {
             const int d = d0 + i;
@@ -328,8 +329,11 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             rr[i] = r;
             zr[i] = ok ? zg[d] : 0.0f;
             gr[i] = ok ? gg[d] : 0.0f;
-            k += (double)r * (double)r;
+            kf = fmaf(r, r, kf);
           }
+          // FP32 over this thread's few elements, FP64 across the chain's
+          // threads (GB300's FP64 rate is a small fraction of its FP32 rate)
+          double k = (double)kf;
           for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
           kin0 = k;
         }
@@ -422,6 +426,18 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     } else if (warp == kBWarp) {
       // backward issuer, concurrent with the forward one: each warp's barrier
       // waits hide behind the other's MMAs in the tensor pipe
+      if (!cache_eval && l == L - 1) {
+        // the Metropolis uniforms of this CTA's chains and their FP64 logs,
+        // computed here (this warp mostly waits) rather than by the owners
+        for (int c = lane; c < CPO; c += 32) {
+          const int cgl = c_base + (int)rank * CPO + c;
+          double lu = 0.0;
+          if (cgl < a.C)
+            lu = log(a.u_ovr ? a.u_ovr[(size_t)it * a.C + cgl]
+                             : u01d(philox_at(a.seed, 2u, iter, (uint32_t)cgl, 0u).x));
+          s_logu[c] = lu;
+        }
+      }
       const uint32_t issue = elect_one();
       fence_proxy_async();
       const uint32_t id_b = idesc_tf32(kCT, PP);
@@ -572,19 +588,24 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           }
         }
       }
+      // log-likelihood of the chain: R CTAs x 4 quarter partials, one per
+      // thread of the chain (4R threads), reduced across them
       double llsum = 0.0;
-      if (need_ll)
-        for (uint32_t q = 0; q < R; ++q)
-          for (int h = 0; h < 4; ++h) llsum += ld_dsmem_f64(mapa(llpart_addr + 8u * (h * kCT + cc), q));
-      double lp = plogc;
+      if (need_ll) {
+        const uint32_t q = (uint32_t)part >> 2, h = (uint32_t)part & 3u;
+        llsum = ld_dsmem_f64(mapa(llpart_addr + 8u * (h * kCT + cc), q));
+        for (int o = TPC >> 1; o > 0; o >>= 1) llsum += __shfl_xor_sync(0xffffffffu, llsum, o);
+      }
+      float lpf = 0.0f;
 #pragma unroll
       for (int i = 0; i < kMaxEPT; ++i) {
         const int d = min(d0 + i, PP - 1);
         const float pr = i < EPT ? s_pprec[d] : 0.0f;
         const float dz = zr[i] - s_ploc[d];
         G[i] = (i < EPT && d0 + i < P) ? G[i] - dz * pr : 0.0f;
-        if (need_ll) lp += (double)(-0.5f * dz * dz * pr);
+        if (need_ll) lpf += -0.5f * dz * dz * pr;
       }
+      double lp = plogc + (double)lpf;
       if (need_ll)
         for (int o = TPC >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
       if (cache_eval) {
@@ -601,20 +622,22 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           rr[i] = rr[i] + half * G[i];
         }
         if (l == L - 1) {
-          // Metropolis test in FP64 (hmc.py:100-109)
-          double k = 0.0;
+          // Metropolis test in FP64 (hmc.py:100-109), on the chain's first
+          // thread; the decision is broadcast to the chain's other threads
+          float kf = 0.0f;
 #pragma unroll
-          for (int i = 0; i < kMaxEPT; ++i) k += (double)rr[i] * (double)rr[i];
+          for (int i = 0; i < kMaxEPT; ++i) kf = fmaf(rr[i], rr[i], kf);
+          double k = (double)kf;
           for (int o = TPC >> 1; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
           const double lj_new = llsum + lp;
-          const double lj0 = cvalid ? a.lj[cg] : 0.0;
-          __syncwarp();  // every thread of the chain has read lj before it is replaced
-          const double ratio = 0.5 * kin0 - 0.5 * k + lj_new - lj0;
-          double u = 0.5;
-          if (cvalid)
-            u = a.u_ovr ? a.u_ovr[(size_t)it * a.C + cg]
-                        : u01d(philox_at(a.seed, 2u, iter, (uint32_t)cg, 0u).x);
-          const bool accept = log(u) < ratio;
+          double ratio = 0.0;
+          int acc_lead = 0;
+          if (part == 0 && cvalid) {
+            const double lj0 = a.lj[cg];
+            ratio = 0.5 * kin0 - 0.5 * k + lj_new - lj0;
+            acc_lead = s_logu[chain_local] < ratio ? 1 : 0;
+          }
+          const bool accept = __shfl_sync(0xffffffffu, acc_lead, lane & ~(TPC - 1)) != 0;
           if (cvalid) {
             if (part == 0) {
               if (accept) a.lj[cg] = lj_new;
