@@ -18,9 +18,9 @@
 //   warp 12     TMEM owner and MMA issuer (one elected lane).
 // Tiles are 128 (M) x 256 (N) x 16 (K) with 2 split (hi/lo) shared-memory
 // stages, 3 raw stages and two TMEM accumulators (2 x 256 columns), so the
-// epilogue of one tile overlaps the main loop of the next.  The core-matrix strides (LBO = 160 B between K groups,
-// SBO = 656 B between 8-row groups) make both producer store patterns free of
-// shared-memory bank conflicts.
+// epilogue of one tile overlaps the main loop of the next.  The core-matrix
+// strides (LBO = 160 B between K groups, SBO = 656 B between 8-row groups)
+// make both producer store patterns free of shared-memory bank conflicts.
 //
 // Long reductions are split over K (kchunk rows per split, partial tiles
 // summed in FP32 with round-to-nearest by a reduce kernel): the tensor core's
@@ -297,7 +297,6 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(Problem p, Epi epi
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nk_full = (p.kchunk + BK - 1) / BK;
 
   if (warp < kProdWarps) {
     // ---------------------------------------------------------------- producers

@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(kThreads) hmc_glm_kernel(GLMDev m, HmcArgs a) 
     Z0[idx] = ok ? a.z[g] : 0.0f;
     G0[idx] = (ok && a.cache_valid) ? a.grad[g] : 0.0f;
   }
-  if (threadIdx.x < CT) lj0[threadIdx.x] = (a.cache_valid && threadIdx.x < nc) ? a.lj[cbase + threadIdx.x] : 0.0;
+  if (threadIdx.x < CT)
+    lj0[threadIdx.x] = (a.cache_valid && threadIdx.x < nc) ? a.lj[cbase + threadIdx.x] : 0.0;
   __syncthreads();
   if (!a.cache_valid) {
     transpose_into<CT>(Z0, S.Zt, PP);

@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(kT) accept_kernel(AccArgs a) {
   const int64_t t = a.state->t;
   if (threadIdx.x == 0) {
     const double ratio = a.lj_new[c] - a.lj[c] + a.lq[c];
-    const double u = a.u_ovr ? a.u_ovr[c] : u01d(philox_at(a.seed, kKindUniform, (uint32_t)t, (uint32_t)c, 0u).x);
+    const double u = a.u_ovr ? a.u_ovr[c]
+                             : u01d(philox_at(a.seed, kKindUniform, (uint32_t)t, (uint32_t)c, 0u).x);
     const bool acc = log(u) < ratio;
     s_acc = acc;
     if (acc) {

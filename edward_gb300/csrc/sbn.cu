@@ -529,7 +529,8 @@ static size_t carve(const Dims& d, int sms, void* base, Workspace* w) {
   }
   const int nb = (d.B + kT / 32 - 1) / (kT / 32);
   const size_t o[] = {
-      take(B * d.ldx * 4),   take(mlp ? B * d.ldx * 4 : 0), take(B * d.H0 * 4), take(R * d.ld0 * 4), take(R * d.ld1 * 4),
+      take(B * d.ldx * 4),   take(mlp ? B * d.ldx * 4 : 0), take(B * d.H0 * 4),
+      take(R * d.ld0 * 4),   take(R * d.ld1 * 4),
       take(R * d.H0 * 4),    take(R * d.H1 * 4), take(R * d.H0 * 4),  take(R * d.V * 4),
       take(B * d.H0 * 4),    take(5 * R * 4),    take(R * 4),
       take(mlp ? B * d.ldh * 4 : 0), take(B * 4), take(B * 4), take(mlp ? B * d.BH * 4 : 0),
