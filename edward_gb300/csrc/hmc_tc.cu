@@ -14,7 +14,7 @@
 //   * 3xTF32: every operand is split a = hi + lo (hi = tf32(a), lo = tf32(a - hi))
 //     and each product is hi*hi + hi*lo + lo*hi with FP32 accumulation;
 //   * X is re-laid once per model into 64-row tiles already in the canonical
-//     K-major shared-memory layout (hi, lo, transposed hi, transposed lo, y),
+//     K-major shared-memory layout (hi, lo, transposed hi, transposed lo),
 //     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
 //
 // Warp roles (608 threads): warp 0 bulk-copy producers, warp 1 forward MMA
@@ -44,7 +44,7 @@ constexpr int kFWarp = 1, kBWarp = 2 + kEpiWarps;  // MMA issuers
 constexpr int kThreads = 32 * (3 + kEpiWarps);     // + the bulk-copy warp
 constexpr uint32_t kTmemCols = 512;
 
-__host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP + 256u; }
+__host__ __device__ constexpr uint32_t stage_bytes(int PP) { return 1024u * PP; }
 
 // Canonical K-major, no-swizzle layout: 8-row x 16-byte core matrices; core
 // matrices adjacent along K are 128 B apart (LBO), 8-row groups are
@@ -54,7 +54,7 @@ __host__ __device__ inline uint32_t kmajor_off(int row, int k, int Kext) {
 }
 
 // ------------------------------------------------------------------ tiling
-__global__ void prep_tiles_kernel(const float* __restrict__ X, const float* __restrict__ y, int N,
+__global__ void prep_tiles_kernel(const float* __restrict__ X, int N,
                                   int D, int bias, int PP, int ntiles,
                                   unsigned char* __restrict__ out) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -84,12 +84,12 @@ __global__ void prep_tiles_kernel(const float* __restrict__ X, const float* __re
   xlo[o1] = lo;
   xthi[o2] = hi;
   xtlo[o2] = lo;
-  if (d == 0) reinterpret_cast<float*>(base + 1024 * PP)[n] = row < N ? y[row] : 0.0f;
 }
 
 // ------------------------------------------------------------------ main kernel
 struct TcArgs {
   const unsigned char* tiles;
+  const float* y;  // the model's observations (the epilogue reads them directly)
   int ntiles, N, P, PP, lik;
   float inv_lik_var, lik_norm;
   const float* prior_loc;
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const int PP = a.PP, P = a.P;
   const uint32_t SB = stage_bytes(PP);
   const uint32_t XB = 512u * PP;      // forward part of a tile: X hi, X lo
-  const uint32_t TB = SB - XB;        // backward part: X^T hi, X^T lo, y
+  const uint32_t TB = SB - XB;        // backward part: X^T hi, X^T lo
   unsigned char* stage0 = smem;
   unsigned char* stage1 = smem + SB;
   float* Zhi = reinterpret_cast<float*>(smem + 2 * SB);
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     // ================= gradient evaluation over this CTA's row tiles
     if (warp == 0) {
       // lane 0 streams the forward parts (X hi/lo), lane 1 the backward parts
-      // (X^T hi/lo, y); each part is one bulk copy into a double buffer
+      // (X^T hi/lo); each part is one bulk copy into a double buffer
       if (lane < 2) {
         const uint32_t part_off = lane == 0 ? 0u : XB;
         const uint32_t bytes = lane == 0 ? XB : TB;
@@ -483,6 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
       for (int k = 0; k < 16; ++k) Gacc[k] = 0.0f;
       Kahan kl;
+      const bool y_vec = (reinterpret_cast<uintptr_t>(a.y) & 15u) == 0;
       auto consume_gpart = [&](int i) {
         const uint32_t g = gt + i, b = g & 1u;
         mbar_wait(b_gfull + 8 * b, (g >> 1) & 1u, err);
@@ -508,27 +509,34 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         __syncwarp();
       };
       for (int i = 0; i < nt; ++i) {
-        const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
-        mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
-        mbar_wait(b_fullt + 8 * s, (g >> 1) & 1u, err);  // y lives in the backward part
-        tc_fence_after();
-        const float4* yt4 =
-            reinterpret_cast<const float4*>((s ? stage1 : stage0) + 1024 * PP) + 4 * qs;
+        const uint32_t g = gt + i, b = g & 1u;
+        // y of this thread's 16 rows straight from the model (L2-resident),
+        // loaded before the eta wait so that its latency hides behind it
+        const int row0 = (t_begin + i) * kNR + 16 * qs;
         const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
-        // eta of 16 rows in one TMEM load, y loaded while it is in flight;
-        // then two halves of 8 rows: residuals, st hi / lo.  One compact loop
-        // per (log-likelihood wanted, likelihood), so the leapfrog's inner
-        // evaluations run the short residual-only loop.
-        float ve[16], ye[16];
-        tmem_ld16_issue(tl + COL_ETA(b) + 16 * qs, ve);
+        float ye[16];
+        if (nvalid >= 16 && y_vec) {
+          const float4* y4p = reinterpret_cast<const float4*>(a.y + row0);
 #pragma unroll
-        for (int k4 = 0; k4 < 4; ++k4) {
-          const float4 y4 = yt4[k4];
-          ye[4 * k4] = y4.x;
-          ye[4 * k4 + 1] = y4.y;
-          ye[4 * k4 + 2] = y4.z;
-          ye[4 * k4 + 3] = y4.w;
+          for (int k4 = 0; k4 < 4; ++k4) {
+            const float4 y4 = __ldg(y4p + k4);
+            ye[4 * k4] = y4.x;
+            ye[4 * k4 + 1] = y4.y;
+            ye[4 * k4 + 2] = y4.z;
+            ye[4 * k4 + 3] = y4.w;
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) ye[k] = k < nvalid ? __ldg(a.y + row0 + k) : 0.0f;
         }
+        mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
+        tc_fence_after();
+        // eta of 16 rows in one TMEM load; then two halves of 8 rows:
+        // residuals, st hi / lo.  One compact loop per (log-likelihood wanted,
+        // likelihood), so the leapfrog's inner evaluations run the short
+        // residual-only loop.
+        float ve[16];
+        tmem_ld16_issue(tl + COL_ETA(b) + 16 * qs, ve);
         tmem_ld_wait(ve);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -754,7 +762,7 @@ extern "C" int edg_hmc_glm_tc_prepare(const edg_glm_t* model, void* tiles, size_
               need);
   const int64_t total = (int64_t)ntiles * kNR * PP;
   prep_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      m.X, m.y, m.N, m.D, m.bias, PP, ntiles, reinterpret_cast<unsigned char*>(tiles));
+      m.X, m.N, m.D, m.bias, PP, ntiles, reinterpret_cast<unsigned char*>(tiles));
   return check_launch("prep_tiles_kernel");
 }
 
@@ -783,6 +791,7 @@ extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, 
               cfg->cluster_size);
   TcArgs a;
   a.tiles = reinterpret_cast<const unsigned char*>(tiles);
+  a.y = m.y;
   a.ntiles = ntiles;
   a.N = m.N;
   a.P = m.P;

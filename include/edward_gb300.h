@@ -467,7 +467,8 @@ int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, i
  * rows of X and reducing each leapfrog gradient through distributed shared
  * memory.  Requires P = D + bias <= 64 and n_steps > 0.  `tiles` is the
  * model's X re-laid into 64-row operand tiles by edg_hmc_glm_tc_prepare
- * (once per model; edg_hmc_glm_tc_tiles_bytes gives its size).
+ * (once per model; edg_hmc_glm_tc_tiles_bytes gives its size); y is read from
+ * model->y during the run.
  * Replaces the same reference code as edg_hmc_glm_run (hmc.py:61-130,195-210;
  * monte_carlo.py:111-150). */
 size_t edg_hmc_glm_tc_tiles_bytes(const edg_glm_t* model);
