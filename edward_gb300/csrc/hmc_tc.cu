@@ -15,7 +15,9 @@
 //     and each product is hi*hi + hi*lo + lo*hi with FP32 accumulation;
 //   * X is re-laid once per model into 64-row tiles already in the canonical
 //     K-major shared-memory layout (hi, lo, transposed hi, transposed lo),
-//     so each tile is ONE cp.async.bulk copy completing on an mbarrier.
+//     so each tile is two cp.async.bulk copies (forward part, backward part),
+//     each completing on its own mbarrier; the epilogue reads y straight from
+//     the model's array.
 //
 // Warp roles (608 threads): warp 0 bulk-copy producers, warp 1 forward MMA
 // issuer and TMEM owner, warp 18 backward MMA issuer, warps 2-17 epilogue;
