@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   GradSmem S;
   unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
   float* sig = reinterpret_cast<float*>(rest);  // [PP]
+  float* epsS = sig + m.PP;                      // [Spad][PP] this step's draws
   __shared__ bool s_last;
   const int P = m.P, PP = m.PP;
   const int64_t t = *(volatile int64_t*)&a.state->t;
@@ -123,7 +124,11 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       const int c = idx / PP, d = idx - c * PP;
       const int s = s0 + c;
       float zv = 0.0f;
-      if (s < a.S && d < P) zv = a.mu[d] + sig[d] * eps_value(a, iter, s, d, P);
+      if (s < a.S && d < P) {
+        const float e = eps_value(a, iter, s, d, P);
+        epsS[s * PP + d] = e;  // kept for the last block's gradient formula
+        zv = a.mu[d] + sig[d] * e;
+      }
       S.Zt[d * CT + c] = zv;
     }
     __syncthreads();
@@ -155,16 +160,32 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   double* red = lsig + a.S;              // [8] per-warp partial sums
   float* gS = S.Xs;                      // [S][PP] gradient per sample
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // (eight interleaved accumulators per quantity, so that the loads of eight
+  // blocks are in flight together; fixed order, so the sums are deterministic)
   for (int s = threadIdx.x; s < a.S; s += kThreads) {
-    double v = 0.0;
-    for (int b = 0; b < a.nblocks; ++b) v += __ldcg(a.ws_ll + (size_t)b * a.Spad + s);
-    llS[s] = v;
+    const double* src = a.ws_ll + s;
+    const size_t st = (size_t)a.Spad;
+    double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int b = 0;
+    for (; b + 8 <= a.nblocks; b += 8) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] += __ldcg(src + (b + k) * st);
+    }
+    for (; b < a.nblocks; ++b) v[0] += __ldcg(src + b * st);
+    llS[s] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   }
   if (need_grad) {
     for (int idx = threadIdx.x; idx < a.S * PP; idx += kThreads) {
-      float v = 0.0f;
-      for (int b = 0; b < a.nblocks; ++b) v += __ldcg(a.ws_g + (size_t)b * a.Spad * PP + idx);
-      gS[idx] = v;
+      const float* src = a.ws_g + idx;
+      const size_t st = (size_t)a.Spad * PP;
+      float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      int b = 0;
+      for (; b + 8 <= a.nblocks; b += 8) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] += __ldcg(src + (b + k) * st);
+      }
+      for (; b < a.nblocks; ++b) v[0] += __ldcg(src + b * st);
+      gS[idx] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
     }
   }
   // score / reparam: per-sample log p(z_s) - log q(z_s), one warp per sample
@@ -173,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       double acc = 0.0;
       for (int d = lane; d < P; d += 32) {
         const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
-        const float e = eps_value(a, iter, s, d, P);
+        const float e = epsS[s * PP + d];
         const float zv = a.mu[d] + sig[d] * e;
         const float ps = m.prior_scale[d];
         const float zp = (zv - m.prior_loc[d]) / ps;
@@ -238,7 +259,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     if (a.method == EDG_KLQP_REPARAM_KL) {
       float sg_mu = 0.0f, sg_sig = 0.0f;
       for (int s = 0; s < a.S; ++s) {
-        const float e = eps_value(a, iter, s, d, P);
+        const float e = epsS[s * PP + d];
         const float g = gS[s * PP + d];
         sg_mu += g;
         sg_sig += g * e;
@@ -249,7 +270,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     } else if (a.method == EDG_KLQP_REPARAM) {
       float acc_mu = 0.0f, acc_sig = 0.0f;
       for (int s = 0; s < a.S; ++s) {
-        const float e = eps_value(a, iter, s, d, P);
+        const float e = epsS[s * PP + d];
         const float zv = mu + sg * e;
         const float dfdz = gS[s * PP + d] - lsc * (zv - pl) / (ps * ps) + lsc * (zv - mu) / (sg * sg);
         const float dlq_dmu = (zv - mu) / (sg * sg);
@@ -262,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     } else {
       float acc_mu = 0.0f, acc_sig = 0.0f;
       for (int s = 0; s < a.S; ++s) {
-        const float e = eps_value(a, iter, s, d, P);
+        const float e = epsS[s * PP + d];
         const float zv = mu + sg * e;
         const float w = (float)(llS[s] + lsig[s]);
         acc_mu += lsc * (zv - mu) / (sg * sg) * w;
@@ -631,7 +652,7 @@ extern "C" size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg
 
 template <int CT>
 static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
-  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4;
+  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4 + (size_t)a.Spad * m.PP * 4;
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED, "P=%d too large for KLqp kernel", m.P);
   EDG_REQUIRE(a.S * 2 + 8 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
   EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,

@@ -270,15 +270,21 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
       }
     }
   }
-  // ---- FP64 reduction of the log-lik partials
+  // ---- FP64 reduction of the log-lik partials: one warp per vector, lanes
+  // over the RT / 2 row-pair partials, then a fixed-order shuffle tree (GB300
+  // runs FP64 at a small fraction of its FP32 rate, so a serial sum of RT / 2
+  // terms by one thread per vector is slow)
   if (need_ll) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) S.llred[rp * CT + 4 * cq + j] = kll[j].value();
     __syncthreads();
-    if (tid < CT) {
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int c = warp; c < CT; c += kThreads / 32) {
       double s = 0.0;
-      for (int q = 0; q < RT / 2; ++q) s += S.llred[q * CT + tid];
-      S.ll[tid] = s * (double)dscale;
+      for (int q = lane; q < RT / 2; q += 32) s += S.llred[q * CT + c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) S.ll[c] = s * (double)dscale;
     }
   }
   __syncthreads();
