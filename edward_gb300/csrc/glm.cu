@@ -114,10 +114,13 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   const int P = m.P, PP = m.PP;
   const int64_t t = *(volatile int64_t*)&a.state->t;
   const uint32_t iter = (uint32_t)t;
+  const int rb = blockIdx.x * a.chunk, re = min(m.N, rb + a.chunk);
+  // the first X tile's copy overlaps the draws below
+  if (re > rb) issue_tile<CT>(m, S.Xs, S.ys, rb, re);
+  cp_async_commit();
   for (int d = threadIdx.x; d < PP; d += kThreads) sig[d] = d < P ? softplusf(a.rho[d]) : 0.0f;
   init_x_pad<CT>(m, S);
   __syncthreads();
-  const int rb = blockIdx.x * a.chunk, re = min(m.N, rb + a.chunk);
   const bool need_grad = a.method != EDG_KLQP_SCORE;
   for (int s0 = 0; s0 < a.S; s0 += CT) {
     for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       S.Zt[d * CT + c] = zv;
     }
     __syncthreads();
-    glm_grad_eval<CT>(m, rb, re, S, true, need_grad, a.dscale);
+    glm_grad_eval<CT>(m, rb, re, S, true, need_grad, a.dscale, s0 == 0);
     for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
       const int c = idx / PP;
       if (s0 + c < a.S && need_grad)
@@ -175,17 +178,24 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     llS[s] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   }
   if (need_grad) {
-    for (int idx = threadIdx.x; idx < a.S * PP; idx += kThreads) {
-      const float* src = a.ws_g + idx;
+    // the S x P entries in use (one per thread for small problems; the padding
+    // columns are never read)
+    for (int q = threadIdx.x; q < a.S * P; q += kThreads) {
+      const int sq = q / P, dq = q - sq * P;
+      const float* src = a.ws_g + sq * PP + dq;
       const size_t st = (size_t)a.Spad * PP;
-      float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-      int b = 0;
-      for (; b + 8 <= a.nblocks; b += 8) {
+      float v[16];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] += __ldcg(src + (b + k) * st);
+      for (int k = 0; k < 16; ++k) v[k] = 0.0f;
+      int b = 0;
+      for (; b + 16 <= a.nblocks; b += 16) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] += __ldcg(src + (b + k) * st);
       }
       for (; b < a.nblocks; ++b) v[0] += __ldcg(src + b * st);
-      gS[idx] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+#pragma unroll
+      for (int k = 1; k < 16; ++k) v[0] += v[k];
+      gS[sq * PP + dq] = v[0];
     }
   }
   // score / reparam: per-sample log p(z_s) - log q(z_s), one warp per sample

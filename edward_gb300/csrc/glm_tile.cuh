@@ -135,7 +135,8 @@ __device__ __forceinline__ void lik_term(const GLMDev& m, float y, float eta, fl
 // results (multiplied by dscale) and a __syncthreads() has been done.
 template <int CT>
 __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const GradSmem& S,
-                              bool need_ll, bool need_grad, float dscale) {
+                              bool need_ll, bool need_grad, float dscale,
+                              bool first_issued = false) {
   constexpr int RT = Tile<CT>::RT, CQ = Tile<CT>::CQ;
   const int tid = threadIdx.x;
   const int PP = m.PP, P4 = PP / 4;
@@ -164,8 +165,12 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
   Kahan kll[4];
 
   const int ntiles = (row_end - row_begin + RT - 1) / RT;
-  if (ntiles > 0) issue_tile<CT>(m, S.Xs, S.ys, row_begin, row_end);
-  cp_async_commit();
+  // (first_issued: the caller already issued and committed the first tile
+  // into buffer 0, so that its copy overlaps the caller's own set-up work)
+  if (!first_issued) {
+    if (ntiles > 0) issue_tile<CT>(m, S.Xs, S.ys, row_begin, row_end);
+    cp_async_commit();
+  }
   for (int it = 0; it < ntiles; ++it) {
     const int buf = it & 1;
     if (it + 1 < ntiles)
