@@ -125,6 +125,8 @@ _SIGS = {
     "edg_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32,
                            c_int64, c_void_p, c_int32, c_int64, c_void_p, c_int32, c_int64, c_int32,
                            c_int32, c_void_p, c_size_t, c_void_p]),
+    "edg_gemm_status": (c_int32, [c_void_p, c_void_p]),
+    "edg_check_bounded_wait": (c_int32, [c_void_p, c_void_p]),
     "edg_bnn_num_params": (c_int32, [c_int32, c_int32, c_int32]),
     "edg_bnn_workspace_bytes": (c_size_t, [ctypes.POINTER(EdgBNN), c_int32]),
     "edg_bnn_klqp_step": (c_int32, [ctypes.POINTER(EdgBNN), ctypes.POINTER(EdgOpt), c_void_p,

@@ -128,5 +128,23 @@ struct GLMDev {
 int make_glm(const edg_glm_t* g, GLMDev* out);
 
 __host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
+// Byte counts of workspaces: rounded in size_t (an int round-up would wrap
+// once a workspace passes 2 GiB and accept an undersized buffer).
+__host__ __device__ constexpr size_t round_up_bytes(size_t a, size_t b) {
+  return (a + b - 1) / b * b;
+}
+
+// Raises a kernel's dynamic shared-memory limit on the CURRENT device.  The
+// runtime keeps this attribute per device, so it is set on every launch
+// (a host-side call of a few hundred nanoseconds) rather than cached once per
+// process, which would leave a second device without it.
+template <typename Kernel>
+inline int set_max_dyn_smem(Kernel kernel, size_t bytes, const char* what) {
+  const cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "%s: raising the shared-memory limit to %zu bytes: %s",
+                                    what, bytes, cudaGetErrorString(e));
+  return EDG_OK;
+}
 
 }  // namespace edg

@@ -35,6 +35,11 @@ int sum_partials(const float* part, int splits, int batch, int M, int N, float* 
 }  // namespace tcg
 }  // namespace edg
 
+namespace edg {
+// Result word of the bounded-wait self test.
+__device__ int32_t g_selftest_word;
+}  // namespace edg
+
 using namespace edg;
 
 extern "C" size_t edg_gemm_workspace_bytes(int32_t engine, int32_t M, int32_t N, int32_t K,
@@ -80,4 +85,55 @@ extern "C" int edg_gemm(int32_t engine, int32_t ta, int32_t tb, int32_t M, int32
                                   simt::EpiIdentity{}, kchunk, part, nullptr, st);
   return tcg::gemm<true, true>(A, B, C, M, N, K, lda, ldb, ldc, sA, sB, sC, batch,
                                simt::EpiIdentity{}, kchunk, part, nullptr, st);
+}
+
+extern "C" int edg_gemm_status(int32_t* status, void* stream) {
+  EDG_REQUIRE(status, EDG_E_NULL, "status must not be NULL");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "edg_gemm_status: %s", cudaGetErrorString(e));
+  unsigned v = 0;
+  e = cudaMemcpyFromSymbol(&v, tcg::g_gemm_err, sizeof(v));
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "edg_gemm_status: %s", cudaGetErrorString(e));
+  const unsigned zero = 0;
+  e = cudaMemcpyToSymbol(tcg::g_gemm_err, &zero, sizeof(zero));
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "edg_gemm_status: %s", cudaGetErrorString(e));
+  *status = v ? -(int32_t)v : EDG_OK;  // the kernels store -EDG_E_TIMEOUT
+  return EDG_OK;
+}
+
+// ---------------------------------------------------------------- bounded-wait self test
+namespace edg {
+// One warp waits on an mbarrier that nothing arrives on, with the bounded
+// wait every tensor-core kernel uses; the wait gives up after ~2^31 cycles
+// (about one second) and the timeout is recorded in *out.
+__global__ void bounded_wait_selftest_kernel(int32_t* out) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ volatile int err;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(ptx::smem_u32(&bar), 1);
+    err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  ptx::mbar_wait(ptx::smem_u32(&bar), 0, &err);
+  __syncthreads();
+  if (threadIdx.x == 0) *out = err ? EDG_E_TIMEOUT : EDG_OK;
+}
+}  // namespace edg
+
+extern "C" int edg_check_bounded_wait(int32_t* status, void* stream) {
+  EDG_REQUIRE(status, EDG_E_NULL, "status must not be NULL");
+  int32_t* d = nullptr;
+  void* a = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&a, g_selftest_word);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "edg_check_bounded_wait: %s", cudaGetErrorString(e));
+  d = reinterpret_cast<int32_t*>(a);
+  cudaStream_t st = (cudaStream_t)stream;
+  bounded_wait_selftest_kernel<<<1, 32, 0, st>>>(d);
+  int rc = check_launch("bounded_wait_selftest_kernel");
+  if (rc) return rc;
+  e = cudaMemcpyAsync(status, d, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "edg_check_bounded_wait: %s", cudaGetErrorString(e));
+  return EDG_OK;
 }

@@ -474,6 +474,9 @@ __global__ void splitk_sum_kernel(const float* __restrict__ part, int splits, in
   }
 }
 
+// Per-device status word of the GEMMs launched without a caller error word
+// (edg_gemm): a bounded wait that gives up stores -EDG_E_TIMEOUT here; it stays
+// set until edg_gemm_status reads and clears it.
 __device__ unsigned g_gemm_err;
 
 inline int sm_count() {
@@ -510,20 +513,20 @@ int gemm(const float* A, const float* B, float* C, int M, int N, int K, int lda,
   p.part = part;
   if (p.splits > 1 && !part) return EDG_E_NULL;
   if (!err) {
+    // the calling device's status word (looked up on every call: the address
+    // is per device and does not outlive a device reset)
     void* a = nullptr;
-    cudaGetSymbolAddress(&a, g_gemm_err);
+    const cudaError_t e = cudaGetSymbolAddress(&a, g_gemm_err);
+    if (e != cudaSuccess || !a)
+      return fail(EDG_E_CUDA, "gemm status word: %s", cudaGetErrorString(e));
     err = reinterpret_cast<unsigned*>(a);
   }
   p.err = err;
-  static bool attr_set = false;  // one kernel per Epi, owned by this translation unit
-  if (!attr_set) {
-    cudaFuncSetAttribute(gemm_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kSmemBytes);
-    attr_set = true;
-  }
+  int rc = set_max_dyn_smem(gemm_tc_kernel<Epi>, kSmemBytes, "gemm_tc_kernel");
+  if (rc) return rc;
   const int grid = (int)std::min<int64_t>(p.total, sm_count());
   gemm_tc_kernel<Epi><<<grid, kThreads, kSmemBytes, st>>>(p, epi);
-  int rc = check_launch("gemm_tc_kernel");
+  rc = check_launch("gemm_tc_kernel");
   if (rc || p.splits == 1) return rc;
   const int64_t total = (int64_t)M * N * batch;
   splitk_sum_kernel<<<(int)std::min<int64_t>((total + 255) / 256, 8 * sm_count()), 256, 0, st>>>(

@@ -583,7 +583,8 @@ static int launch_partial(const GLMDev& m, const float* Z, int B, const GradPlan
   const size_t sm = grad_smem_bytes<CT>(m.PP);
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED,
               "P=%d needs %zu bytes of shared memory", m.P, sm);
-  cudaFuncSetAttribute(glm_partial_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int rc = set_max_dyn_smem(glm_partial_kernel<CT>, sm, "glm_partial_kernel");
+  if (rc) return rc;
   dim3 grid(p.nchunks, p.ntiles);
   glm_partial_kernel<CT><<<grid, kThreads, sm, st>>>(m, Z, B, p.chunk, dscale, wg, wl, p.Bpad,
                                                      need_grad);
@@ -598,7 +599,7 @@ extern "C" size_t edg_glm_logjoint_grad_workspace_bytes(const edg_glm_t* model, 
   GLMDev m;
   if (make_glm(model, &m) != EDG_OK || B <= 0) return 0;
   const GradPlan p = plan_grad(m, B);
-  return round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+  return round_up_bytes(p.ws_g_bytes, 256) + p.ws_ll_bytes;
 }
 
 extern "C" int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int32_t B,
@@ -612,12 +613,12 @@ extern "C" int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int
   EDG_REQUIRE(B > 0, EDG_E_SHAPE, "B must be positive (got %d)", B);
   if (!lp_out && !grad_out) return EDG_OK;
   const GradPlan p = plan_grad(m, B);
-  const size_t need = round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+  const size_t need = round_up_bytes(p.ws_g_bytes, 256) + p.ws_ll_bytes;
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
   float* wg = reinterpret_cast<float*>(workspace);
   double* wl = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) +
-                                         round_up((int)p.ws_g_bytes, 256));
+                                         round_up_bytes(p.ws_g_bytes, 256));
   cudaStream_t st = (cudaStream_t)stream;
   const int ng = grad_out ? 1 : 0;
   switch (p.CT) {
@@ -657,7 +658,7 @@ extern "C" size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg
   GLMDev m;
   if (!cfg || make_glm(model, &m) != EDG_OK || cfg->n_samples <= 0) return 0;
   const KlqpPlan p = plan_klqp(m, cfg->n_samples);
-  return round_up((int)p.ws_g, 256) + p.ws_ll;
+  return round_up_bytes(p.ws_g, 256) + p.ws_ll;
 }
 
 template <int CT>
@@ -667,7 +668,8 @@ static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
   EDG_REQUIRE(a.S * 2 + 8 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
   EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,
               "n_samples too large");
-  cudaFuncSetAttribute(klqp_glm_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int rc = set_max_dyn_smem(klqp_glm_kernel<CT>, sm, "klqp_glm_kernel");
+  if (rc) return rc;
   klqp_glm_kernel<CT><<<a.nblocks, kThreads, sm, st>>>(m, a);
   return check_launch("klqp_glm_kernel");
 }
@@ -690,7 +692,7 @@ extern "C" int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg,
   EDG_REQUIRE(opt->optimizer >= 0 && opt->optimizer <= 5, EDG_E_VALUE, "unknown optimizer %d",
               opt->optimizer);
   const KlqpPlan p = plan_klqp(m, cfg->n_samples);
-  const size_t need = round_up((int)p.ws_g, 256) + p.ws_ll;
+  const size_t need = round_up_bytes(p.ws_g, 256) + p.ws_ll;
   EDG_REQUIRE(workspace && workspace_bytes >= need, EDG_E_WORKSPACE,
               "workspace of %zu bytes needed (got %zu)", need, workspace_bytes);
   KlqpArgs a;
@@ -712,7 +714,7 @@ extern "C" int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg,
   a.grad_out = grad_out;
   a.apply = apply;
   a.ws_g = reinterpret_cast<float*>(workspace);
-  a.ws_ll = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) + round_up((int)p.ws_g, 256));
+  a.ws_ll = reinterpret_cast<double*>(reinterpret_cast<char*>(workspace) + round_up_bytes(p.ws_g, 256));
   cudaStream_t st = (cudaStream_t)stream;
   switch (p.CT) {
     case 8: return launch_klqp<8>(m, a, st);
@@ -727,7 +729,8 @@ static int launch_hmc(const GLMDev& m, const HmcArgs& a, cudaStream_t st) {
   const size_t sm = hmc_smem_bytes<CT>(m.PP);
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED,
               "P=%d needs %zu bytes of shared memory for %d chains per block", m.P, sm, CT);
-  cudaFuncSetAttribute(hmc_glm_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int rc = set_max_dyn_smem(hmc_glm_kernel<CT>, sm, "hmc_glm_kernel");
+  if (rc) return rc;
   const int nblocks = (a.C + CT - 1) / CT;
   hmc_glm_kernel<CT><<<nblocks, kThreads, sm, st>>>(m, a);
   return check_launch("hmc_glm_kernel");
@@ -821,7 +824,7 @@ extern "C" int edg_glm_logjoint_grad_noalloc(const edg_glm_t* model, const float
   EDG_REQUIRE(B > 0, EDG_E_SHAPE, "B must be positive (got %d)", B);
   if (!lp_out && !grad_out) return EDG_OK;
   const GradPlan p = plan_grad(m, B);
-  const size_t need = round_up((int)p.ws_g_bytes, 256) + p.ws_ll_bytes;
+  const size_t need = round_up_bytes(p.ws_g_bytes, 256) + p.ws_ll_bytes;
   EDG_REQUIRE(need <= kNoAllocScratchBytes, EDG_E_WORKSPACE,
               "this call needs %zu bytes of scratch but the fixed scratch holds %zu bytes; "
               "split the %d vectors into smaller batches or use edg_glm_logjoint_grad",
@@ -831,7 +834,7 @@ extern "C" int edg_glm_logjoint_grad_noalloc(const edg_glm_t* model, const float
   if (rc) return rc;
   float* wg = reinterpret_cast<float*>(scratch);
   double* wl = reinterpret_cast<double*>(reinterpret_cast<char*>(scratch) +
-                                         round_up((int)p.ws_g_bytes, 256));
+                                         round_up_bytes(p.ws_g_bytes, 256));
   cudaStream_t st = (cudaStream_t)stream;
   const int ng = grad_out ? 1 : 0;
   switch (p.CT) {

@@ -384,7 +384,8 @@ extern "C" int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, i
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   EDG_REQUIRE((int)sm <= optin, EDG_E_UNSUPPORTED, "max_D=%d needs %zu bytes of shared memory",
               model->max_D, sm);
-  cudaFuncSetAttribute(hmc_hier_kernel<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int rc_attr = set_max_dyn_smem(hmc_hier_kernel<CT>, sm, "hmc_hier_kernel");
+  if (rc_attr) return rc_attr;
   const int64_t nblocks = (int64_t)a.I * a.tiles_per_inst;
   EDG_REQUIRE(nblocks < (1ll << 31), EDG_E_SHAPE, "too many instances x chain tiles");
   hmc_hier_kernel<CT><<<(unsigned)nblocks, kThreads, sm, (cudaStream_t)stream>>>(a);

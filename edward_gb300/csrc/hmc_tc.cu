@@ -821,12 +821,8 @@ extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, 
   a.u_ovr = u_override;
   a.ratio_out = ratio_out;
   const size_t sm = smem_bytes(PP);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(hmc_glm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem_bytes(64));
-    attr_done = true;
-  }
+  rc = set_max_dyn_smem(hmc_glm_tc_kernel, sm, "hmc_glm_tc_kernel");
+  if (rc) return rc;
   const int nclusters = (C + kCT - 1) / kCT;
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3(nclusters * R);

@@ -173,7 +173,9 @@ int edg_glm_logjoint_grad(const edg_glm_t* model, const float* Z, int32_t B,
  *    P = 51 over 10,000 rows need 1.8 MB).
  *  - The first call on each device looks up the array's device address
  *    (cudaGetSymbolAddress) and caches it; make that first call before any
- *    stream capture.
+ *    stream capture.  The cached address belongs to the device's current
+ *    primary context: after cudaDeviceReset (or anything else that destroys
+ *    that context) the process must not call this entry point again.
  *  - Every call on a device uses the same array, so calls that overlap on the
  *    GPU (different streams, or threads without ordering) race and corrupt
  *    each other's results; serialise them on one stream.  Nothing needs to be
@@ -208,7 +210,9 @@ int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg, const edg_o
  * EDG_GEMM_TC: tcgen05 tensor cores with 3xTF32 (operands split hi/lo in
  * flight, FP32 accumulation); kchunk > 0 splits K into chunks of kchunk rows
  * summed in FP32 (workspace: edg_gemm_workspace_bytes).  EDG_GEMM_SIMT: FP32
- * CUDA cores. */
+ * CUDA cores.  The tensor-core kernel's waits are bounded: one that gives up
+ * leaves C incomplete and sets the device's GEMM status word, which
+ * edg_gemm_status reports. */
 enum { EDG_GEMM_TC = 0, EDG_GEMM_SIMT = 1 };
 size_t edg_gemm_workspace_bytes(int32_t engine, int32_t M, int32_t N, int32_t K, int32_t batch,
                                 int32_t kchunk);
@@ -216,6 +220,18 @@ int edg_gemm(int32_t engine, int32_t ta, int32_t tb, int32_t M, int32_t N, int32
              const float* A, int32_t lda, int64_t sA, const float* B, int32_t ldb, int64_t sB,
              float* C, int32_t ldc, int64_t sC, int32_t batch, int32_t kchunk, void* workspace,
              size_t workspace_bytes, void* stream);
+/* Status of the edg_gemm calls on the current device since the last query:
+ * synchronises `stream`, stores EDG_OK or EDG_E_TIMEOUT (a bounded wait of a
+ * tensor-core GEMM gave up, its C is incomplete) in *status and clears the
+ * word.  Calls on several streams of one device share the word. */
+int edg_gemm_status(int32_t* status, void* stream);
+
+/* Self test of the bounded device-side wait that every tensor-core kernel
+ * uses (no counterpart in the reference): one warp waits on an mbarrier that
+ * nothing completes; the wait gives up after about one second.  Synchronises
+ * `stream` and stores the kernel's verdict in *status: EDG_E_TIMEOUT when the
+ * wait gave up and returned as designed.  The context stays usable. */
+int edg_check_bounded_wait(int32_t* status, void* stream);
 
 /* ---------------------------------------------------------------- Bayesian NN
  * KLqp for the regression network h1 = tanh(X W0 + b0), h2 = tanh(h1 W1 + b1),

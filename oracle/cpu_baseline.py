@@ -11,7 +11,8 @@ module reproduces the reference's execution structure in NumPy FP32:
   fresh log-joint graph: a GEMV over X (``ed.dot``,
   ``edward/util/tensorflow.py:41-47``), the Bernoulli log-prob, and a
   transposed GEMV for ``tf.gradients``; the Metropolis ratio adds two more
-  log-joint evaluations (``hmc.py:100-105``).
+  log-joint evaluations without gradients (``hmc.py:100-105``): per
+  iteration n_steps + 1 gradients and 2 plain log joints.
 * KLqp (``klqp.py:707-769``): one model copy per Monte Carlo sample (GEMV
   forward + GEMV backward each), the analytic KL, then an unfused Adam apply
   (``variational_inference.py:97,120-121``).
@@ -30,6 +31,17 @@ def _softplus(x):
 
 def _sigmoid(x):
     return 0.5 * (1.0 + np.tanh(0.5 * x))
+
+
+def _log_joint(X, y, w, b, prior_loc, prior_scale):
+    """One reference log-joint graph without its gradient (one GEMV over X):
+    the two Metropolis log joints of ``hmc.py:103-104``."""
+    eta = X @ w + b                                              # ed.dot
+    ll = -(np.maximum(eta, 0) - eta * y + np.log1p(np.exp(-np.abs(eta)))).sum(dtype=np.float32)
+    z = np.concatenate([w, [b]]).astype(np.float32)
+    zz = (z - prior_loc) / prior_scale
+    lp = (-0.5 * zz * zz - np.log(prior_scale) - np.float32(0.9189385)).sum(dtype=np.float32)
+    return np.float32(ll + lp)
 
 
 def _log_joint_and_grad(X, y, w, b, prior_loc, prior_scale):
@@ -65,8 +77,8 @@ def hmc_logreg_chain(X, y, z0, n_iter, step_size, n_steps, seed, chain, prior_lo
             zn = zn + eps * r
             _, g = _log_joint_and_grad(X, y, zn[:D], zn[D], prior_loc, prior_scale)
             r = r + np.float32(0.5) * eps * g
-        lj_new, _ = _log_joint_and_grad(X, y, zn[:D], zn[D], prior_loc, prior_scale)
-        lj_old, _ = _log_joint_and_grad(X, y, z[:D], z[D], prior_loc, prior_scale)
+        lj_new = _log_joint(X, y, zn[:D], zn[D], prior_loc, prior_scale)
+        lj_old = _log_joint(X, y, z[:D], z[D], prior_loc, prior_scale)
         ratio = 0.5 * (r0 * r0).sum() - 0.5 * (r * r).sum() + lj_new - lj_old
         if np.log(u) < ratio:
             z = zn

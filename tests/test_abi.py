@@ -53,3 +53,25 @@ def test_library_targets_sm103a():
     """The build uses exactly one -gencode, for sm_103a."""
     from edward_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_workspace_sizes_beyond_2gib(lib):
+    """Workspace sizes are computed in size_t: a batch whose gradient partials
+    pass 4 GiB reports at least the bytes of those partials (an int round-up
+    would wrap to a small value and accept an undersized buffer).  No GPU is
+    needed: the size query only reads the descriptor (fake non-NULL pointers)."""
+    from edward_gb300 import _lib
+    g = _lib.EdgGLM()
+    g.X = g.y = g.prior_loc = g.prior_scale = 0x1000
+    g.N, g.D, g.bias, g.lik, g.lik_scale = 10_000, 255, 1, 0, 1.0
+    f = lib.edg_glm_logjoint_grad_workspace_bytes
+    f.restype = ctypes.c_size_t
+    f.argtypes = [ctypes.POINTER(_lib.EdgGLM), ctypes.c_int32]
+    B, PP = 4_300_000, 256
+    need = f(ctypes.byref(g), B)
+    partials = B * PP * 4 + B * 8            # one row chunk of FP32 gradients + FP64 sums
+    assert partials > 2 ** 32
+    assert need >= partials, (need, partials)
+    assert need % 8 == 0
+    small = f(ctypes.byref(g), 64)
+    assert 0 < small < need

@@ -59,3 +59,37 @@ def test_gemm_tc_aligned_large(cuda):
     err = ((C.double() - ref).abs().max() / ref.abs().max()).item()
     print(f"gemm tc large: max rel err {err:.2e}")
     assert err < 1e-5, err
+
+
+def test_gemm_status_clean_after_gemm(cuda):
+    """edg_gemm reports bounded-wait timeouts through edg_gemm_status; a normal
+    call leaves the status at EDG_OK."""
+    import ctypes
+    from edward_gb300 import _lib, ops
+    A = torch.randn(300, 64, device=cuda)
+    B = torch.randn(64, 200, device=cuda)
+    C = ops.gemm(A, B, 300, 200, 64)
+    st = ctypes.c_int32(99)
+    _lib.call("edg_gemm_status", ctypes.byref(st), _lib.stream_ptr())
+    assert st.value == 0
+    np.testing.assert_allclose(C[0].cpu().numpy(), (A @ B).cpu().numpy(), rtol=1e-4, atol=1e-3)
+
+
+def test_bounded_wait_gives_up_and_context_survives(cuda):
+    """A wait on an mbarrier that nothing completes gives up after about one
+    second with EDG_E_TIMEOUT (the bounded wait of every tensor-core kernel);
+    the CUDA context stays usable afterwards."""
+    import ctypes
+    import time
+    from edward_gb300 import _lib, ops
+    st = ctypes.c_int32(0)
+    t0 = time.perf_counter()
+    _lib.call("edg_check_bounded_wait", ctypes.byref(st), _lib.stream_ptr())
+    dt = time.perf_counter() - t0
+    assert st.value == _lib.EDG_E_TIMEOUT
+    assert dt < 30.0
+    A = torch.randn(128, 32, device=cuda)
+    B = torch.randn(32, 64, device=cuda)
+    C = ops.gemm(A, B, 128, 64, 32)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(C[0].cpu().numpy(), (A @ B).cpu().numpy(), rtol=1e-4, atol=1e-3)

@@ -283,3 +283,41 @@ def test_sbn_baseline_regression_gradient():
         if abs(g) > 1e-8:
             assert np.sign(bp[p] - new_bp[p]) == np.sign(g)
     assert new_stats[2] == 6 and new_stats[5] == pytest.approx(mse(bp))
+
+
+def test_cpu_baseline_hmc_matches_oracle():
+    """The timed CPU restatement (one chain, GEMV per gradient, FP32) follows
+    the same chain as the FP64 oracle fed the same Philox draws."""
+    from oracle.cpu_baseline import hmc_logreg_chain
+    X, y, _, _ = synthetic_logreg(300, 6, seed=3)
+    P = 7
+    m = GLM(X, y, bias=True)
+    f = glm_lj_grad(m)
+    z0 = np.random.default_rng(1).standard_normal((4, P)) * 0.1
+    samples, n_acc = run_hmc(f, z0, 3, 0.02, 4, seed=11)
+    for c in range(4):
+        z, acc = hmc_logreg_chain(X, y, z0[c].astype(np.float32), 3, 0.02, 4, 11, c,
+                                  np.zeros(P, np.float32), np.ones(P, np.float32))
+        assert acc == n_acc[c]
+        np.testing.assert_allclose(z, samples[-1, c], rtol=1e-4, atol=1e-5)
+
+
+def test_cpu_baseline_klqp_matches_oracle():
+    """The timed CPU KLqp step (one model copy per sample, unfused TF Adam)
+    follows the oracle's optimisation trajectory with the same draws."""
+    from oracle.cpu_baseline import klqp_logreg_step
+    from oracle.klqp import default_learning_rate
+    X, y, _, _ = synthetic_logreg(400, 5, seed=2)
+    P = 6
+    m = GLM(X, y, bias=True)
+    mu0 = np.zeros(P)
+    rho0 = np.full(P, -1.0)
+    e_mu, e_rho, e_losses = run_klqp_glm(m, mu0, rho0, 5, 3, seed=21)
+    mu, rho = mu0.astype(np.float32), rho0.astype(np.float32)
+    mm, vv = np.zeros(2 * P, np.float32), np.zeros(2 * P, np.float32)
+    for t in range(5):
+        loss = klqp_logreg_step(X, y, mu, rho, mm, vv, t, 3, 21, np.zeros(P, np.float32),
+                                np.ones(P, np.float32), default_learning_rate(t))
+        assert abs(loss - e_losses[t]) <= 1e-4 * abs(e_losses[t])
+    np.testing.assert_allclose(mu, e_mu, rtol=1e-3, atol=1e-4)
+    np.testing.assert_allclose(rho, e_rho, rtol=1e-3, atol=1e-4)
