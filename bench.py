@@ -87,6 +87,70 @@ def cpu_baseline(budget_s=10.0, procs=None):
                       f"NumPy FP32, BLAS 1 thread/process), {wall:.1f} s wall"}
 
 
+# ------------------------------------------------------------------ KLqp workload (the ELBO-gradient half)
+
+KLQP_S, KLQP_ITERS, KLQP_SEED = 5, 1000, 1
+KLQP_METRIC = "KLqp ELBO-grad evals/s (Bayesian logistic regression, S=5)"
+KLQP_UNIT = "evals/s"
+
+
+def klqp_init():
+    """q initialisation shared by the GPU run and the CPU leg: mu = 0 and
+    rho ~ N(0, 1) (seed 2), so both optimise from the same point with the
+    same Philox draws (seed 1)."""
+    import numpy as np
+    P = N_FEAT + 1
+    return np.zeros(P, np.float32), np.random.default_rng(2).standard_normal(P).astype(np.float32)
+
+
+def _cpu_klqp_worker(n_steps):
+    import numpy as np
+    from oracle.cpu_baseline import klqp_logreg_step
+    from oracle.klqp import default_learning_rate
+    X, y, _ = make_data()
+    P = N_FEAT + 1
+    mu, rho = klqp_init()
+    m = np.zeros(2 * P, np.float32)
+    v = np.zeros(2 * P, np.float32)
+    loc, scale = np.zeros(P, np.float32), np.ones(P, np.float32)
+    losses = []
+    t0 = time.perf_counter()
+    for t in range(n_steps):
+        losses.append(klqp_logreg_step(X, y, mu, rho, m, v, t, KLQP_S, KLQP_SEED, loc, scale,
+                                       default_learning_rate(t)))
+    return time.perf_counter() - t0, losses
+
+
+def cpu_klqp_baseline(n_steps=KLQP_ITERS):
+    """The reference-structured CPU KLqp (one model copy per Monte Carlo
+    sample, GEMV forward + GEMV backward each, analytic KL, unfused TF Adam;
+    NumPy FP32) for the whole 1,000-step optimisation, in one spawned process
+    whose BLAS uses every host core (the reference's TF intra-op pool).
+    Returns the cpu_baseline dict and the final ELBO per datum (mean of the
+    last 100 losses / N)."""
+    import multiprocessing as mp
+    import numpy as np
+    ncores = len(os.sched_getaffinity(0))
+    keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ[k] = str(ncores)
+    try:
+        with mp.get_context("spawn").Pool(1) as pool:
+            dt, losses = pool.apply(_cpu_klqp_worker, (n_steps,))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    elbo = -float(np.mean(losses[-100:])) / N_ROWS
+    cb = {"value": n_steps / dt, "unit": KLQP_UNIT, "cores": ncores, "kind": "port",
+          "sample": f"the full {n_steps}-step optimisation (S={KLQP_S}, analytic KL, TF Adam, "
+                    f"staircase lr), one process, BLAS on {ncores} threads, {dt:.1f} s wall"}
+    return cb, elbo
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -101,13 +165,20 @@ def run_reference(args):
     val = statistics.median(s["value"] for s in steps)
     cb = dict(cb)
     cb["value"] = val
+    kcb, kelbo = cpu_klqp_baseline()
+    klqp = {"metric": KLQP_METRIC, "value": kcb["value"], "unit": KLQP_UNIT,
+            "higher_is_better": True, "config": {"workload": "klqp_logreg_N10000_D50_S5_T1000"},
+            "cpu_baseline": kcb, "final_elbo_per_datum": kelbo,
+            "e2e": {"value": kcb["value"], "unit": KLQP_UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * N_CHAINS * N_LEAP / val, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(CONFIG, l2_flush="n/a (CPU)"), "impl": "reference",
             "cpu_baseline": cb,
-            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "klqp": klqp}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -181,15 +252,18 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     # CPU baseline first (spawned pool before heavy GPU work), rank 0 at N=1 only
-    cb = None
+    cb = cpu_klqp = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(budget_s=args.cpu_budget)
+        if not args.no_extras:
+            cpu_klqp = cpu_klqp_baseline()
 
     import edward_gb300 as ed
     from edward_gb300 import _lib
     from edward_gb300.models import Bernoulli, Empirical, Normal
 
     X, y, z0 = make_data()
+    tf32 = None if args.no_extras else measure_tf32_peak(dev)
     T = args.warmup + args.steps
     w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
     b = Normal(loc=0.0, scale=1.0)
@@ -250,21 +324,19 @@ def run_gpu(args):
     flops_per_launch = 4.0 * N_ROWS * P * N_CHAINS * N_LEAP
     avg_launch_ms = statistics.mean(per_step)
     achieved = flops_per_launch / (avg_launch_ms / 1e3) / 1e12
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-        bf16 = float(peaks["bf16_tflops"])
-        src = "MEASURED_PEAKS.json bf16_tflops"
-    except (OSError, KeyError, ValueError):
-        bf16 = 1900.0
-        src = "fallback 1.9 PFLOP/s bf16"
-    peak = bf16 / 2.0 / 3.0
+    peak, psrc = tensor_peak(tf32)
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": read_traffic(inf.engine),
-            "kernel": kernel_name,
-            "peak_source": f"{src} {bf16:g} / 2 (TF32 rate) / 3 (3xTF32 passes), of measured",
+            "kernel": kernel_name, "peak_source": psrc,
+            "tf32_tflops_measured": tf32,
             "algorithmic_flops_per_launch": flops_per_launch}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        extras["klqp"] = run_klqp_record(args, dev, X, y, cpu_klqp, flush, tf32)
+        posterior, target_hmc = run_hmc_posterior_and_target(args, dev, X, y, z0)
+        extras["posterior"] = posterior
+        extras["target"] = {"hmc": target_hmc, "klqp": run_klqp_target(X, y, dev)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -277,6 +349,7 @@ def run_gpu(args):
                 "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "wall_s_timed_region": wall}
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -372,11 +445,436 @@ def run_e2e(args, inf, X, y, z0, dev):
                     "wall clock"}
 
 
+def measure_tf32_peak(dev, n=8192, reps=10):
+    """Dense TF32 tensor-core rate of this GPU, measured here: cuBLAS FP32 GEMM
+    with TF32 math (torch.matmul with allow_tf32), n^3, best of `reps` after
+    warm-up, CUDA events.  The 3xTF32 kernels' roofline is this rate / 3."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(n, n, device=dev)
+        b = torch.randn(n, n, device=dev)
+        c = torch.empty(n, n, device=dev)
+        for _ in range(3):
+            torch.matmul(a, b, out=c)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b, c
+        torch.cuda.empty_cache()
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def tensor_peak(tf32_tflops):
+    """(3xTF32 peak, source) from the TF32 rate measured in this run, else from
+    MEASURED_PEAKS.json's bf16 rate / 2."""
+    if tf32_tflops:
+        return tf32_tflops / 3.0, (f"cuBLAS TF32 GEMM 8192^3 measured in this run: "
+                                   f"{tf32_tflops:.0f} TFLOP/s / 3 (3xTF32 passes), of measured")
+    p, src = _peak_3xtf32()
+    return p, src
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs, of measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s, of fallback"
+
+
+def _klqp_inference(X, y):
+    import torch
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Normal
+    w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
+    b = Normal(loc=0.0, scale=1.0)
+    yv = Bernoulli(logits=ed.dot(X, w) + b)
+    inf = ed.KLqp([w, b], data={yv: y})
+    inf.initialize(n_samples=KLQP_S, n_iter=KLQP_ITERS, n_print=0)
+    inf._cfg.seed = KLQP_SEED
+    mu0, rho0 = klqp_init()
+
+    def restart():
+        inf.reset()
+        inf._graphs = {}
+        inf._mu.copy_(torch.as_tensor(mu0))
+        inf._rho.copy_(torch.as_tensor(rho0))
+    restart()
+    return inf, restart
+
+
+def run_klqp_record(args, dev, X, y, cpu_klqp, flush, tf32):
+    """The KLqp half of the metric on the S = 5 logistic regression: ELBO-grad
+    evals/s of the fused step (one launch per step: Philox eps, X z for all
+    samples, log-likelihood + adjoint, analytic KL, Adam), device-timed with an
+    L2 flush before every step; the whole 1,000-step run and its final ELBO;
+    the same step end to end through the C ABI with host buffers."""
+    import ctypes
+    import numpy as np
+    import torch
+    from edward_gb300 import _lib
+    inf, restart = _klqp_inference(X, y)
+    stream = torch.cuda.current_stream()
+    # the full optimisation: 900 steps from CUDA graphs, the last 100 read one by one
+    t0 = time.perf_counter()
+    for _ in range(18):
+        inf.steps(50)
+    losses = []
+    for _ in range(100):
+        inf._step(apply=True)
+        losses.append(float(inf._read_state().loss))
+    torch.cuda.synchronize()
+    run_wall = time.perf_counter() - t0
+    final_elbo = -float(np.mean(losses)) / N_ROWS
+    assert inf.t == KLQP_ITERS
+    # device-timed steps, L2 flushed before each (outside the events)
+    restart()
+    for _ in range(5):
+        inf._step(apply=True)
+    torch.cuda.synchronize()
+    K = args.klqp_steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    with ClockSampler(dev.index or 0) as clk:
+        for i in range(K):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            inf._step(apply=True)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / K
+    # the same steps replayed back to back from a CUDA graph (X L2-resident)
+    restart()
+    inf.steps(50)
+    inf.steps(50)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(10):
+        inf.steps(50)
+    b.record()
+    b.synchronize()
+    ms_graph = a.elapsed_time(b) / 500
+    # end to end through the C ABI: X, y and the optimiser state copied in from
+    # pinned host memory and the state copied back every step
+    P = N_FEAT + 1
+    sizes = [("X", X.size * 4), ("y", y.size * 4), ("mu", P * 4), ("rho", P * 4),
+             ("slots", 4 * P * 4), ("st", ctypes.sizeof(_lib.EdgState))]
+    off, o = {}, 0
+    for name, nbytes in sizes:
+        off[name] = (o, nbytes)
+        o += (nbytes + 255) // 256 * 256
+    h = torch.zeros(o, dtype=torch.uint8).pin_memory()
+
+    def hview(name, dtype):
+        o0, nb = off[name]
+        return h[o0:o0 + nb].view(dtype)
+    mu0, rho0 = klqp_init()
+    hview("X", torch.float32).copy_(torch.as_tensor(X).reshape(-1))
+    hview("y", torch.float32).copy_(torch.as_tensor(y).reshape(-1))
+    hview("mu", torch.float32).copy_(torch.as_tensor(mu0))
+    hview("rho", torch.float32).copy_(torch.as_tensor(rho0))
+    hview("st", torch.uint8).copy_(_lib.new_state("cpu"))
+    d = torch.empty(o, dtype=torch.uint8, device=dev)
+    base = d.data_ptr()
+    glm = _lib.EdgGLM()
+    glm.X, glm.y, glm.N, glm.D, glm.bias, glm.lik, glm.lik_scale = (
+        base + off["X"][0], base + off["y"][0], N_ROWS, N_FEAT, 1, 0, 1.0)
+    glm.prior_loc = inf._glm.prior_loc.data_ptr()
+    glm.prior_scale = inf._glm.prior_scale.data_ptr()
+    out0 = off["mu"][0]
+    sp = _lib.stream_ptr(stream)
+
+    def e2e_step():
+        d.copy_(h, non_blocking=True)
+        _lib.call("edg_klqp_glm_step", ctypes.byref(glm), ctypes.byref(inf._cfg),
+                  ctypes.byref(inf._opt), ctypes.c_void_p(base + off["mu"][0]),
+                  ctypes.c_void_p(base + off["rho"][0]), ctypes.c_void_p(base + off["slots"][0]),
+                  ctypes.c_void_p(base + off["st"][0]), None, None, 1, _lib.ptr(inf._ws),
+                  inf._ws_bytes, sp)
+        h[out0:].copy_(d[out0:], non_blocking=True)
+        stream.synchronize()
+    for _ in range(5):
+        e2e_step()
+    hview("mu", torch.float32).copy_(torch.as_tensor(mu0))
+    hview("rho", torch.float32).copy_(torch.as_tensor(rho0))
+    hview("slots", torch.float32).zero_()
+    hview("st", torch.uint8).copy_(_lib.new_state("cpu"))
+    t0 = time.perf_counter()
+    for _ in range(K):
+        e2e_step()
+    e2e_dt = time.perf_counter() - t0
+    st_h = _lib.EdgState.from_buffer_copy(bytes(hview("st", torch.uint8).numpy().tobytes()))
+    assert st_h.t == K and np.isfinite(st_h.loss)
+    hbm, hsrc = hbm_peak()
+    alg_bytes = 4.0 * N_ROWS * N_FEAT + 4.0 * N_ROWS
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    rec = {"metric": KLQP_METRIC, "value": 1e3 / ms, "unit": KLQP_UNIT, "steps": K,
+           "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+           "config": {"workload": "klqp_logreg_N10000_D50_S5_T1000", "n_samples": KLQP_S,
+                      "n_iter": KLQP_ITERS, "optimizer": "Adam, lr 0.1 * 0.9^(t/100) staircase",
+                      "l2_flush": "256 MB write before each timed step, outside the events"},
+           "value_graph_l2_resident": 1e3 / ms_graph,
+           "e2e": {"value": K / e2e_dt, "unit": KLQP_UNIT,
+                   "h2d_bytes_per_step": int(o), "d2h_bytes_per_step": int(o - out0),
+                   "path": "edg_klqp_glm_step (C ABI), one packed pinned host buffer "
+                           "[X | y | mu | rho | slots | state] copied in and the optimiser "
+                           "state copied out every step, wall clock"},
+           "gpu_launches": K,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "traffic": read_traffic_file(
+                            "klqp_glm_kernel_logreg_S5.txt"),
+                        "kernel": "klqp_glm_kernel<8> (fused step, 40 blocks)",
+                        "peak_source": hsrc, "algorithmic_bytes_per_launch": alg_bytes,
+                        "note": "2 MB of X per step: launch- and latency-bound by construction"},
+           "final_elbo_per_datum": final_elbo, "run_wall_s_1000_steps": run_wall,
+           "cpu_baseline": cpu_klqp[0] if cpu_klqp else None,
+           "cpu_final_elbo_per_datum": cpu_klqp[1] if cpu_klqp else None,
+           "clocks": clk.summary()}
+    if cpu_klqp:
+        rec["final_elbo_abs_diff_vs_cpu"] = abs(final_elbo - cpu_klqp[1])
+    return rec
+
+
+def plain_klqp_torch(X, y, n_iter, dev):
+    """The plain GPU method for KLqp: the reference's execution on a GPU one op
+    at a time, as TF runs its graph there -- per Monte Carlo sample a copy of
+    the model (GEMV over X, Bernoulli log-likelihood), the analytic KL,
+    autodiff, and an unfused Adam with the staircase learning rate.  Eager
+    torch ops; a comparison arm only (nothing of the library runs in it).
+    Returns (wall seconds, losses)."""
+    import torch
+    import torch.nn.functional as F
+    mu0, rho0 = klqp_init()
+    Xd = torch.as_tensor(X, device=dev)
+    yd = torch.as_tensor(y, device=dev)
+    mu = torch.tensor(mu0, device=dev, requires_grad=True)
+    rho = torch.tensor(rho0, device=dev, requires_grad=True)
+    opt = torch.optim.Adam([mu, rho], lr=0.1, betas=(0.9, 0.999), eps=1e-8)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(KLQP_SEED)
+    losses = torch.empty(n_iter, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(n_iter):
+        for grp in opt.param_groups:
+            grp["lr"] = 0.1 * 0.9 ** (t // 100)
+        sig = F.softplus(rho)
+        ll = 0.0
+        for _ in range(KLQP_S):
+            z = mu + sig * torch.randn(N_FEAT + 1, device=dev, generator=gen)
+            eta = Xd @ z[:N_FEAT] + z[N_FEAT]
+            ll = ll + (yd * eta - F.softplus(eta)).sum()
+        kl = (0.5 * mu * mu + 0.5 * (sig * sig - 1.0) - torch.log(sig)).sum()
+        loss = -(ll / KLQP_S - kl)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        losses[t] = loss.detach()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, losses.cpu().numpy()
+
+
+def run_klqp_target(X, y, dev, chunk=10):
+    """Spec target for KLqp: wall time for the fused step to come within
+    0.1 nat/datum of the plain GPU method's final ELBO (mean of its last 100
+    losses after 1,000 steps), against the plain method's 1,000-step time.
+    The fused run reads the loss after every `chunk` steps (replayed from a
+    CUDA graph) and stops at the first chunk whose ELBO estimate (mean of the
+    last 5 chunk-end losses) is there; the reads count in its time."""
+    import numpy as np
+    import torch
+    plain_wall, plain_losses = plain_klqp_torch(X, y, KLQP_ITERS, dev)
+    plain_elbo = -float(np.mean(plain_losses[-100:])) / N_ROWS
+    inf, restart = _klqp_inference(X, y)
+    inf.steps(chunk)
+    torch.cuda.synchronize()
+    restart()
+    torch.cuda.synchronize()
+    recent, steps, reached = [], 0, None
+    t0 = time.perf_counter()
+    while steps < KLQP_ITERS:
+        inf.steps(chunk)
+        steps += chunk
+        recent.append(float(inf._read_state().loss))
+        est = -float(np.mean(recent[-5:])) / N_ROWS
+        if len(recent) >= 5 and est >= plain_elbo - 0.1:
+            reached = time.perf_counter() - t0
+            break
+    return {"plain_method": "eager per-op GPU form (per-sample GEMV copies, autodiff, "
+                            "unfused Adam), 1,000 steps",
+            "plain_wall_s": plain_wall, "plain_final_elbo_per_datum": plain_elbo,
+            "fused_steps_to_within_0.1_nat": steps if reached is not None else None,
+            "fused_wall_s": reached, "fused_elbo_per_datum_at_stop": est,
+            "wall_time_ratio": (plain_wall / reached) if reached else None}
+
+
+def _hmc_glm(X, y, dev):
+    """Device copy of the logistic-regression model for direct C-ABI runs."""
+    import numpy as np
+    from edward_gb300.compile import GLMSpec
+    from edward_gb300.ops import GLMDevice
+    P = N_FEAT + 1
+    spec = GLMSpec(X=X, y=y, bias=True, lik=0, lik_scale=1.0,
+                   prior_loc=np.zeros(P, np.float32), prior_scale=np.ones(P, np.float32))
+    return GLMDevice(spec, dev)
+
+
+def _hmc_launch(g, tiles, engine, z, gr, lj, cache, n_iter, st, seed, samples=None,
+                moments=None, nacc=None):
+    import ctypes
+    from edward_gb300 import _lib
+    cfg = _lib.EdgHMC()
+    cfg.step_size, cfg.n_steps, cfg.seed = STEP, N_LEAP, seed
+    C = z.shape[0]
+    T = samples.shape[0] if samples is not None else 0
+    if engine == "tc":
+        _lib.call("edg_hmc_glm_tc_run", g.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(tiles),
+                  _lib.ptr(z), _lib.ptr(gr), _lib.ptr(lj), cache, _lib.ptr(nacc), _lib.ptr(st),
+                  _lib.ptr(samples), T, _lib.ptr(moments), None, None, None, _lib.stream_ptr())
+    else:
+        cfg.chains_per_block = 8
+        _lib.call("edg_hmc_glm_run", g.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(z),
+                  _lib.ptr(gr), _lib.ptr(lj), cache, _lib.ptr(nacc), _lib.ptr(st),
+                  _lib.ptr(samples), T, _lib.ptr(moments), None, None, None, _lib.stream_ptr())
+
+
+def run_hmc_posterior_and_target(args, dev, X, y, z0):
+    """Posterior error of the batched sampler and the spec wall-time
+    comparison for HMC on the 10,000 x 50 logistic regression.
+
+    * truth: the batched tensor-core run, 4,096 chains, 200 burn-in
+      iterations, then 300 iterations of running moments (1.2 M draws);
+    * long single-chain run (SIMT engine, one chain, one launch):
+      1,000 burn-in + args.long_chain_iters iterations, its mean and variance
+      against the truth, with its batch-means standard error;
+    * plain GPU method: one chain, one SIMT launch per iteration, the
+      configuration's 2,000 iterations from an N(0, 1) start, mean over the
+      second half; batched form: 4,096 chains, one tensor-core launch per
+      iteration from N(0, 1) starts, mean over the second half of the
+      iterations run so far at checkpoints k = 2, 4, ..., 512; the wall time
+      of the first checkpoint whose posterior-mean error (max over
+      coordinates of |mean - truth| / posterior sd) is at most the plain
+      method's is compared with the plain method's wall time."""
+    import numpy as np
+    import torch
+    from edward_gb300 import _lib
+    P = N_FEAT + 1
+    g = _hmc_glm(X, y, dev)
+    lib = _lib.load()
+    nb = lib.edg_hmc_glm_tc_tiles_bytes(g.ref())
+    tiles = torch.empty(nb, dtype=torch.uint8, device=dev)
+    _lib.call("edg_hmc_glm_tc_prepare", g.ref(), _lib.ptr(tiles), nb, _lib.stream_ptr())
+
+    def fresh(C, start):
+        z = torch.as_tensor(start, device=dev).reshape(C, P).clone()
+        return (z, torch.zeros(C, P, device=dev), torch.zeros(C, dtype=torch.float64, device=dev),
+                _lib.new_state(dev), torch.zeros(C, dtype=torch.int32, device=dev))
+    # truth
+    C = N_CHAINS
+    z, gr, lj, st, nacc = fresh(C, z0)
+    _hmc_launch(g, tiles, "tc", z, gr, lj, 0, 200, st, 11, nacc=nacc)
+    mom = torch.zeros(2, C, P, dtype=torch.float64, device=dev)
+    _hmc_launch(g, tiles, "tc", z, gr, lj, 1, 300, st, 11, moments=mom, nacc=nacc)
+    torch.cuda.synchronize()
+    n_t = 300 * C
+    m_true = (mom[0].sum(0) / n_t).cpu().numpy()
+    v_true = (mom[1].sum(0) / n_t).cpu().numpy() - m_true ** 2
+    sd_true = np.sqrt(v_true)
+    acc_true = float(nacc.double().mean().item()) / 500
+    # long single chain
+    T_long = args.long_chain_iters
+    z, gr, lj, st, nacc = fresh(1, z0[0])
+    _hmc_launch(g, None, "simt", z, gr, lj, 0, 1000, st, 12, nacc=nacc)
+    samp = torch.zeros(T_long + 1000, 1, P, device=dev)
+    t0 = time.perf_counter()
+    _hmc_launch(g, None, "simt", z, gr, lj, 1, T_long, st, 12, samples=samp, nacc=nacc)
+    torch.cuda.synchronize()
+    long_wall = time.perf_counter() - t0
+    s1 = samp[1000:1000 + T_long, 0].double().cpu().numpy()
+    m1, v1 = s1.mean(0), s1.var(0)
+    nbat = 20
+    bm = s1[: T_long // nbat * nbat].reshape(nbat, -1, P).mean(1)
+    se1 = bm.std(0, ddof=1) / np.sqrt(nbat)
+    posterior = {
+        "truth": f"batched tensor-core run, {C} chains x 300 iterations after 200 of burn-in "
+                 f"(acceptance {acc_true:.3f})",
+        "long_single_chain": f"SIMT engine, 1 chain, {T_long} iterations after 1,000 of burn-in, "
+                             f"{long_wall:.2f} s",
+        "long_chain_mean_err_max_over_sd": float(np.max(np.abs(m1 - m_true) / sd_true)),
+        "long_chain_mean_err_max_over_se": float(np.max(np.abs(m1 - m_true) / se1)),
+        "long_chain_var_rel_err_max": float(np.max(np.abs(v1 - v_true) / v_true)),
+        "posterior_sd_range": [float(sd_true.min()), float(sd_true.max())]}
+    # plain GPU method: one chain, one launch per iteration
+    T_plain = 2000
+    z, gr, lj, st, nacc = fresh(1, z0[0])
+    samp = torch.zeros(T_plain, 1, P, device=dev)
+    _hmc_launch(g, None, "simt", z.clone(), gr.clone(), lj.clone(), 0, 1, _lib.new_state(dev), 13)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(T_plain):
+        _hmc_launch(g, None, "simt", z, gr, lj, 1 if i else 0, 1, st, 13, samples=samp, nacc=nacc)
+    torch.cuda.synchronize()
+    plain_wall = time.perf_counter() - t0
+    sp_ = samp[T_plain // 2:, 0].double().cpu().numpy()
+    err_plain = float(np.max(np.abs(sp_.mean(0) - m_true) / sd_true))
+    # batched form: 4,096 chains, one launch per iteration, checkpoints
+    Kmax = 512
+    z, gr, lj, st, nacc = fresh(C, z0)
+    samp = torch.zeros(Kmax, C, P, device=dev)
+    zw, gw, ljw, stw = z.clone(), gr.clone(), lj.clone(), _lib.new_state(dev)
+    _hmc_launch(g, tiles, "tc", zw, gw, ljw, 0, 1, stw, 14)
+    torch.cuda.synchronize()
+    marks, t_mark = [2 ** k for k in range(1, 10)], {}
+    t0 = time.perf_counter()
+    for i in range(Kmax):
+        _hmc_launch(g, tiles, "tc", z, gr, lj, 1 if i else 0, 1, st, 14, samples=samp, nacc=nacc)
+        if i + 1 in marks:
+            torch.cuda.synchronize()
+            t_mark[i + 1] = time.perf_counter() - t0
+    errs = {}
+    reached = None
+    mt = torch.as_tensor(m_true, device=dev)
+    sdt = torch.as_tensor(sd_true, device=dev)
+    for k in marks:
+        mk = samp[k // 2:k].double().mean(dim=(0, 1))
+        errs[k] = float(((mk - mt).abs() / sdt).max().item())
+        if reached is None and errs[k] <= err_plain:
+            reached = k
+    target = {
+        "plain_method": f"one chain, one SIMT launch per iteration, {T_plain} iterations, mean "
+                        f"over the second half",
+        "plain_wall_s": plain_wall, "plain_mean_err_max_over_sd": err_plain,
+        "batched_method": f"{C} chains, one tensor-core launch per iteration, mean over the "
+                          f"second half of the iterations so far",
+        "batched_mean_err_max_over_sd_at": {str(k): v for k, v in errs.items()},
+        "batched_wall_s_at": {str(k): v for k, v in t_mark.items()},
+        "batched_iterations_to_plain_error": reached,
+        "batched_wall_s": t_mark.get(reached) if reached else None,
+        "wall_time_ratio": (plain_wall / t_mark[reached]) if reached else None}
+    return posterior, target
+
+
 def read_traffic(engine):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
     summary (a line 'dram_bytes_per_launch: <int>'), else None."""
     name = "hmc_glm_tc_kernel_logreg_C4096.txt" if engine == "tc" else \
         "hmc_glm_kernel_logreg_C4096.txt"
+    return read_traffic_file(name)
+
+
+def read_traffic_file(name):
     p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
@@ -756,6 +1254,11 @@ def main():
     ap.add_argument("--engine", default="auto", choices=["auto", "tc", "simt"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline HMC measurement only (no KLqp record, posterior error, "
+                         "wall-time target or TF32 peak)")
+    ap.add_argument("--klqp-steps", type=int, default=200)
+    ap.add_argument("--long-chain-iters", type=int, default=20000)
     ap.add_argument("--hier-instances", type=int, default=2048)
     ap.add_argument("--sbn-compare-steps", type=int, default=1000)
     ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn", "sgld"],

@@ -254,11 +254,13 @@ def require_cuda():
     load()
 
 
-def new_state(device, beta1=0.9, beta2=0.999):
-    """Device edg_state_t initialised like TF's Adam accumulators."""
+def new_state(device, beta1=0.9, beta2=0.999, t=0):
+    """Device edg_state_t initialised like TF's Adam accumulators, at
+    iteration t."""
     st = EdgState()
     st.beta1_power = beta1
     st.beta2_power = beta2
+    st.t = t
     host = torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8)
     return host.to(device)
 

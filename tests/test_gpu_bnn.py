@@ -66,8 +66,8 @@ def test_bnn_loss_and_gradient_parity(cuda, D, H1, H2, M, S, engine):
                                               D, H1, H2, cfg.prior_scale)
     assert abs(st.loss - loss) <= 1e-5 * abs(loss)
     g = t["grad"].cpu().numpy()
-    close(g[:P], gmu, 2e-5)
-    close(g[P:], grho, 2e-5)
+    close(g[:P], gmu, 1e-5)
+    close(g[P:], grho, 1e-5)
 
 
 @ENGINES
@@ -140,8 +140,8 @@ def test_bnn_klqp_api_full_batch_matches_oracle(cuda):
     loss, gmu, grho = inf.loss_and_gradients(eps)
     l0, m0, r0 = bnn.klqp_loss_and_grads(mu, rho, eps, *args)
     assert abs(loss - l0) <= 1e-5 * abs(l0)
-    close(gmu.cpu().numpy(), m0, 2e-5)
-    close(grho.cpu().numpy(), r0, 2e-5)
+    close(gmu.cpu().numpy(), m0, 1e-5)
+    close(grho.cpu().numpy(), r0, 1e-5)
     opt = TFAdam(2 * P)
     th = np.concatenate([mu, rho]).astype(np.float64)
     for t in range(2):
@@ -231,8 +231,8 @@ def test_bnn_reparameterization_klqp_monte_carlo_kl(cuda):
     loss, gmu, grho = inf.loss_and_gradients(eps)
     l0, m0, r0 = bnn.klqp_loss_and_grads(mu, rho, eps, X, y, 0.2, 1.0, D, H1, H2, 1.5, method=1)
     assert abs(loss - l0) <= 1e-5 * abs(l0)
-    close(gmu.cpu().numpy(), m0, 2e-5)
-    close(grho.cpu().numpy(), r0, 2e-5)
+    close(gmu.cpu().numpy(), m0, 1e-5)
+    close(grho.cpu().numpy(), r0, 1e-5)
 
 
 @ENGINES
@@ -251,4 +251,4 @@ def test_bnn_log_lik_autograd_function(cuda, engine):
     (ll * w).sum().backward()
     ll0, g0 = bnn.log_lik_and_grad(theta, X, y, 0.4, 3.0, D, H1, H2)
     close(ll.detach().cpu().numpy(), ll0, 1e-5)
-    close(th.grad.cpu().numpy(), g0 * np.array([1.0, -0.5, 2.0])[:, None], 2e-5)
+    close(th.grad.cpu().numpy(), g0 * np.array([1.0, -0.5, 2.0])[:, None], 1e-5)

@@ -72,8 +72,8 @@ def test_hier_iteration_parity(cuda):
         assert np.all(np.abs(np.log(u[0, sl]) - res["ratio"])[differ] < 1e-3)
         same = ~differ
         exp = res["z"][same]
-        np.testing.assert_allclose(zk[sl][:, cols(D)][same], exp, rtol=1e-4,
-                                   atol=1e-4 * np.abs(exp).max())
+        np.testing.assert_allclose(zk[sl][:, cols(D)][same], exp, rtol=1e-5,
+                                   atol=1e-5 * np.abs(exp).max())
 
 
 def test_hier_in_kernel_rng_two_iterations(cuda):
