@@ -712,8 +712,18 @@ def run_klqp_target(X, y, dev, chunk=10):
         if len(recent) >= 5 and est >= plain_elbo - 0.1:
             reached = time.perf_counter() - t0
             break
+    # the fused run's whole 1,000 steps, for the same-work comparison
+    restart()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(KLQP_ITERS // 50):
+        inf.steps(50)
+    torch.cuda.synchronize()
+    full_wall = time.perf_counter() - t1
     return {"plain_method": "eager per-op GPU form (per-sample GEMV copies, autodiff, "
                             "unfused Adam), 1,000 steps",
+            "fused_wall_s_1000_steps": full_wall,
+            "wall_time_ratio_1000_steps": plain_wall / full_wall,
             "plain_wall_s": plain_wall, "plain_final_elbo_per_datum": plain_elbo,
             "fused_steps_to_within_0.1_nat": steps if reached is not None else None,
             "fused_wall_s": reached, "fused_elbo_per_datum_at_stop": est,
@@ -756,10 +766,10 @@ def run_hmc_posterior_and_target(args, dev, X, y, z0):
 
     * truth: the batched tensor-core run, 4,096 chains, 200 burn-in
       iterations, then 300 iterations of running moments (1.2 M draws);
-    * long single-chain run (SIMT engine, one chain, one launch):
+    * long single-chain run (one chain, one launch):
       1,000 burn-in + args.long_chain_iters iterations, its mean and variance
       against the truth, with its batch-means standard error;
-    * plain GPU method: one chain, one SIMT launch per iteration, the
+    * plain GPU method: one chain, one launch per iteration, the
       configuration's 2,000 iterations from an N(0, 1) start, mean over the
       second half; batched form: 4,096 chains, one tensor-core launch per
       iteration from N(0, 1) starts, mean over the second half of the
@@ -793,13 +803,14 @@ def run_hmc_posterior_and_target(args, dev, X, y, z0):
     v_true = (mom[1].sum(0) / n_t).cpu().numpy() - m_true ** 2
     sd_true = np.sqrt(v_true)
     acc_true = float(nacc.double().mean().item()) / 500
-    # long single chain
+    # long single chain (one launch; the tensor-core engine is the faster one
+    # for a single chain: 0.55 ms against 1.9 ms per iteration on the SIMT one)
     T_long = args.long_chain_iters
     z, gr, lj, st, nacc = fresh(1, z0[0])
-    _hmc_launch(g, None, "simt", z, gr, lj, 0, 1000, st, 12, nacc=nacc)
+    _hmc_launch(g, tiles, "tc", z, gr, lj, 0, 1000, st, 12, nacc=nacc)
     samp = torch.zeros(T_long + 1000, 1, P, device=dev)
     t0 = time.perf_counter()
-    _hmc_launch(g, None, "simt", z, gr, lj, 1, T_long, st, 12, samples=samp, nacc=nacc)
+    _hmc_launch(g, tiles, "tc", z, gr, lj, 1, T_long, st, 12, samples=samp, nacc=nacc)
     torch.cuda.synchronize()
     long_wall = time.perf_counter() - t0
     s1 = samp[1000:1000 + T_long, 0].double().cpu().numpy()
@@ -810,25 +821,31 @@ def run_hmc_posterior_and_target(args, dev, X, y, z0):
     posterior = {
         "truth": f"batched tensor-core run, {C} chains x 300 iterations after 200 of burn-in "
                  f"(acceptance {acc_true:.3f})",
-        "long_single_chain": f"SIMT engine, 1 chain, {T_long} iterations after 1,000 of burn-in, "
-                             f"{long_wall:.2f} s",
+        "long_single_chain": f"tensor-core engine, 1 chain, {T_long} iterations after 1,000 of "
+                             f"burn-in, {long_wall:.2f} s",
         "long_chain_mean_err_max_over_sd": float(np.max(np.abs(m1 - m_true) / sd_true)),
         "long_chain_mean_err_max_over_se": float(np.max(np.abs(m1 - m_true) / se1)),
         "long_chain_var_rel_err_max": float(np.max(np.abs(v1 - v_true) / v_true)),
         "posterior_sd_range": [float(sd_true.min()), float(sd_true.max())]}
-    # plain GPU method: one chain, one launch per iteration
+    # plain GPU method: one chain, one launch per iteration (the reference's
+    # one-chain update per sess.run), on each engine; the faster one is the
+    # comparison point
     T_plain = 2000
-    z, gr, lj, st, nacc = fresh(1, z0[0])
-    samp = torch.zeros(T_plain, 1, P, device=dev)
-    _hmc_launch(g, None, "simt", z.clone(), gr.clone(), lj.clone(), 0, 1, _lib.new_state(dev), 13)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(T_plain):
-        _hmc_launch(g, None, "simt", z, gr, lj, 1 if i else 0, 1, st, 13, samples=samp, nacc=nacc)
-    torch.cuda.synchronize()
-    plain_wall = time.perf_counter() - t0
-    sp_ = samp[T_plain // 2:, 0].double().cpu().numpy()
-    err_plain = float(np.max(np.abs(sp_.mean(0) - m_true) / sd_true))
+    plain = {}
+    for eng, tl in (("tc", tiles), ("simt", None)):
+        z, gr, lj, st, nacc = fresh(1, z0[0])
+        samp = torch.zeros(T_plain, 1, P, device=dev)
+        _hmc_launch(g, tl, eng, z.clone(), gr.clone(), lj.clone(), 0, 1, _lib.new_state(dev), 13)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(T_plain):
+            _hmc_launch(g, tl, eng, z, gr, lj, 1 if i else 0, 1, st, 13, samples=samp, nacc=nacc)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        sp_ = samp[T_plain // 2:, 0].double().cpu().numpy()
+        plain[eng] = (wall, float(np.max(np.abs(sp_.mean(0) - m_true) / sd_true)))
+    plain_eng = min(plain, key=lambda e: plain[e][0])
+    plain_wall, err_plain = plain[plain_eng]
     # batched form: 4,096 chains, one launch per iteration, checkpoints
     Kmax = 512
     z, gr, lj, st, nacc = fresh(C, z0)
@@ -853,9 +870,11 @@ def run_hmc_posterior_and_target(args, dev, X, y, z0):
         if reached is None and errs[k] <= err_plain:
             reached = k
     target = {
-        "plain_method": f"one chain, one SIMT launch per iteration, {T_plain} iterations, mean "
-                        f"over the second half",
+        "plain_method": f"one chain, one launch per iteration, {T_plain} iterations, mean over "
+                        f"the second half; engine: {plain_eng} (the faster for one chain)",
         "plain_wall_s": plain_wall, "plain_mean_err_max_over_sd": err_plain,
+        "plain_by_engine": {e: {"wall_s": w, "mean_err_max_over_sd": er}
+                            for e, (w, er) in plain.items()},
         "batched_method": f"{C} chains, one tensor-core launch per iteration, mean over the "
                           f"second half of the iterations so far",
         "batched_mean_err_max_over_sd_at": {str(k): v for k, v in errs.items()},
@@ -1151,29 +1170,90 @@ def run_sbn(args):
         4.0 * B * (V + 1) * (H0 + BH)
     peak, src = _peak_3xtf32()
     ach = flops / (ms / 1e3) / 1e12
-    # gradient variance at the trained parameters, one frozen minibatch
-    inf._sbn.gather = False
     nq = (V + 1) * H0 + (H0 + 1) * H1
-    gvar = {}
-    for mode, rb, name in ((0, 0, "none"), (0, 1, "rao_blackwell"), (1, 0, "mean"),
-                           (2, 0, "mlp")):
-        inf._cfg.baseline, inf._cfg.rao_blackwell = mode, rb
-        gs = []
-        for k in range(24):
-            inf.seed = 7000 + k
-            gs.append(inf.score_gradients()[1][:nq].double())
-        gvar[name] = float(torch.stack(gs).var(dim=0).sum())
-    inf._cfg.baseline, inf._cfg.rao_blackwell = 2, 0
-    # ELBO after equal training with the running-mean and the MLP baseline
-    elbo = {}
-    for name in ("mean", "mlp"):
-        run = _sbn_inference(data, B, S, name, seed=1)
+
+    def q_grad_variance(run, modes, draws=24):
+        """Summed variance of the q-gradient over `draws` Philox draws at the
+        run's current parameters and one frozen minibatch, per estimator."""
+        run._sbn.gather = False
+        out = {}
+        for mode, rb, name in modes:
+            run._cfg.baseline, run._cfg.rao_blackwell = mode, rb
+            gs = []
+            for k in range(draws):
+                run.seed = 7000 + k
+                gs.append(run.score_gradients()[1][:nq].double())
+            out[name] = float(torch.stack(gs).var(dim=0).sum())
+        run._cfg.baseline, run._cfg.rao_blackwell = 2, 0
+        run._sbn.gather = True
+        return out
+
+    def train(run, n):
+        """n steps; returns the ELBO per row (mean of the last 10 chunk-end losses)."""
         losses = []
-        for i in range(args.sbn_compare_steps // chunk):
+        for i in range(n // chunk):
             run.steps(chunk)
-            if i >= args.sbn_compare_steps // chunk - 10:
+            if i >= n // chunk - 10:
                 losses.append(run._read_state().loss)
-        elbo[name] = -float(np.mean(losses)) / B
+        return -float(np.mean(losses)) / B
+
+    def ci95(xs):
+        xs = np.asarray(xs, np.float64)
+        t = {2: 12.71, 3: 4.30, 4: 3.18, 5: 2.78, 6: 2.57, 7: 2.45, 8: 2.36}.get(len(xs), 2.0)
+        return [float(xs.mean() - t * xs.std(ddof=1) / np.sqrt(len(xs))),
+                float(xs.mean() + t * xs.std(ddof=1) / np.sqrt(len(xs)))]
+    # all four estimators at the trained parameters of the timed run
+    gvar = q_grad_variance(inf, ((0, 0, "none"), (0, 1, "rao_blackwell"), (1, 0, "mean"),
+                                 (2, 0, "mlp")))
+    # learned baseline against the running mean over independent seeds: each seed
+    # trains an MLP-baseline run and a running-mean run for the same steps, then
+    # measures both estimators' q-gradient variance at the MLP run's parameters
+    n_cmp = args.sbn_compare_steps
+    seeds = []
+    for sd in range(args.sbn_seeds):
+        run_mlp = _sbn_inference(data, B, S, "mlp", seed=100 + sd)
+        e_mlp = train(run_mlp, n_cmp)
+        v = q_grad_variance(run_mlp, ((1, 0, "mean"), (2, 0, "mlp")))
+        run_mean = _sbn_inference(data, B, S, "mean", seed=100 + sd)
+        e_mean = train(run_mean, n_cmp)
+        seeds.append({"seed": 100 + sd, "q_grad_var_mean": v["mean"], "q_grad_var_mlp": v["mlp"],
+                      "variance_ratio_mlp_over_mean": v["mlp"] / v["mean"],
+                      "elbo_per_row_mean": e_mean, "elbo_per_row_mlp": e_mlp})
+        del run_mlp, run_mean
+    ratios = [r["variance_ratio_mlp_over_mean"] for r in seeds]
+    gains = [r["elbo_per_row_mlp"] - r["elbo_per_row_mean"] for r in seeds]
+    baseline_gain = {
+        "seeds": seeds, "steps_per_run": n_cmp,
+        "variance_ratio_mlp_over_mean_mean": float(np.mean(ratios)),
+        "variance_ratio_mlp_over_mean_ci95": ci95(ratios) if len(ratios) > 1 else None,
+        "elbo_gain_per_row_mean": float(np.mean(gains)),
+        "elbo_gain_per_row_ci95": ci95(gains) if len(gains) > 1 else None}
+    # north-star target for the learned part: wall time for the learned-baseline
+    # run to come within 0.1 nat/row of the ELBO that the plain estimator (the
+    # reference's ScoreKLqp, no baseline) reaches in n_cmp steps
+    plain = _sbn_inference(data, B, S, "none", seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_plain = train(plain, n_cmp)
+    plain_wall = time.perf_counter() - t0
+    del plain
+    learned = _sbn_inference(data, B, S, "mlp", seed=1)
+    learned.steps(chunk)
+    torch.cuda.synchronize()
+    recent, steps, reached = [], chunk, None
+    t0 = time.perf_counter()
+    while steps < n_cmp:
+        learned.steps(chunk)
+        steps += chunk
+        recent.append(learned._read_state().loss)
+        if len(recent) >= 10 and -float(np.mean(recent[-10:])) / B >= e_plain - 0.1:
+            reached = time.perf_counter() - t0
+            break
+    target = {"plain_method": f"ScoreKLqp without a baseline (the reference estimator), "
+                              f"{n_cmp} steps", "plain_wall_s": plain_wall,
+              "plain_elbo_per_row": e_plain, "learned_steps_to_within_0.1_nat": steps
+              if reached is not None else None, "learned_wall_s": reached,
+              "wall_time_ratio": plain_wall / reached if reached else None}
     st = inf._read_state()
     from edward_gb300 import _lib
     launches = _lib.load().edg_sbn_launches_per_step(inf._cfg, B, 1)
@@ -1192,8 +1272,8 @@ def run_sbn(args):
                          "frac": ach / peak, "traffic": None,
                          "kernel": "whole step (SIMT bgemm + row kernels + baseline)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
-            "q_grad_variance": gvar,
-            "elbo_per_row_after_%d_steps" % args.sbn_compare_steps: elbo,
+            "q_grad_variance": gvar, "learned_baseline_gain": baseline_gain,
+            "target": target,
             "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0
@@ -1258,9 +1338,10 @@ def main():
                     help="headline HMC measurement only (no KLqp record, posterior error, "
                          "wall-time target or TF32 peak)")
     ap.add_argument("--klqp-steps", type=int, default=200)
-    ap.add_argument("--long-chain-iters", type=int, default=20000)
+    ap.add_argument("--long-chain-iters", type=int, default=10000)
     ap.add_argument("--hier-instances", type=int, default=2048)
     ap.add_argument("--sbn-compare-steps", type=int, default=1000)
+    ap.add_argument("--sbn-seeds", type=int, default=5)
     ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn", "sgld"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
