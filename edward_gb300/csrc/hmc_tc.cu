@@ -399,7 +399,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       const uint64_t dx_hi[2] = {sdesc(st0, 128, sbo_k), sdesc(st1, 128, sbo_k)};
       const uint64_t dx_lo[2] = {sdesc(st0 + 256u * PP, 128, sbo_k),
                                  sdesc(st1 + 256u * PP, 128, sbo_k)};
-      const int KF = PP / 8;  // forward K steps (2, 4 or 8)
+      // forward K steps: only the 8-wide K blocks that hold a coordinate of z
+      // (columns P .. PP-1 of Z and of the X tile are zero), 7 instead of 8
+      // for P = 51
+      const int KF = (P + 7) / 8;
       for (int i = 0; i < nt; ++i) {
         const uint32_t g = gt + i, s = g & 1u, b = g & 1u;
         mbar_wait(b_fullx + 8 * s, (g >> 1) & 1u, err);
