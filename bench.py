@@ -938,7 +938,9 @@ def hier_data(I=2048, seed=0):
 
 def run_hier(args):
     """All 2,048 instances x 64 chains, 10 leapfrog steps per iteration, one
-    launch per iteration (edg_hmc_hier_run)."""
+    launch per iteration (edg_hmc_hier_run), timed for both launch forms (the
+    persistent work-queue grid and one CTA per (instance, chain tile)); the
+    faster form is then replayed from a CUDA graph, which is the value."""
     import ctypes
     import numpy as np
     import torch
@@ -956,26 +958,43 @@ def run_hier(args):
     st = _lib.new_state(dev)
     cfg = _lib.EdgHMC()
     cfg.step_size, cfg.n_steps, cfg.seed = 0.01, L, 1
-    sp = _lib.stream_ptr()
     state = {"cache": 0}
 
     def step():
         _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
                   _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), state["cache"], _lib.ptr(nacc),
-                  _lib.ptr(st), None, 0, None, None, None, None, sp)
+                  _lib.ptr(st), None, 0, None, None, None, None, _lib.stream_ptr())
         state["cache"] = 1
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    def timed(fn, k):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        for _ in range(args.steps):
-            step()
+        for _ in range(k):
+            fn()
         b.record()
         b.synchronize()
-    ms = a.elapsed_time(b) / args.steps
+        return a.elapsed_time(b) / k
+
+    forms = {}
+    for launch, name in ((0, "persistent"), (1, "one_cta_per_item")):
+        cfg.launch = launch
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        forms[name] = timed(step, args.steps)
+    best = min(forms, key=forms.get)
+    cfg.launch = 0 if best == "persistent" else 1
+    graph = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            step()
+    torch.cuda.current_stream().wait_stream(s)
+    graph.replay()
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        ms = timed(graph.replay, args.steps)
     work = float((hd.Ns.astype(np.int64) * hd.Ds).sum())
     flops = 4.0 * work * C * L
     peak, src = _peak_3xtf32()
@@ -986,14 +1005,15 @@ def run_hier(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"hier_ragged_I{hd.I}_C64_L10", "instances": hd.I, "chains": C,
                        "leapfrog_steps": L, "sum_N_D": int(work),
-                       "x_bytes": int(work * 4),
+                       "x_bytes": int(work * 4), "launch": f"{best}, replayed from a CUDA graph",
                        "l2_flush": "inputs larger than L2 (X is %.2f GB)" % (work * 4 / 1e9)},
+            "launch_forms_ms_per_step": forms,
             "gpu_launches": args.steps,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                          "frac": ach / peak, "traffic": None, "kernel": "hmc_hier_kernel<32> (SIMT FP32)",
                          "peak_source": src, "algorithmic_flops_per_launch": flops,
                          "x_stream_GBs": 2 * L * work * 4 / (ms / 1e3) / 1e9},
-            "accept_rate": float(nacc.sum().item()) / (n * (args.warmup + args.steps)),
+            "accept_rate": float(nacc.sum().item()) / (n * (2 * args.warmup + 3 * args.steps + 1)),
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0

@@ -93,7 +93,7 @@ class EdgExpFam(ctypes.Structure):
 
 class EdgHMC(ctypes.Structure):
     _fields_ = [("step_size", c_float), ("n_steps", c_int32), ("seed", c_uint64),
-                ("chains_per_block", c_int32), ("cluster_size", c_int32)]
+                ("chains_per_block", c_int32), ("cluster_size", c_int32), ("launch", c_int32)]
 
 
 # name -> (restype, argtypes)

@@ -43,6 +43,7 @@ struct HierArgs {
   const float* r_ovr;
   const double* u_ovr;
   double* ratio_out;
+  int persistent;  // 1: each CTA pulls (instance, chain tile) items from a work counter
 };
 
 template <int CT>
@@ -91,11 +92,12 @@ __device__ __forceinline__ void hier_prior_warp(const float* Zc, float* Gc, int 
   }
 }
 
+// All n_iter iterations of one work item: the chains [ctile*CT, ctile*CT + CT)
+// of instance order[item / tiles_per_inst].
 template <int CT>
-__global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int inst = a.order ? a.order[blockIdx.x / a.tiles_per_inst] : blockIdx.x / a.tiles_per_inst;
-  const int ctile = blockIdx.x % a.tiles_per_inst;
+__device__ void hier_item(const HierArgs& a, int item, unsigned char* smem) {
+  const int inst = a.order ? a.order[item / a.tiles_per_inst] : item / a.tiles_per_inst;
+  const int ctile = item % a.tiles_per_inst;
   GLMDev m;
   m.X = a.X + a.x_off[inst];
   m.y = a.y + a.y_off[inst];
@@ -124,7 +126,6 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
   double* lpn = ljn + CT;
   int* acc = reinterpret_cast<int*>(lpn + CT);
   float* G = S.G;
-  __shared__ bool s_last;
   float *mu0 = H, *u0 = H + CT, *gmu0 = H + 2 * CT, *gu0 = H + 3 * CT;
   float *hmu = H + 4 * CT, *hu = H + 5 * CT, *rmu = H + 6 * CT, *ru = H + 7 * CT;
   float *gmu = H + 8 * CT, *gu = H + 9 * CT;
@@ -308,14 +309,43 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
     a.grad[g] = d < D ? G0[c * PP + d] : (d == D ? gmu0[c] : gu0[c]);
   }
   if (threadIdx.x < nc) a.lj[gchain(threadIdx.x)] = lj0[threadIdx.x];
+  __syncthreads();  // the next item reuses the shared memory
+}
+
+// One launch runs every item for n_iter iterations.  Persistent form: a grid
+// of resident CTAs, each taking items from the state's work counter in the
+// launch order (heaviest instances first, so the ragged tail is short).
+// Otherwise one CTA per item.  The last CTA to finish advances t and clears
+// the counters.
+template <int CT>
+__global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item;
+  __shared__ bool s_last;
+  __shared__ int64_t s_t0;
+  if (threadIdx.x == 0) s_t0 = *(volatile int64_t*)&a.state->t;
+  if (a.persistent) {
+    const int total = a.I * a.tiles_per_inst;
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.state->reserved, 1u);
+      __syncthreads();
+      const int item = s_item;
+      if (item >= total) break;
+      hier_item<CT>(a, item, smem);
+    }
+  } else {
+    hier_item<CT>(a, blockIdx.x, smem);
+  }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned prev = atomicAdd(&a.state->done, 1u);
     s_last = (prev == gridDim.x - 1);
     if (s_last) {
-      a.state->t = t0 + a.n_iter;
+      a.state->t = s_t0 + a.n_iter;
       a.state->done = 0;
+      a.state->reserved = 0;
       __threadfence();
     }
   }
@@ -386,8 +416,18 @@ extern "C" int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, i
               model->max_D, sm);
   const int rc_attr = set_max_dyn_smem(hmc_hier_kernel<CT>, sm, "hmc_hier_kernel");
   if (rc_attr) return rc_attr;
-  const int64_t nblocks = (int64_t)a.I * a.tiles_per_inst;
-  EDG_REQUIRE(nblocks < (1ll << 31), EDG_E_SHAPE, "too many instances x chain tiles");
+  const int64_t nitems = (int64_t)a.I * a.tiles_per_inst;
+  EDG_REQUIRE(nitems < (1ll << 31), EDG_E_SHAPE, "too many instances x chain tiles");
+  EDG_REQUIRE(cfg->launch == 0 || cfg->launch == 1, EDG_E_VALUE, "launch must be 0 or 1 (got %d)",
+              cfg->launch);
+  a.persistent = cfg->launch == 0 ? 1 : 0;
+  int64_t nblocks = nitems;
+  if (a.persistent) {
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hmc_hier_kernel<CT>, kThreads, sm);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    nblocks = std::min<int64_t>(nitems, (int64_t)std::max(per_sm, 1) * std::max(sms, 1));
+  }
   hmc_hier_kernel<CT><<<(unsigned)nblocks, kThreads, sm, (cudaStream_t)stream>>>(a);
   return check_launch("hmc_hier_kernel");
 }

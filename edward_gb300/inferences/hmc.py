@@ -186,8 +186,33 @@ class HMC(MonteCarlo):
         cfg.seed = next_seed()
         self._cfg = cfg
         self.engine = "hier"
+        self._graphs = {}
+        cfg.launch = self._autotune_hier()
         self.train = self.update
         return self.train
+
+    def _autotune_hier(self):
+        """Launch form of the ragged batch (persistent work-queue grid or one
+        CTA per (instance, chain tile)), timed on scratch copies of the state
+        and cached per model shape."""
+        hd, C = self._hier, self.C
+        z = self._z.clone()
+        g = torch.zeros_like(self._g)
+        lj = torch.zeros_like(self._lj)
+
+        def run(launch):
+            cfg = _lib.EdgHMC()
+            cfg.step_size, cfg.n_steps, cfg.seed, cfg.launch = (self._cfg.step_size,
+                                                                 self._cfg.n_steps, 1, launch)
+            z.copy_(self._z)
+            st = _lib.new_state(self._device)
+            _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
+                      _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st), None, 0,
+                      None, None, None, None, _lib.stream_ptr())
+
+        work = int((hd.Ns.astype(np.int64) * hd.Ds).sum())
+        key = f"I{hd.I}_work{work}_maxD{hd.max_D}_C{C}_L{self.n_steps}"
+        return autotune.choose("hmc_hier", key, [0, 1], run)
 
     def _build_expfam(self):
         """Chains of the unconstrained latent u (FP64); the Empirical shows the
@@ -245,13 +270,33 @@ class HMC(MonteCarlo):
             self._cache_valid = 1
             return
         if self.engine == "hier":
-            _lib.call("edg_hmc_hier_run", self._hier.ref(), ctypes.byref(self._cfg), self.C,
-                      int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),
-                      _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
-                      _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
-                      self._samples.shape[0], None, _lib.ptr(r_override), _lib.ptr(u_override),
-                      _lib.ptr(ratio_out), _lib.stream_ptr())
-            self._cache_valid = 1
+            def launch():
+                _lib.call("edg_hmc_hier_run", self._hier.ref(), ctypes.byref(self._cfg), self.C,
+                          int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),
+                          _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
+                          _lib.ptr(self._n_accept), _lib.ptr(self._state),
+                          _lib.ptr(self._samples), self._samples.shape[0], None,
+                          _lib.ptr(r_override), _lib.ptr(u_override), _lib.ptr(ratio_out),
+                          _lib.stream_ptr())
+            plain = r_override is not None or u_override is not None or ratio_out is not None
+            if plain or not self._cache_valid:
+                launch()
+                self._cache_valid = 1
+                return
+            # the k-iteration launch with a valid cache is replayed from a CUDA
+            # graph (its arguments are fixed; t and the work counter live on
+            # the device)
+            gph = self._graphs.get(int(n_iter))
+            if gph is None:
+                gph = torch.cuda.CUDAGraph()
+                s = torch.cuda.Stream()
+                s.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(s):
+                    with torch.cuda.graph(gph, stream=s):
+                        launch()
+                torch.cuda.current_stream().wait_stream(s)
+                self._graphs[int(n_iter)] = gph
+            gph.replay()
             return
         if self.engine == "tc":
             _lib.call("edg_hmc_glm_tc_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,

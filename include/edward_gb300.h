@@ -91,7 +91,7 @@ typedef struct {
   uint32_t done;         /* internal completion counter; 0 between calls */
   uint32_t nonfinite;    /* non-finite loss/gradient values seen */
   uint32_t error;        /* EDG_E_* of a kernel that gave up a bounded wait (0 = none) */
-  uint32_t reserved;
+  uint32_t reserved;      /* work counter of persistent launches; 0 between calls */
   double loss;           /* loss of the last KLqp update */
   double aux[3];         /* estimator-specific diagnostics */
 } edg_state_t;
@@ -128,6 +128,9 @@ typedef struct {
   uint64_t seed;
   int32_t chains_per_block; /* SIMT engine: 0 = library default; else 8, 16 or 32 */
   int32_t cluster_size;     /* tensor-core engine: CTAs per 128 chains (1,2,4,8); 0 = auto */
+  int32_t launch;           /* hierarchical engine: 0 = persistent grid of resident CTAs taking
+                               (instance, chain tile) items from a work counter, 1 = one CTA
+                               per item */
 } edg_hmc_t;
 
 /* ---------------------------------------------------------------- library */

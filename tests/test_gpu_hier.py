@@ -18,11 +18,11 @@ def _instances(seed=3):
     return Xs + X2, ys + y2
 
 
-def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None):
+def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launch=0):
     from edward_gb300 import _lib
     cuda = z0.device
     cfg = _lib.EdgHMC()
-    cfg.step_size, cfg.n_steps, cfg.seed = step, L, seed
+    cfg.step_size, cfg.n_steps, cfg.seed, cfg.launch = step, L, seed, launch
     n = hd.I * C
     z = z0.clone()
     g = torch.zeros_like(z)
@@ -104,7 +104,7 @@ def test_hier_in_kernel_rng_two_iterations(cuda):
             res = hmc_step(f, zi, gr, lj, r0, uu, step, L)
             scale = max(np.abs(lj).max(), 1.0)
             np.testing.assert_allclose(rk[t, i * C:(i + 1) * C], res["ratio"], rtol=0,
-                                       atol=2e-5 * scale)
+                                       atol=1e-5 * scale)
             zi = sk[t, i * C:(i + 1) * C][:, cols(D)].astype(np.float64)  # resync on kept states
             lj, gr = f(zi)
 
@@ -139,3 +139,63 @@ def test_hier_public_api_ragged_batch(cuda):
     for i, (Xi, yi) in enumerate(zip(Xs, ys)):
         D = Xi.shape[1]
         assert np.all(np.isfinite(wm[i, :D])) and np.all(wm[i, D:] == 0)
+
+
+def test_hier_launch_forms_agree(cuda):
+    """The persistent work-queue grid and the one-CTA-per-item grid run the
+    same arithmetic per (instance, chain tile): identical chains, ratios and
+    acceptance counts; t advances and the work counter is left at 0."""
+    from edward_gb300.ops import HierDevice
+    Xs, ys = _instances(seed=11)
+    hd = HierDevice(Xs, ys)
+    C, T = 48, 3
+    z0 = torch.as_tensor(np.random.default_rng(2).standard_normal((hd.I * C, hd.SP))
+                         .astype(np.float32) * 0.1, device=cuda)
+    outs = []
+    for launch in (0, 1):
+        samples = torch.zeros(T, hd.I * C, hd.SP, device=cuda)
+        z, g, lj, nacc, ratio, st = _run(hd, C, z0, T, 0.01, 4, seed=5, samples=samples,
+                                         launch=launch)
+        assert st.t == T and st.done == 0 and st.reserved == 0
+        outs.append((samples.cpu().numpy(), lj.cpu().numpy(), nacc.cpu().numpy(),
+                     ratio.cpu().numpy()))
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_hier_graph_replay_matches_direct_launch(cuda):
+    """ed.HMC on the ragged batch replays k-iteration launches from a CUDA
+    graph once the gradient cache is valid: five one-iteration calls (the
+    first launched directly, the rest replayed) give the same samples as one
+    five-iteration launch."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Empirical, HalfNormal, Normal
+    Xs, ys = hier.synthetic_instances(4, seed=31, n_range=(100, 900), d_range=(5, 20))
+    Dmax = max(x.shape[1] for x in Xs)
+    runs = []
+    for mode in ("graph", "direct"):
+        ed.set_seed(9)
+        X = ed.placeholder(np.float32, [None, None])
+        mu = Normal(loc=0.0, scale=1.0)
+        tau = HalfNormal(scale=1.0)
+        tau.support = "nonnegative"
+        w = Normal(loc=mu * ed.ones(Dmax), scale=tau * ed.ones(Dmax))
+        y = Bernoulli(logits=ed.dot(X, w))
+        T, C = 5, 8
+        qw = Empirical(ed.Variable(np.zeros((T, 4, C, Dmax), np.float32)), n_chains=None)
+        qmu = Empirical(ed.Variable(np.zeros((T, 4, C), np.float32)))
+        qtau = Empirical(ed.Variable(np.zeros((T, 4, C), np.float32)))
+        inf = ed.HMC({w: qw, mu: qmu, tau: qtau}, data={X: Xs, y: ys}, n_chains=C)
+        inf.initialize(step_size=0.02, n_steps=4, n_print=0)
+        if mode == "graph":
+            for _ in range(T):
+                inf.run_iterations(1)
+            assert 1 in inf._graphs
+        else:
+            inf.run_iterations(T)
+        torch.cuda.synchronize()
+        assert inf.t == T
+        runs.append((qw.params.cpu().numpy(), qmu.params.cpu().numpy(),
+                     inf.n_accept.cpu().numpy()))
+    for a, b in zip(runs[0], runs[1]):
+        np.testing.assert_array_equal(a, b)
