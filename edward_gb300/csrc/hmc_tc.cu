@@ -515,8 +515,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       };
       for (int i = 0; i < nt; ++i) {
         const uint32_t g = gt + i, b = g & 1u;
-        // y of this thread's 16 rows straight from the model (L2-resident),
-        // loaded before the eta wait so that its latency hides behind it
+        // y of this thread's 16 rows straight from the model (L2-resident;
+        // the next tile's rows are prefetched into L1 below, since eta is
+        // usually ready when a tile starts and would not hide an L2 latency)
         const int row0 = (t_begin + i) * kNR + 16 * qs;
         const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
         float ye[16];
@@ -534,6 +535,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
           for (int k = 0; k < 16; ++k) ye[k] = k < nvalid ? __ldg(a.y + row0 + k) : 0.0f;
         }
+        if (lane == 0 && i + 1 < nt) prefetch_l1(a.y + min(row0 + kNR, a.N - 1));
         mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
         tc_fence_after();
         // eta of 16 rows in one TMEM load; then two halves of 8 rows:
