@@ -151,6 +151,60 @@ def cpu_klqp_baseline(n_steps=KLQP_ITERS):
     return cb, elbo
 
 
+def _cpu_net_worker(kind, n_steps):
+    """Times n_steps of the reference-structured CPU step of a network
+    workload (after one untimed step); returns (seconds, steps)."""
+    import numpy as np
+    from oracle import cpu_baseline as cb
+    if kind == "bnn":
+        N, D, H1, H2, M, S = 100000, 32, 256, 256, 4096, 64
+        X, y = bnn_data(N, D, H1, H2)
+        X, y = X[:M], y[:M]
+        P = D * H1 + H1 + H1 * H2 + H2 + H2 + 1
+        rng = np.random.default_rng(1)
+        mu = (rng.standard_normal(P) * 0.1).astype(np.float32)
+        rho = np.full(P, -3.0, np.float32)
+        m, v = np.zeros(2 * P, np.float32), np.zeros(2 * P, np.float32)
+        step = lambda t: cb.bnn_klqp_step(X, y, mu, rho, m, v, t, S, 1, 0.1, N / M,  # noqa: E731
+                                          D, H1, H2, 1e-3)
+    else:
+        V, H0, H1, B, S = 784, 200, 200, 1024, 16
+        X = sbn_data(V=V, H0=H0, H1=H1)[:B].astype(np.float32)
+        P = (V + 1) * H0 + (H0 + 1) * H1 + (H1 + 1) * H0 + (H0 + 1) * V
+        theta = (np.random.default_rng(1).standard_normal(P) * 0.05).astype(np.float32)
+        m, v = np.zeros(P, np.float32), np.zeros(P, np.float32)
+        step = lambda t: cb.sbn_score_step(X, theta, m, v, t, S, 1, V, H0, H1, 1e-3)  # noqa: E731
+    step(0)
+    t0 = time.perf_counter()
+    for t in range(1, n_steps + 1):
+        step(t)
+    return time.perf_counter() - t0, n_steps
+
+
+def cpu_net_baseline(kind, n_steps, what):
+    """cpu_baseline record for a network workload: the reference-structured
+    CPU step (one model copy per Monte Carlo sample, NumPy FP32) in one spawned
+    process whose BLAS uses every host core."""
+    import multiprocessing as mp
+    ncores = len(os.sched_getaffinity(0))
+    keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ[k] = str(ncores)
+    try:
+        with mp.get_context("spawn").Pool(1) as pool:
+            dt, n = pool.apply(_cpu_net_worker, (kind, n_steps))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return {"value": n / dt, "unit": "evals/s", "cores": ncores, "kind": "port",
+            "sample": f"{n} steps of {what} after one untimed step, one process, BLAS on "
+                      f"{ncores} threads, {dt:.1f} s wall"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -1077,6 +1131,9 @@ def run_bnn(args):
     import edward_gb300 as ed
     from edward_gb300.models import Normal
     N, D, H1, H2, M, S = 100000, 32, 256, 256, 4096, 64
+    cb = None if args.no_cpu_baseline else cpu_net_baseline(
+        "bnn", 3, "the Bayesian NN KLqp step (S=64 network copies over M=4096 rows, analytic "
+        "KL, Adam)")
     X, y = bnn_data(N, D, H1, H2)
     W0 = Normal(loc=ed.zeros([D, H1]), scale=ed.ones([D, H1]))
     W1 = Normal(loc=ed.zeros([H1, H2]), scale=ed.ones([H1, H2]))
@@ -1126,7 +1183,8 @@ def run_bnn(args):
                          "frac": ach / peak, "traffic": None,
                          "kernel": "whole step (tcgen05 3xTF32 GEMMs + fused head/adjoint + finalize)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
-            "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
+            "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary(),
+            "cpu_baseline": cb}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -1170,6 +1228,8 @@ def run_sbn(args):
     import numpy as np
     import torch
     V, H0, H1, B, S, BH = 784, 200, 200, 1024, 16, 100
+    cb = None if args.no_cpu_baseline else cpu_net_baseline(
+        "sbn", 5, "the plain ScoreKLqp step (S=16 copies of q and p over B=1024 rows, Adam)")
     data = sbn_data(V=V, H0=H0, H1=H1)
     inf = _sbn_inference(data, B, S, "mlp")
     chunk = 10
@@ -1293,7 +1353,7 @@ def run_sbn(args):
                          "kernel": "whole step (SIMT bgemm + row kernels + baseline)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
             "q_grad_variance": gvar, "learned_baseline_gain": baseline_gain,
-            "target": target,
+            "target": target, "cpu_baseline": cb,
             "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0

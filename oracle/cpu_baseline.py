@@ -122,3 +122,102 @@ def klqp_logreg_step(X, y, mu, rho, m, v, t, n_samples, seed, prior_loc, prior_s
     mu[:] = theta[:P]
     rho[:] = theta[P:]
     return float(loss)
+
+
+def _adam(theta, g, m, v, t, lr):
+    b1, b2 = 0.9, 0.999
+    lr_t = lr * np.sqrt(1 - b2 ** (t + 1)) / (1 - b1 ** (t + 1))
+    m[:] = b1 * m + (1 - b1) * g
+    v[:] = b2 * v + (1 - b2) * g * g
+    return theta - lr_t * m / (np.sqrt(v) + 1e-8)
+
+
+def bnn_klqp_step(X, y, mu, rho, m, v, t, n_samples, seed, noise, scale, D, H1, H2, lr):
+    """One reference-structured Bayesian-NN KLqp step (analytic KL,
+    ``klqp.py:707-769`` on ``examples/bayesian_nn.py:120-162``): one copy of
+    the network per Monte Carlo sample (three matmuls forward and their
+    transposes for ``tf.gradients``), the analytic KL and an unfused Adam;
+    NumPy FP32.  Updates mu, rho, m, v in place and returns the loss."""
+    X = np.asarray(X, np.float32)
+    y = np.asarray(y, np.float32)
+    P = mu.shape[0]
+    sig = _softplus(rho).astype(np.float32)
+    eps = normals(seed, KIND_EPS, t, n_samples, P).astype(np.float32)
+    gmu = np.zeros(P, np.float32)
+    gsig = np.zeros(P, np.float32)
+    ll_sum = 0.0
+    n0, n1, n2 = D * H1, H1 * H2, H2
+    for s in range(n_samples):                     # one model copy per sample
+        th = mu + sig * eps[s]
+        W0 = th[:n0].reshape(D, H1)
+        b0 = th[n0:n0 + H1]
+        o = n0 + H1
+        W1 = th[o:o + n1].reshape(H1, H2)
+        b1 = th[o + n1:o + n1 + H2]
+        o += n1 + H2
+        W2 = th[o:o + n2].reshape(H2, 1)
+        b2 = th[o + n2]
+        h1 = np.tanh(X @ W0 + b0)
+        h2 = np.tanh(h1 @ W1 + b1)
+        res = y - (h2 @ W2)[:, 0] - b2
+        ll_sum += float(scale * ((-0.5 * (res / noise) ** 2).sum(dtype=np.float32)
+                                 - res.shape[0] * (np.log(noise) + 0.9189385332)))
+        dout = (scale * res / noise ** 2).astype(np.float32)
+        dh2 = np.outer(dout, W2[:, 0]) * (1.0 - h2 * h2)
+        dh1 = (dh2 @ W1.T) * (1.0 - h1 * h1)
+        g = np.concatenate([(X.T @ dh1).reshape(-1), dh1.sum(0), (h1.T @ dh2).reshape(-1),
+                            dh2.sum(0), h2.T @ dout, [dout.sum()]]).astype(np.float32)
+        gmu -= g / n_samples
+        gsig -= g * eps[s] / n_samples
+    kl = (0.5 * mu * mu + 0.5 * (sig * sig - 1.0) - np.log(sig)).sum()
+    gmu += mu
+    gsig += sig - 1.0 / sig
+    grho = gsig * _sigmoid(rho)
+    theta = _adam(np.concatenate([mu, rho]), np.concatenate([gmu, grho]), m, v, t, lr)
+    mu[:] = theta[:P]
+    rho[:] = theta[P:]
+    return -(ll_sum / n_samples - kl)
+
+
+def sbn_score_step(X, theta, m, v, t, n_samples, seed, V, H0, H1, lr):
+    """One reference-structured ScoreKLqp step on the sigmoid belief network
+    (``build_score_loss_and_gradients``, ``klqp.py:840-906``, model of
+    ``examples/sigmoid_belief_network.py:54-86``): per Monte Carlo sample a
+    copy of q (784 -> 200 -> 200, Bernoulli draws) and of p (200 -> 200 -> 784),
+    the per-sample learning signal log p - log q, and the score and
+    reparameterisation-free gradients through transposed matmuls; unfused
+    Adam; NumPy FP32.  Updates theta, m, v in place and returns the loss."""
+    X = np.asarray(X, np.float32)
+    B = X.shape[0]
+    rng = np.random.default_rng(seed * 1000003 + t)
+    shapes = [(V + 1, H0), (H0 + 1, H1), (H1 + 1, H0), (H0 + 1, V)]
+    Ws, o = [], 0
+    for r, c in shapes:
+        Ws.append(theta[o:o + r * c].reshape(r, c))
+        o += r * c
+    Wq0, Wq1, Wp1, Wp0 = Ws
+    aug = lambda a: np.concatenate([a, np.ones((a.shape[0], 1), np.float32)], 1)  # noqa: E731
+    blogp = lambda z, lg: (z * lg - _softplus(lg)).sum(-1)                           # noqa: E731
+    Xa = aug(X)
+    g = [np.zeros_like(W) for W in Ws]
+    F_sum = 0.0
+    for _ in range(n_samples):                     # one copy of q and p per sample
+        Lq0 = Xa @ Wq0
+        z0 = (rng.random(Lq0.shape, dtype=np.float32) < _sigmoid(Lq0)).astype(np.float32)
+        Z0a = aug(z0)
+        Lq1 = Z0a @ Wq1
+        z1 = (rng.random(Lq1.shape, dtype=np.float32) < _sigmoid(Lq1)).astype(np.float32)
+        Z1a = aug(z1)
+        Lp1 = Z1a @ Wp1
+        Lp0 = Z0a @ Wp0
+        f = (blogp(z1, np.zeros_like(z1)) + blogp(z0, Lp1) + blogp(X, Lp0)
+             - blogp(z0, Lq0) - blogp(z1, Lq1))
+        F = float(f.sum())
+        F_sum += F
+        g[0] -= Xa.T @ (F * (z0 - _sigmoid(Lq0))) / n_samples
+        g[1] -= Z0a.T @ (F * (z1 - _sigmoid(Lq1))) / n_samples
+        g[2] -= Z1a.T @ (z0 - _sigmoid(Lp1)) / n_samples
+        g[3] -= Z0a.T @ (X - _sigmoid(Lp0)) / n_samples
+    grad = np.concatenate([a.reshape(-1) for a in g]).astype(np.float32)
+    theta[:] = _adam(theta, grad, m, v, t, lr)
+    return -F_sum / n_samples / B

@@ -321,3 +321,27 @@ def test_cpu_baseline_klqp_matches_oracle():
         assert abs(loss - e_losses[t]) <= 1e-4 * abs(e_losses[t])
     np.testing.assert_allclose(mu, e_mu, rtol=1e-3, atol=1e-4)
     np.testing.assert_allclose(rho, e_rho, rtol=1e-3, atol=1e-4)
+
+
+def test_cpu_baseline_bnn_step_matches_oracle():
+    """The timed CPU Bayesian-NN step (one network copy per sample, FP32)
+    gives the oracle's loss, and its first Adam step moves every parameter
+    against the oracle's gradient."""
+    from oracle import bnn
+    from oracle.cpu_baseline import bnn_klqp_step
+    from oracle.philox import KIND_EPS, normals
+    D, H1, H2, M, S = 6, 12, 10, 80, 3
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((M, D)).astype(np.float32)
+    y = rng.standard_normal(M).astype(np.float32)
+    P = bnn.n_params(D, H1, H2)
+    mu = (rng.standard_normal(P) * 0.3).astype(np.float32)
+    rho = np.full(P, -2.0, np.float32)
+    eps = normals(5, KIND_EPS, 0, S, P)
+    loss64, gmu64, _ = bnn.klqp_loss_and_grads(mu, rho, eps, X, y, 0.3, 2.0, D, H1, H2)
+    mu0 = mu.copy()
+    m, v = np.zeros(2 * P, np.float32), np.zeros(2 * P, np.float32)
+    loss = bnn_klqp_step(X, y, mu, rho, m, v, 0, S, 5, 0.3, 2.0, D, H1, H2, 1e-3)
+    assert abs(loss - loss64) <= 1e-4 * abs(loss64)
+    big = np.abs(gmu64) > 1e-3 * np.abs(gmu64).max()
+    assert np.all(np.sign(mu0 - mu)[big] == np.sign(gmu64)[big])
