@@ -94,6 +94,8 @@ struct TcArgs {
   const float* y;  // the model's observations (the epilogue reads them directly)
   int ntiles, N, P, PP, lik;
   float inv_lik_var, lik_norm;
+  float zscale;  // Z is broadcast as zscale * z: -log2(e) for Bernoulli (the MMA gives
+                 // -log2(e) eta, the exponent the residual needs), 1 for Normal
   const float* prior_loc;
   const float* prior_scale;
   int C, n_iter, n_steps, cache_valid;
@@ -115,22 +117,25 @@ struct TcArgs {
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
 
 
-// Residuals r = d log p(y | eta) / d eta of 8 consecutive rows (eta in v on
-// entry), split into tf32 hi (v) and lo = r - hi (exact; only the tensor core's
-// own rounding of lo, a relative 2^-21 of r, remains).
+// Residuals r = d log p(y | eta) / d eta of 8 consecutive rows, split into
+// tf32 hi (v) and lo = r - hi.  On entry v holds what the forward MMA gave:
+// w = -log2(e) eta for Bernoulli (Z was broadcast scaled), eta for Normal.
+// hi keeps r's top 10 mantissa bits (truncation: one logical operation) and
+// lo = r - hi is exact; the tensor core's own truncation of lo leaves a
+// relative 2^-20 of r.
 //   LL (the evaluation also needs the log-likelihood): Bernoulli with
-//     e = e^-|eta| = 2^(-|eta| log2 e) <= 1 and a = 1 + e: sigmoid(eta) = 1/a
-//     (eta >= 0) or e/a, one reciprocal per pair of rows, and
-//     log p(y | eta) = -(max(eta, 0) - eta y + log1p(e)) with
-//     log1p(e) = ln 2 * log2(a) (absolute error ~2e-7 per row); the 8 rows'
-//     terms are summed in FP32 and added to kl (compensated) once.  Rows at
-//     or beyond nvalid get r = 0 and add nothing to kl.
-//   otherwise the short form: Bernoulli sigmoid(eta) = 1 / (1 + e^-eta) with
-//     e^-eta = 2^(-eta log2 e) and one reciprocal per PAIR of rows,
-//     1/a = b / (a b), 1/b = a / (a b); e^-eta is capped at e^40 so that a b
-//     stays below 2^116 (sigmoid changes by at most e^-40 absolute).  Rows
-//     beyond N are not masked: their X rows are zero, so their r only ever
-//     multiplies zeros in the backward MMA.
+//     e = 2^-|w| = e^-|eta| <= 1 and a = 1 + e: sigmoid(eta) = 1/a
+//     (eta >= 0, i.e. w <= 0) or e/a, one reciprocal per pair of rows, and
+//     log p(y | eta) = -(max(eta, 0) - eta y + log1p(e))
+//                    = -ln 2 (max(-w, 0) + w y + log2(a))
+//     (absolute error ~2e-7 per row); the 8 rows' terms are summed in FP32
+//     and added to kl (compensated) once.  Rows at or beyond nvalid get r = 0
+//     and add nothing to kl.
+//   otherwise the short form: Bernoulli sigmoid(eta) = 1 / (1 + 2^w) with one
+//     reciprocal per PAIR of rows, 1/a = b / (a b), 1/b = a / (a b); 2^w is
+//     capped at e^40 so that a b stays below 2^116 (sigmoid changes by at most
+//     e^-40 absolute).  Rows beyond N are not masked: their X rows are zero,
+//     so their r only ever multiplies zeros in the backward MMA.
 template <bool LL, bool BERN>
 __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float (&y)[8],
                                                int nvalid, float inv_var, float lik_norm,
@@ -142,19 +147,19 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
       float e[8], a[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        e[k] = ex2_approx(-kLog2e * fabsf(v[k]));
+        e[k] = ex2_approx(-fabsf(v[k]));
         a[k] = 1.0f + e[k];
       }
 #pragma unroll
       for (int k = 0; k < 8; k += 2) {
         const float ir = rcp_approx(a[k] * a[k + 1]);
         const float s0 = a[k + 1] * ir, s1 = a[k] * ir;  // 1/a[k], 1/a[k+1]
-        r[k] = y[k] - (v[k] >= 0.0f ? s0 : e[k] * s0);
-        r[k + 1] = y[k + 1] - (v[k + 1] >= 0.0f ? s1 : e[k + 1] * s1);
+        r[k] = y[k] - (v[k] <= 0.0f ? s0 : e[k] * s0);
+        r[k + 1] = y[k + 1] - (v[k + 1] <= 0.0f ? s1 : e[k + 1] * s1);
       }
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        const float l = (fmaxf(v[k], 0.0f) - v[k] * y[k]) + kLn2 * lg2_approx(a[k]);
+        const float l = kLn2 * ((fmaxf(-v[k], 0.0f) + v[k] * y[k]) + lg2_approx(a[k]));
         part -= k < nvalid ? l : 0.0f;
       }
     } else {
@@ -172,7 +177,7 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
     constexpr float kCap = 57.70780163555854f;  // 40 log2 e
     float a[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = 1.0f + ex2_approx(fminf(-kLog2e * v[k], kCap));
+    for (int k = 0; k < 8; ++k) a[k] = 1.0f + ex2_approx(fminf(v[k], kCap));
 #pragma unroll
     for (int k = 0; k < 8; k += 2) {
       const float ir = rcp_approx(a[k] * a[k + 1]);
@@ -185,7 +190,7 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
   }
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    v[k] = tf32_rna(r[k]);
+    v[k] = __uint_as_float(__float_as_uint(r[k]) & 0xFFFFE000u);
     lo[k] = r[k] - v[k];
   }
 }
@@ -352,7 +357,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           float h[4], lo4[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const float v = zr[i + j];
+            const float v = zr[i + j] * a.zscale;
             h[j] = tf32_rna(v);
             lo4[j] = tf32_rna(v - h[j]);
           }
@@ -804,6 +809,7 @@ extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, 
   a.P = m.P;
   a.PP = PP;
   a.lik = m.lik;
+  a.zscale = m.lik == EDG_LIK_BERNOULLI ? -kLog2e : 1.0f;
   a.inv_lik_var = m.inv_lik_var;
   a.lik_norm = m.lik_norm;
   a.prior_loc = m.prior_loc;
