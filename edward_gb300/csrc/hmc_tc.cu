@@ -30,6 +30,7 @@
 // waiting further, so no launch can hang.
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 
 #include "edg_common.cuh"
 #include "tc_common.cuh"
@@ -518,64 +519,73 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         tc_fence_before();
         __syncwarp();
       };
-      for (int i = 0; i < nt; ++i) {
-        const uint32_t g = gt + i, b = g & 1u;
-        // y of this thread's 16 rows straight from the model (L2-resident;
-        // the next tile's rows are prefetched into L1 below, since eta is
-        // usually ready when a tile starts and would not hide an L2 latency)
-        const int row0 = (t_begin + i) * kNR + 16 * qs;
-        const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
-        float ye[16];
-        if (nvalid >= 16 && y_vec) {
-          const float4* y4p = reinterpret_cast<const float4*>(a.y + row0);
+      // The tile loop, compiled once per (log-likelihood wanted, likelihood)
+      // and selected once per evaluation, so the loop body has no branch on
+      // either.
+      auto tile_loop = [&](auto ll_tag, auto bern_tag) {
+        constexpr bool LL = decltype(ll_tag)::value;
+        constexpr bool BERN = decltype(bern_tag)::value;
+        for (int i = 0; i < nt; ++i) {
+          const uint32_t g = gt + i, b = g & 1u;
+          // y of this thread's 16 rows straight from the model (L2-resident;
+          // the next tile's rows are prefetched into L1 below, since eta is
+          // usually ready when a tile starts and would not hide an L2 latency)
+          const int row0 = (t_begin + i) * kNR + 16 * qs;
+          const int nvalid = min(kNR, a.N - (t_begin + i) * kNR) - 16 * qs;
+          float ye[16];
+          if (nvalid >= 16 && y_vec) {
+            const float4* y4p = reinterpret_cast<const float4*>(a.y + row0);
 #pragma unroll
-          for (int k4 = 0; k4 < 4; ++k4) {
-            const float4 y4 = __ldg(y4p + k4);
-            ye[4 * k4] = y4.x;
-            ye[4 * k4 + 1] = y4.y;
-            ye[4 * k4 + 2] = y4.z;
-            ye[4 * k4 + 3] = y4.w;
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 16; ++k) ye[k] = k < nvalid ? __ldg(a.y + row0 + k) : 0.0f;
-        }
-        if (lane == 0 && i + 1 < nt) prefetch_l1(a.y + min(row0 + kNR, a.N - 1));
-        mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
-        tc_fence_after();
-        // eta of 16 rows in one TMEM load; then two halves of 8 rows:
-        // residuals, st hi / lo.  One compact loop per (log-likelihood wanted,
-        // likelihood), so the leapfrog's inner evaluations run the short
-        // residual-only loop.
-        float ve[16];
-        tmem_ld16_issue(tl + COL_ETA(b) + 16 * qs, ve);
-        tmem_ld_wait(ve);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          float lo[8];
-          float (&v)[8] = *reinterpret_cast<float (*)[8]>(&ve[8 * h]);
-          const float (&yh)[8] = *reinterpret_cast<const float (*)[8]>(&ye[8 * h]);
-          const uint32_t col = 16 * qs + 8 * h;
-          const int nv = nvalid - 8 * h;
-          if (need_ll) {
-            if (a.lik == EDG_LIK_BERNOULLI)
-              residual_block<true, true>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
-            else
-              residual_block<true, false>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+            for (int k4 = 0; k4 < 4; ++k4) {
+              const float4 y4 = __ldg(y4p + k4);
+              ye[4 * k4] = y4.x;
+              ye[4 * k4 + 1] = y4.y;
+              ye[4 * k4 + 2] = y4.z;
+              ye[4 * k4 + 3] = y4.w;
+            }
           } else {
-            if (a.lik == EDG_LIK_BERNOULLI)
-              residual_block<false, true>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
-            else
-              residual_block<false, false>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) ye[k] = k < nvalid ? __ldg(a.y + row0 + k) : 0.0f;
           }
-          tmem_st8(tl + COL_RHI(b) + col, v);
-          tmem_st8(tl + COL_RLO(b) + col, lo);
+          if (lane == 0 && i + 1 < nt) prefetch_l1(a.y + min(row0 + kNR, a.N - 1));
+          mbar_wait(b_eta + 8 * b, (g >> 1) & 1u, err);
+          tc_fence_after();
+          // eta of 16 rows in one TMEM load; then two halves of 8 rows:
+          // residuals, st hi / lo.  One compact loop per (log-likelihood wanted,
+          // likelihood), so the leapfrog's inner evaluations run the short
+          // residual-only loop.
+          float ve[16];
+          tmem_ld16_issue(tl + COL_ETA(b) + 16 * qs, ve);
+          tmem_ld_wait(ve);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            float lo[8];
+            float (&v)[8] = *reinterpret_cast<float (*)[8]>(&ve[8 * h]);
+            const float (&yh)[8] = *reinterpret_cast<const float (*)[8]>(&ye[8 * h]);
+            const uint32_t col = 16 * qs + 8 * h;
+            const int nv = nvalid - 8 * h;
+            residual_block<LL, BERN>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+            tmem_st8(tl + COL_RHI(b) + col, v);
+            tmem_st8(tl + COL_RLO(b) + col, lo);
+          }
+          tmem_st_wait();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(b_r + 8 * b);
+          if (i >= 1) consume_gpart(i - 1);
         }
-        tmem_st_wait();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(b_r + 8 * b);
-        if (i >= 1) consume_gpart(i - 1);
+      };
+      const bool bern = a.lik == EDG_LIK_BERNOULLI;
+      if (need_ll) {
+        if (bern)
+          tile_loop(std::true_type{}, std::true_type{});
+        else
+          tile_loop(std::true_type{}, std::false_type{});
+      } else {
+        if (bern)
+          tile_loop(std::false_type{}, std::true_type{});
+        else
+          tile_loop(std::false_type{}, std::false_type{});
       }
       consume_gpart(nt - 1);
       // this CTA's partial gradient and log-likelihood for the owners
