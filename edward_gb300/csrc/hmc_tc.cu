@@ -302,8 +302,11 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
   const float eps = a.step_size, half = 0.5f * a.step_size;
   const uint32_t zhi_addr = smem_u32(Zhi), zlo_addr = smem_u32(Zlo);
   // end-of-evaluation exchange buffers (alias stage 0, idle between evaluations)
-  float* Gsum = reinterpret_cast<float*>(stage0);                   // [128][PP]
-  double* llpart = reinterpret_cast<double*>(stage0 + 512 * PP);    // [4][128]
+  // Gsum rows are PP + 4 floats apart, so the epilogue's row-per-lane float4
+  // stores spread over 8 bank groups
+  const int GS = PP + 4;
+  float* Gsum = reinterpret_cast<float*>(stage0);                           // [128][PP + 4]
+  double* llpart = reinterpret_cast<double*>(stage0 + (size_t)kCT * GS * 4);  // [4][128]
   const uint32_t gsum_addr = smem_u32(Gsum), llpart_addr = smem_u32(llpart);
 
   // every CTA of the cluster must be running before any DSMEM access
@@ -592,7 +595,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
       for (int c4 = 0; c4 < 4; ++c4)
         if (4 * c4 < gcols)
-          *reinterpret_cast<float4*>(Gsum + row * PP + gc0 + 4 * c4) =
+          *reinterpret_cast<float4*>(Gsum + row * GS + gc0 + 4 * c4) =
               make_float4(Gacc[4 * c4], Gacc[4 * c4 + 1], Gacc[4 * c4 + 2], Gacc[4 * c4 + 3]);
       if (need_ll) llpart[qs * kCT + row] = kl.value();
       tc_fence_before();
@@ -610,7 +613,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
         for (int i = 0; i < kMaxEPT; i += 4) {
           if (i < EPT) {
-            const float4 v = ld_dsmem4(mapa(gsum_addr + 4u * (cc * PP + d0 + i), q));
+            const float4 v = ld_dsmem4(mapa(gsum_addr + 4u * (cc * GS + d0 + i), q));
             G[i] += v.x;
             G[i + 1] += v.y;
             G[i + 2] += v.z;
