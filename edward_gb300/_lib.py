@@ -56,7 +56,8 @@ class EdgOpt(ctypes.Structure):
 
 class EdgKLqp(ctypes.Structure):
     _fields_ = [("method", c_int32), ("n_samples", c_int32), ("data_scale", c_float),
-                ("kl_scaling", c_void_p), ("latent_scale", c_void_p), ("seed", c_uint64)]
+                ("kl_scaling", c_void_p), ("latent_scale", c_void_p), ("seed", c_uint64),
+                ("point", c_void_p)]
 
 
 class EdgHier(ctypes.Structure):

@@ -9,6 +9,9 @@ description of a supported family and evaluates it with fused kernels:
   with Normal priors on w and b.  Covers ``ed.dot`` regressions
   (``tests/inferences/hmc_test.py:48-91``) and the Normal-Normal model
   (``tests/inferences/klqp_test.py:14-44``: x ~ Normal(mu, 1), X = ones).
+  w or b may also be trainable Variables of the model (model parameters, the
+  reference's p_vars: ``klqp.py:902-904``, ``variational_inference.py:62-64``;
+  ``klqp_test.py:46-56`` fits Bernoulli(probs=sigmoid(Variable))).
 
 Models outside the supported families raise NotImplementedError.  This
 module is host-only and runs without a GPU.
@@ -26,10 +29,11 @@ LIK_BERNOULLI, LIK_NORMAL = 0, 1
 
 @dataclass
 class LatentBlock:
-    rv: RandomVariable      # prior random variable
+    rv: RandomVariable      # prior random variable (a Variable for a model parameter)
     offset: int             # first coordinate in the flat parameter vector z
     size: int
     shape: Tuple[int, ...]
+    point: bool = False     # a model parameter: no prior, no q, point value
 
 
 @dataclass
@@ -90,9 +94,11 @@ def _prior(rv, bindings):
     return np.broadcast_to(loc, shp).reshape(-1), np.broadcast_to(scale, shp).reshape(-1), shp
 
 
-def compile_glm(latents, data):
+def compile_glm(latents, data, params=False):
     """``latents``: list of prior RandomVariables; ``data``: Edward data dict.
-    Returns a GLMSpec or raises UnsupportedModel."""
+    ``params``: trainable Variables in the linear predictor are model
+    parameters (KLqp fits them; the samplers do not take them).  Returns a
+    GLMSpec or raises UnsupportedModel."""
     observed, bindings = _split_data(data)
     if len(observed) != 1:
         raise UnsupportedModel("the GLM family has exactly one observed random variable")
@@ -107,9 +113,14 @@ def compile_glm(latents, data):
             raise UnsupportedModel("the GLM family needs the observed values bound to an array")
     y = np.asarray(yval, np.float32).reshape(-1)
     if isinstance(yrv, Bernoulli):
-        if yrv.logits is None:
-            raise UnsupportedModel("Bernoulli likelihood must be parameterised by logits")
-        eta, lik, lik_scale = yrv.logits, LIK_BERNOULLI, 1.0
+        if yrv.logits is not None:
+            eta = yrv.logits
+        elif isinstance(yrv.probs, Op) and yrv.probs.op == "sigmoid":
+            eta = yrv.probs.args[0]        # Bernoulli(probs=sigmoid(e)) = Bernoulli(logits=e)
+        else:
+            raise UnsupportedModel("Bernoulli likelihood must be parameterised by logits "
+                                   "or probs=sigmoid(...)")
+        lik, lik_scale = LIK_BERNOULLI, 1.0
     elif isinstance(yrv, Normal):
         eta, lik = yrv.loc, LIK_NORMAL
         s = _const_param(yrv.scale, "likelihood scale", bindings)
@@ -120,27 +131,48 @@ def compile_glm(latents, data):
         raise UnsupportedModel(f"unsupported likelihood {type(yrv).__name__}")
 
     latent_set = set(id(z) for z in latents)
+
+    def is_param(n):
+        return params and isinstance(n, Variable) and n.trainable
+
     dot_terms, bias_terms = [], []
     for term in flatten_add(eta):
         if isinstance(term, Op) and term.op == "dot":
             Xn, w = term.args
-            if not isinstance(w, RandomVariable) or id(w) not in latent_set:
-                raise UnsupportedModel("ed.dot(X, w) needs w to be a latent random variable")
+            if not (isinstance(w, RandomVariable) and id(w) in latent_set) and not is_param(w):
+                raise UnsupportedModel("ed.dot(X, w) needs w to be a latent random variable or a "
+                                       "trainable Variable")
             if isinstance(Xn, Placeholder) and isinstance(bindings.get(Xn), (list, tuple)):
                 raise UnsupportedModel("X bound to a list (ragged instances) is not a GLM")
             X = const_value(Xn, bindings)
             if X is None:
                 raise UnsupportedModel("X in ed.dot(X, w) must be data (an array or a bound placeholder)")
             dot_terms.append((np.asarray(X, np.float32), w))
-        elif isinstance(term, RandomVariable) and id(term) in latent_set:
+        elif (isinstance(term, RandomVariable) and id(term) in latent_set) or is_param(term):
             bias_terms.append(term)
         else:
             raise UnsupportedModel(f"term {term!r} of the linear predictor is not supported")
     if len(dot_terms) > 1 or len(bias_terms) > 1:
         raise UnsupportedModel("the GLM family supports one ed.dot term and one intercept")
     used = [w for _, w in dot_terms] + bias_terms
-    if set(id(z) for z in used) != latent_set or len(used) != len(latent_set):
+    used_rv = [z for z in used if isinstance(z, RandomVariable)]
+    if set(id(z) for z in used_rv) != latent_set or len(used_rv) != len(latent_set):
         raise UnsupportedModel("every latent variable must appear once in the linear predictor")
+    if not used:
+        raise UnsupportedModel("the linear predictor has no latent variable or model parameter")
+
+    def block(rv, offset, size):
+        """(LatentBlock, prior loc, prior scale); a model parameter gets a
+        placeholder N(0, 1) prior that no kernel reads."""
+        if is_param(rv):
+            if int(np.prod(rv.shape)) != size:
+                raise ValueError(f"{rv.name} has {int(np.prod(rv.shape))} elements; {size} needed")
+            return (LatentBlock(rv, offset, size, tuple(rv.shape), point=True),
+                    np.zeros(size), np.ones(size))
+        loc, scale, shp = _prior(rv, bindings)
+        if int(np.prod(shp)) != size:
+            raise ValueError(f"{rv.name} has {int(np.prod(shp))} elements; {size} needed")
+        return LatentBlock(rv, offset, size, shp), loc, scale
 
     N = y.shape[0]
     blocks, locs, scales = [], [], []
@@ -148,29 +180,28 @@ def compile_glm(latents, data):
         X, w = dot_terms[0]
         if X.ndim != 2 or X.shape[0] != N:
             raise ValueError(f"X has shape {X.shape}; expected [{N}, D]")
-        loc, scale, shp = _prior(w, bindings)
-        if int(np.prod(shp)) != X.shape[1]:
-            raise ValueError(f"w has {int(np.prod(shp))} elements but X has {X.shape[1]} columns")
-        blocks.append(LatentBlock(w, 0, X.shape[1], shp))
+        blk, loc, scale = block(w, 0, X.shape[1])
+        blocks.append(blk)
         locs.append(loc)
         scales.append(scale)
         bias = bool(bias_terms)
         if bias:
             b = bias_terms[0]
-            loc, scale, shp = _prior(b, bindings)
-            if int(np.prod(shp)) != 1:
-                raise UnsupportedModel("the intercept must be a scalar (or shape [1]) latent")
-            blocks.append(LatentBlock(b, X.shape[1], 1, shp))
+            if int(np.prod(getattr(b, "shape", ()) or (1,))) != 1:
+                raise UnsupportedModel("the intercept must be a scalar (or shape [1])")
+            blk, loc, scale = block(b, X.shape[1], 1)
+            blocks.append(blk)
             locs.append(loc)
             scales.append(scale)
     else:
-        # x ~ Lik(mu): a scalar latent broadcast over all rows (Normal-Normal)
+        # x ~ Lik(mu): a scalar latent (Normal-Normal) or model parameter broadcast
+        # over all rows
         mu = bias_terms[0]
-        loc, scale, shp = _prior(mu, bindings)
-        if int(np.prod(shp)) != 1:
-            raise UnsupportedModel("a latent used without ed.dot must be a scalar")
+        if int(np.prod(getattr(mu, "shape", ()) or (1,))) != 1:
+            raise UnsupportedModel("a latent or parameter used without ed.dot must be a scalar")
         X = np.ones((N, 1), np.float32)
-        blocks.append(LatentBlock(mu, 0, 1, shp))
+        blk, loc, scale = block(mu, 0, 1)
+        blocks.append(blk)
         locs.append(loc)
         scales.append(scale)
         bias = False

@@ -86,6 +86,7 @@ struct KlqpArgs {
   float dscale;
   const float* kl_scaling;
   const float* latent_scale;
+  const int32_t* point;  // model parameters: z = mu, no prior, no q, pathwise gradient
   uint64_t seed;
   edg_opt_t opt;
   float* mu;
@@ -118,10 +119,12 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   // the first X tile's copy overlaps the draws below
   if (re > rb) issue_tile<CT>(m, S.Xs, S.ys, rb, re);
   cp_async_commit();
-  for (int d = threadIdx.x; d < PP; d += kThreads) sig[d] = d < P ? softplusf(a.rho[d]) : 0.0f;
+  for (int d = threadIdx.x; d < PP; d += kThreads)
+    sig[d] = (d < P && !(a.point && a.point[d])) ? softplusf(a.rho[d]) : 0.0f;
   init_x_pad<CT>(m, S);
   __syncthreads();
-  const bool need_grad = a.method != EDG_KLQP_SCORE;
+  // the score method needs d log p / d z only for model parameters
+  const bool need_grad = a.method != EDG_KLQP_SCORE || a.point != nullptr;
   for (int s0 = 0; s0 < a.S; s0 += CT) {
     for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
       const int c = idx / PP, d = idx - c * PP;
@@ -203,6 +206,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     for (int s = warp; s < a.S; s += kThreads / 32) {
       double acc = 0.0;
       for (int d = lane; d < P; d += 32) {
+        if (a.point && a.point[d]) continue;
         const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
         const float e = epsS[s * PP + d];
         const float zv = a.mu[d] + sig[d] * e;
@@ -223,6 +227,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   if (a.method == EDG_KLQP_REPARAM_KL) {
     double kl = 0.0;
     for (int d = threadIdx.x; d < P; d += kThreads) {
+      if (a.point && a.point[d]) continue;
       const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
       const float sp = m.prior_scale[d], sq = sig[d];
       const float dm = (a.mu[d] - m.prior_loc[d]) / sp;
@@ -266,7 +271,13 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     const float ps = m.prior_scale[d], pl = m.prior_loc[d];
     const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
     float gmu = 0.0f, gsig = 0.0f;
-    if (a.method == EDG_KLQP_REPARAM_KL) {
+    const bool point = a.point && a.point[d];
+    if (point) {
+      // model parameter: d loss / d theta = -mean_s d log p(x | z_s) / d theta
+      float sg_mu = 0.0f;
+      for (int s = 0; s < a.S; ++s) sg_mu += gS[s * PP + d];
+      gmu = -sg_mu * invS;
+    } else if (a.method == EDG_KLQP_REPARAM_KL) {
       float sg_mu = 0.0f, sg_sig = 0.0f;
       for (int s = 0; s < a.S; ++s) {
         const float e = epsS[s * PP + d];
@@ -302,7 +313,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       gmu = -acc_mu * invS;
       gsig = -acc_sig * invS;
     }
-    const float grho = gsig * sigmoidf(rho);
+    const float grho = point ? 0.0f : gsig * sigmoidf(rho);
     if (!isfinite(gmu) || !isfinite(grho)) atomicAdd(&a.state->nonfinite, 1u);
     if (a.grad_out) {
       a.grad_out[d] = gmu;
@@ -311,7 +322,8 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     if (a.apply) {
       const int n = 2 * P;
       a.mu[d] = opt_apply(a.opt, mu, gmu, a.slots + d, a.slots + n + d, lr, b1p, b2p);
-      a.rho[d] = opt_apply(a.opt, rho, grho, a.slots + P + d, a.slots + n + P + d, lr, b1p, b2p);
+      if (!point)
+        a.rho[d] = opt_apply(a.opt, rho, grho, a.slots + P + d, a.slots + n + P + d, lr, b1p, b2p);
     }
   }
   __syncthreads();
@@ -704,6 +716,7 @@ extern "C" int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg,
   a.dscale = cfg->data_scale;
   a.kl_scaling = cfg->kl_scaling;
   a.latent_scale = cfg->latent_scale;
+  a.point = cfg->point;
   a.seed = cfg->seed;
   a.opt = *opt;
   a.mu = mu;

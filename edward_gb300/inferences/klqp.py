@@ -84,7 +84,8 @@ class KLqp(VariationalInference):
     def _validate(self):
         method = self._choose_method()
         latents = list(self.latent_vars.keys())
-        discrete = all(not q.reparameterizable for q in self.latent_vars.values())
+        discrete = bool(self.latent_vars) and all(not q.reparameterizable
+                                                  for q in self.latent_vars.values())
         self._rao_blackwell = method == SCORE_RB
         if method == SCORE_RB and not discrete:
             raise NotImplementedError(
@@ -101,7 +102,7 @@ class KLqp(VariationalInference):
             return
         method = self._method_id
         try:
-            self._spec = compile_glm(latents, self.data)
+            self._spec = compile_glm(latents, self.data, params=True)
             self._family = "glm"
         except UnsupportedModel as e_glm:
             try:
@@ -132,7 +133,8 @@ class KLqp(VariationalInference):
         if self._family == "glm" and self.n_minibatch is not None:
             raise NotImplementedError("n_minibatch applies to the Bayesian NN family")
         for blk in self._spec.blocks:
-            parse_normal_q(self.latent_vars[blk.rv])
+            if not getattr(blk, "point", False):
+                parse_normal_q(self.latent_vars[blk.rv])
 
     def build_loss_and_gradients(self, var_list):
         if self._family == "expfam":
@@ -159,6 +161,11 @@ class KLqp(VariationalInference):
             raise NotImplementedError("per-row data scale is not supported; pass a scalar")
         self._kls = torch.as_tensor(kls, device=dev)
         self._lsc = torch.as_tensor(lsc, device=dev)
+        point = np.zeros(P, np.int32)
+        for blk in spec.blocks:
+            if blk.point:
+                point[blk.offset:blk.offset + blk.size] = 1
+        self._point = torch.as_tensor(point, device=dev) if point.any() else None
         self._slots = torch.zeros(4 * P, dtype=torch.float32, device=dev)
         self._reset_optimizer()
         cfg = _lib.EdgKLqp()
@@ -167,6 +174,7 @@ class KLqp(VariationalInference):
         cfg.data_scale = float(dscale.reshape(-1)[0])
         cfg.kl_scaling = self._kls.data_ptr()
         cfg.latent_scale = self._lsc.data_ptr()
+        cfg.point = self._point.data_ptr() if self._point is not None else None
         cfg.seed = next_seed()
         self._cfg = cfg
         self._opt = self.optimizer.to_c()
@@ -184,6 +192,13 @@ class KLqp(VariationalInference):
         self._rho = torch.empty(spec.P, dtype=torch.float32, device=dev)
         q_vars = []
         for blk in spec.blocks:
+            if getattr(blk, "point", False):
+                # a model parameter: its value lives in mu (rho is unused)
+                var = blk.rv
+                var._rebind(self._mu[blk.offset:blk.offset + blk.size].view(var.shape or ()))
+                self._rho[blk.offset:blk.offset + blk.size].zero_()
+                q_vars.append(var)
+                continue
             q = parse_normal_q(self.latent_vars[blk.rv])
             for var, buf in ((q.loc_var, self._mu), (q.rho_var, self._rho)):
                 if int(np.prod(var.shape)) != blk.size:

@@ -119,6 +119,10 @@ typedef struct {
   const float* kl_scaling;   /* [P] or NULL (= 1) */
   const float* latent_scale; /* [P] or NULL (= 1): Inference.scale[z] */
   uint64_t seed;
+  const int32_t* point;      /* [P] or NULL: 1 marks a model parameter (a trainable variable
+                                of the model, not a latent: no prior and no q; z = mu and its
+                                gradient is the pathwise gradient of the loss, as the
+                                reference's p_vars get, klqp.py:902-904); rho is left as is */
 } edg_klqp_t;
 
 /* HMC configuration (HMC.initialize, edward/inferences/hmc.py:45-59). */
@@ -401,13 +405,15 @@ typedef struct {
   const double* prior;  /* device: (a, b) | (a, rate) | alpha[K + 1] */
   const double* stats;  /* device: (n1, n0) | (sum x, N, sum log x!) | counts[K + 1] */
 } edg_expfam_t;
-/* HMC over C chains (FP64 state u [C, K], gradient and log joint caches, the
- * reference's leapfrog and Metropolis test); Philox streams and overrides as in
- * edg_hmc_glm_run; samples [T_cap, C, K] (unconstrained) or NULL. */
+/* HMC over C chains (FP32 state u [C, K] and gradient cache, FP64 log joint
+ * cache lj [C]; the reference's leapfrog and Metropolis test, with the log
+ * joint's terms and the energy difference summed in FP64); Philox streams and
+ * overrides (r_override FP32 [n_iter, C, K], u_override FP64 [n_iter, C]) as
+ * in edg_hmc_glm_run; samples FP32 [T_cap, C, K] (unconstrained) or NULL. */
 int edg_expfam_hmc_run(const edg_expfam_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
-                       double* u, double* grad, double* lj, int32_t cache_valid,
-                       int32_t* n_accept, edg_state_t* state, double* samples, int64_t T_cap,
-                       const double* r_override, const double* u_override, void* stream);
+                       float* u, float* grad, double* lj, int32_t cache_valid,
+                       int32_t* n_accept, edg_state_t* state, float* samples, int64_t T_cap,
+                       const float* r_override, const double* u_override, void* stream);
 /* One KLqp step with q(u) = N(mu, softplus(rho)) [K]: reparameterisation gradient
  * with Monte Carlo KL (klqp.py:642-704), S <= 256 draws (Philox stream 0 at
  * iteration state->t, or eps_override [S, K]), then the optimizer apply
