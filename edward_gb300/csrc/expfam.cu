@@ -5,8 +5,9 @@
 //   Gamma(a, rate b) + Poisson(rate=z)      : z = softplus(u)
 //   Dirichlet(alpha) + Categorical(probs=z) : z = softmax([u, 0])  (SoftmaxCentered)
 // The target is log p(x, z(u)) + log|det dz/du|, from the observations'
-// sufficient statistics; everything is FP64 (the models are a handful of
-// numbers per chain).
+// sufficient statistics.  The chain state, the momenta and every per-term
+// quantity are FP32; FP64 is used only for the sum of the log joint's terms
+// and for the Hamiltonian energy difference of the Metropolis test.
 //   edg_expfam_hmc_run   HMC over C chains, one thread per chain, the
 //                        reference's leapfrog (hmc.py:195-210) and
 //                        Metropolis test (hmc.py:98-118), n_iter iterations
@@ -25,68 +26,71 @@ namespace ef {
 
 constexpr int kMaxK = 32;  // unconstrained dimension (Dirichlet: categories - 1)
 
-__device__ __forceinline__ double softplus_d(double x) {
-  return fmax(x, 0.0) + log1p(exp(-fabs(x)));
+__device__ __forceinline__ float softplus_f(float x) {
+  return fmaxf(x, 0.0f) + log1pf(expf(-fabsf(x)));
 }
-__device__ __forceinline__ double sigmoid_d(double x) {
-  const double e = exp(-fabs(x));
-  return x >= 0.0 ? 1.0 / (1.0 + e) : e / (1.0 + e);
+__device__ __forceinline__ float sigmoid_f(float x) {
+  const float e = expf(-fabsf(x));
+  return x >= 0.0f ? 1.0f / (1.0f + e) : e / (1.0f + e);
 }
 
 // log p(x, z(u)) + log|det dz/du| (up to the data's constant terms for
-// Dirichlet-Categorical, which carries none) and its gradient g[K].
-__device__ double log_joint_grad(const edg_expfam_t& m, const double* u, double* g) {
+// Dirichlet-Categorical, which carries none) and its gradient g[K].  Every
+// term that depends on u, and the gradient, is FP32; the terms and the
+// model's constants (the priors' normalisers) are summed in FP64.
+__device__ double log_joint_grad(const edg_expfam_t& m, const float* u, float* g) {
   const double* pr = m.prior;
   const double* st = m.stats;
   if (m.family == EDG_EXPFAM_BETA) {
-    const double a = pr[0], b = pr[1], n1 = st[0], n0 = st[1];
-    const double lz = -softplus_d(-u[0]), l1z = -softplus_d(u[0]);
-    const double s = sigmoid_d(u[0]);
-    g[0] = (a + n1) * (1.0 - s) - (b + n0) * s;
-    return (a - 1.0 + n1 + 1.0) * lz + (b - 1.0 + n0 + 1.0) * l1z -
-           (lgamma(a) + lgamma(b) - lgamma(a + b));
+    const float a = (float)pr[0], b = (float)pr[1], n1 = (float)st[0], n0 = (float)st[1];
+    const float lz = -softplus_f(-u[0]), l1z = -softplus_f(u[0]);
+    const float s = sigmoid_f(u[0]);
+    g[0] = (a + n1) * (1.0f - s) - (b + n0) * s;
+    return (double)((a + n1) * lz) + (double)((b + n0) * l1z) -
+           (lgamma(pr[0]) + lgamma(pr[1]) - lgamma(pr[0] + pr[1]));
   }
   if (m.family == EDG_EXPFAM_GAMMA) {
-    const double a = pr[0], rate = pr[1], sx = st[0], n = st[1], slf = st[2];
-    const double z = softplus_d(u[0]), dz = sigmoid_d(u[0]);
-    const double lz = log(z);
-    g[0] = ((a - 1.0 + sx) / z - rate - n) * dz + sigmoid_d(-u[0]);
-    return a * log(rate) - lgamma(a) + (a - 1.0 + sx) * lz - (rate + n) * z - slf -
-           softplus_d(-u[0]);
+    const float a = (float)pr[0], rate = (float)pr[1], sx = (float)st[0], n = (float)st[1];
+    const float z = softplus_f(u[0]), dz = sigmoid_f(u[0]);
+    const float lz = logf(z);
+    g[0] = ((a - 1.0f + sx) / z - rate - n) * dz + sigmoid_f(-u[0]);
+    return pr[0] * log(pr[1]) - lgamma(pr[0]) + (double)((a - 1.0f + sx) * lz) -
+           (double)((rate + n) * z) - st[2] - (double)softplus_f(-u[0]);
   }
   // Dirichlet-Categorical, SoftmaxCentered: z = softmax([u, 0])
   const int K = m.K;
-  double mx = 0.0;
-  for (int j = 0; j < K; ++j) mx = fmax(mx, u[j]);
-  double den = exp(-mx);
-  for (int j = 0; j < K; ++j) den += exp(u[j] - mx);
-  const double lden = mx + log(den);
-  double sw = 0.0, lj = 0.0, sa = 0.0, slga = 0.0;
+  float mx = 0.0f;
+  for (int j = 0; j < K; ++j) mx = fmaxf(mx, u[j]);
+  float den = expf(-mx);
+  for (int j = 0; j < K; ++j) den += expf(u[j] - mx);
+  const float lden = mx + logf(den);
+  float sw = 0.0f;
+  double lj = 0.0, sa = 0.0, slga = 0.0;
   for (int k = 0; k <= K; ++k) {
-    const double w = pr[k] + st[k];  // (alpha - 1) + counts + 1 (log-det term)
-    const double lz = (k < K ? u[k] : 0.0) - lden;
-    lj += w * lz;
+    const float w = (float)pr[k] + (float)st[k];  // (alpha - 1) + counts + 1 (log-det term)
+    const float lz = (k < K ? u[k] : 0.0f) - lden;
+    lj += (double)(w * lz);
     sw += w;
     sa += pr[k];
     slga += lgamma(pr[k]);
   }
-  for (int j = 0; j < K; ++j) g[j] = (pr[j] + st[j]) - exp(u[j] - lden) * sw;
+  for (int j = 0; j < K; ++j) g[j] = ((float)pr[j] + (float)st[j]) - expf(u[j] - lden) * sw;
   return lj + lgamma(sa) - slga;
 }
 
 struct HmcArgs {
   edg_expfam_t m;
   int C, n_iter, L, cache_valid;
-  double eps;
+  float eps;
   uint64_t seed;
-  double* u;      // [C, K]
-  double* grad;   // [C, K]
+  float* u;       // [C, K]
+  float* grad;    // [C, K]
   double* lj;     // [C]
   int32_t* n_accept;
   edg_state_t* state;
-  double* samples;  // [T_cap, C, K]
+  float* samples;  // [T_cap, C, K]
   int64_t T_cap;
-  const double* r_ovr;  // [n_iter, C, K]
+  const float* r_ovr;   // [n_iter, C, K]
   const double* u_ovr;  // [n_iter, C]
 };
 
@@ -95,7 +99,7 @@ __global__ void hmc_kernel(HmcArgs a) {
   const int K = a.m.K;
   const int64_t t0 = a.state->t;
   if (c < a.C) {
-    double z[kMaxK], g[kMaxK], z0[kMaxK], g0[kMaxK], r[kMaxK];
+    float z[kMaxK], g[kMaxK], z0[kMaxK], g0[kMaxK], r[kMaxK];
     for (int j = 0; j < K; ++j) z[j] = a.u[(int64_t)c * K + j];
     double lj;
     if (a.cache_valid) {
@@ -104,28 +108,30 @@ __global__ void hmc_kernel(HmcArgs a) {
     } else {
       lj = log_joint_grad(a.m, z, g);
     }
+    const float half = 0.5f * a.eps;
     for (int it = 0; it < a.n_iter; ++it) {
       const int64_t t = t0 + it;
-      double k0 = 0.0;
+      float k0 = 0.0f;
       for (int j = 0; j < K; ++j) {
         r[j] = a.r_ovr ? a.r_ovr[((int64_t)it * a.C + c) * K + j]
-                       : (double)philox_normal(a.seed, 1u, (uint32_t)t, (uint32_t)c, (uint32_t)j);
-        k0 += 0.5 * r[j] * r[j];
+                       : philox_normal(a.seed, 1u, (uint32_t)t, (uint32_t)c, (uint32_t)j);
+        k0 = fmaf(r[j], r[j], k0);
         z0[j] = z[j];
         g0[j] = g[j];
       }
       const double lj0 = lj;
       for (int l = 0; l < a.L; ++l) {
         for (int j = 0; j < K; ++j) {
-          r[j] += 0.5 * a.eps * g[j];
+          r[j] += half * g[j];
           z[j] += a.eps * r[j];
         }
         lj = log_joint_grad(a.m, z, g);
-        for (int j = 0; j < K; ++j) r[j] += 0.5 * a.eps * g[j];
+        for (int j = 0; j < K; ++j) r[j] += half * g[j];
       }
-      double k1 = 0.0;
-      for (int j = 0; j < K; ++j) k1 += 0.5 * r[j] * r[j];
-      const double ratio = k0 - k1 + lj - lj0;
+      float k1 = 0.0f;
+      for (int j = 0; j < K; ++j) k1 = fmaf(r[j], r[j], k1);
+      // the energy difference in FP64 (hmc.py:98-105)
+      const double ratio = 0.5 * (double)k0 - 0.5 * (double)k1 + lj - lj0;
       const double uu = a.u_ovr ? a.u_ovr[(int64_t)it * a.C + c]
                                 : u01d(philox_at(a.seed, 2u, (uint32_t)t, (uint32_t)c, 0u).x);
       const bool acc = isfinite(ratio) && log(uu) < ratio;
@@ -172,18 +178,18 @@ __global__ void __launch_bounds__(256) klqp_kernel(KlqpArgs a) {
   __shared__ double part[8][2 * kMaxK + 1];
   const int K = a.m.K, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t iter = (uint32_t)a.state->t;
-  double g[kMaxK], e[kMaxK];
+  float g[kMaxK], e[kMaxK];
   double f = 0.0;
-  for (int j = 0; j < K; ++j) g[j] = e[j] = 0.0;
+  for (int j = 0; j < K; ++j) g[j] = e[j] = 0.0f;
   if (tid < a.S) {
-    double u[kMaxK];
+    float u[kMaxK];
     double lq = 0.0;
     for (int j = 0; j < K; ++j) {
-      e[j] = a.eps_ovr ? (double)a.eps_ovr[tid * K + j]
-                       : (double)philox_normal(a.seed, 0u, iter, (uint32_t)tid, (uint32_t)j);
-      const double sg = softplus_d((double)a.rho[j]);
-      u[j] = (double)a.mu[j] + sg * e[j];
-      lq += -0.5 * e[j] * e[j] - log(sg) - kHalfLog2Pi;
+      e[j] = a.eps_ovr ? a.eps_ovr[tid * K + j]
+                       : philox_normal(a.seed, 0u, iter, (uint32_t)tid, (uint32_t)j);
+      const float sg = softplus_f(a.rho[j]);
+      u[j] = fmaf(sg, e[j], a.mu[j]);
+      lq += (double)(-0.5f * e[j] * e[j] - logf(sg)) - kHalfLog2Pi;
     }
     f = log_joint_grad(a.m, u, g) - lq;
   }
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__(256) klqp_kernel(KlqpArgs a) {
   f = wsum(f);
   if (lane == 0) part[warp][2 * kMaxK] = f;
   for (int j = 0; j < K; ++j) {
-    const double a1 = wsum(g[j]), a2 = wsum(g[j] * e[j]);
+    const double a1 = wsum((double)g[j]), a2 = wsum((double)(g[j] * e[j]));
     if (lane == 0) {
       part[warp][j] = a1;
       part[warp][kMaxK + j] = a2;
@@ -214,9 +220,9 @@ __global__ void __launch_bounds__(256) klqp_kernel(KlqpArgs a) {
       s1 += part[w][j];
       s2 += part[w][kMaxK + j];
     }
-    const double sg = softplus_d((double)a.rho[j]);
+    const float sg = softplus_f(a.rho[j]);
     const float gmu = (float)(-s1 * invS);
-    const float grho = (float)((-s2 * invS - 1.0 / sg) * sigmoid_d((double)a.rho[j]));
+    const float grho = ((float)(-s2 * invS) - 1.0f / sg) * sigmoid_f(a.rho[j]);
     if (a.grad_out) {
       a.grad_out[j] = gmu;
       a.grad_out[K + j] = grho;
@@ -254,9 +260,9 @@ static int check_model(const edg_expfam_t* m) {
 using namespace edg;
 
 extern "C" int edg_expfam_hmc_run(const edg_expfam_t* model, const edg_hmc_t* cfg, int32_t C,
-                                  int32_t n_iter, double* u, double* grad, double* lj,
+                                  int32_t n_iter, float* u, float* grad, double* lj,
                                   int32_t cache_valid, int32_t* n_accept, edg_state_t* state,
-                                  double* samples, int64_t T_cap, const double* r_override,
+                                  float* samples, int64_t T_cap, const float* r_override,
                                   const double* u_override, void* stream) {
   int rc = ef::check_model(model);
   if (rc) return rc;

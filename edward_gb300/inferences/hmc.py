@@ -215,9 +215,9 @@ class HMC(MonteCarlo):
         return autotune.choose("hmc_hier", key, [0, 1], run)
 
     def _build_expfam(self):
-        """Chains of the unconstrained latent u (FP64); the Empirical shows the
-        constrained values (``inference.py:247-253``) while ``params_var``
-        holds u."""
+        """Chains of the unconstrained latent u (FP32, as the reference's
+        chains); the Empirical shows the constrained values
+        (``inference.py:247-253``) while ``params_var`` holds u."""
         spec = self._spec
         dev = self._device
         C = self.n_chains or 1
@@ -229,11 +229,11 @@ class HMC(MonteCarlo):
         m.family, m.K = spec.family, K
         m.prior, m.stats = self._ef_prior.data_ptr(), self._ef_stats.data_ptr()
         self._ef = m
-        self._samples = torch.zeros(T, C, K, dtype=torch.float64, device=dev)
+        self._samples = torch.zeros(T, C, K, dtype=torch.float32, device=dev)
         qz = self.latent_vars[spec.z]
         init = qz.params_var.value
         if init[0].numel() == C * K:
-            self._samples[0] = init[0].to(dev, torch.float64).reshape(C, K)
+            self._samples[0] = init[0].to(dev, torch.float32).reshape(C, K)
         lead = (T, C) if self.n_chains else (T,)
         shape = lead + ((K,) if spec.family == _lib.EXPFAM_DIRICHLET else ())
         qz.params_var._value = self._samples.view(shape)
@@ -262,6 +262,10 @@ class HMC(MonteCarlo):
 
     def _launch(self, n_iter, r_override=None, u_override=None, ratio_out=None):
         if self.engine == "expfam":
+            if r_override is not None:
+                r_override = r_override.to(torch.float32).contiguous()
+            if u_override is not None:
+                u_override = u_override.to(torch.float64).contiguous()
             _lib.call("edg_expfam_hmc_run", ctypes.byref(self._ef), ctypes.byref(self._cfg),
                       self.C, int(n_iter), _lib.ptr(self._z), _lib.ptr(self._g),
                       _lib.ptr(self._lj), self._cache_valid, _lib.ptr(self._n_accept),
