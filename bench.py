@@ -1051,7 +1051,7 @@ def run_hier(args):
         ms = timed(graph.replay, args.steps)
     work = float((hd.Ns.astype(np.int64) * hd.Ds).sum())
     flops = 4.0 * work * C * L
-    peak, src = _peak_3xtf32()
+    peak, src = tensor_peak(measure_tf32_peak(torch.device("cuda")))
     ach = flops / (ms / 1e3) / 1e12
     line = {"metric": "HMC leapfrog chain-steps/s (2048 ragged hierarchical logistic regressions)",
             "value": n * L / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -1167,7 +1167,7 @@ def run_bnn(args):
     P = inf._spec.P
     fwd = 2.0 * (D * H1 + H1 * H2 + H2) * M * S
     flops = 3.0 * fwd
-    peak, src = _peak_3xtf32()
+    peak, src = tensor_peak(measure_tf32_peak(torch.device("cuda")))
     ach = flops / (ms / 1e3) / 1e12
     act_bytes = 4.0 * S * M * (H1 + H2)
     line = {"metric": "KLqp ELBO-grad evals/s (Bayesian NN 32-256-256-1, S=64, M=4096)",
@@ -1248,7 +1248,7 @@ def run_sbn(args):
     R = S * B
     flops = 4.0 * R * ((H0 + 1) * H1 + (H1 + 1) * H0 + (H0 + 1) * V) + \
         4.0 * B * (V + 1) * (H0 + BH)
-    peak, src = _peak_3xtf32()
+    peak, src = tensor_peak(measure_tf32_peak(torch.device("cuda")))
     ach = flops / (ms / 1e3) / 1e12
     nq = (V + 1) * H0 + (H0 + 1) * H1
 
