@@ -947,16 +947,51 @@ def read_traffic(engine):
     return read_traffic_file(name)
 
 
-def read_traffic_file(name):
+def read_traffic_file(name, key="dram_bytes_per_launch"):
+    """The integer after '<key>:' in a committed ncu summary under profiles/, else None."""
     p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_launch:"):
+                if line.startswith(key + ":"):
                     return int(float(line.split(":", 1)[1]))
     except OSError:
         pass
     return None
+
+
+def graph_of(fn):
+    """fn captured into a CUDA graph (run once first, outside the capture)."""
+    import torch
+    fn()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            fn()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    return g
+
+
+def flush_timed(fn, k, dev):
+    """Mean device time in ms of k calls of fn, each preceded by a 256 MB write
+    that flushes L2; CUDA events on the launching stream bracket fn only."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(k)]
+    torch.cuda.synchronize()
+    for i in range(k):
+        flush.fill_(float(i))
+        ev[i][0].record(st)
+        fn()
+        ev[i][1].record(st)
+    torch.cuda.synchronize()
+    del flush
+    return sum(a.elapsed_time(b) for a, b in ev) / k
 
 
 # ------------------------------------------------------------------ secondary workloads
@@ -1053,7 +1088,7 @@ def run_hier(args):
     flops = 4.0 * work * C * L
     peak, src = tensor_peak(measure_tf32_peak(torch.device("cuda")))
     ach = flops / (ms / 1e3) / 1e12
-    line = {"metric": "HMC leapfrog chain-steps/s (2048 ragged hierarchical logistic regressions)",
+    line = {"metric": "HMC leapfrog chain-steps/s (%d ragged hierarchical logistic regressions)" % hd.I,
             "value": n * L / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -1064,7 +1099,10 @@ def run_hier(args):
             "launch_forms_ms_per_step": forms,
             "gpu_launches": args.steps,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                         "frac": ach / peak, "traffic": None, "kernel": "hmc_hier_kernel<32> (SIMT FP32)",
+                         "frac": ach / peak,
+                         "traffic": read_traffic_file("hmc_hier_kernel_ragged_I2048.txt")
+                         if hd.I == 2048 else None,
+                         "kernel": "hmc_hier_kernel<32> (SIMT FP32)",
                          "peak_source": src, "algorithmic_flops_per_launch": flops,
                          "x_stream_GBs": 2 * L * work * 4 / (ms / 1e3) / 1e9},
             "accept_rate": float(nacc.sum().item()) / (n * (2 * args.warmup + 3 * args.steps + 1)),
@@ -1085,25 +1123,29 @@ def run_klqp(args):
     b = Normal(loc=0.0, scale=1.0)
     yv = Bernoulli(logits=ed.dot(X, w) + b)
     inf = ed.KLqp([w, b], data={yv: y})
-    inf.initialize(n_samples=5, n_iter=1000, n_print=0)
-    inf.steps(50)
+    inf.initialize(n_samples=5, n_iter=100000, n_print=0)
+    for _ in range(max(args.warmup, 3)):
+        inf._step(apply=True)
+    K = args.steps
+    ms = flush_timed(lambda: inf._step(apply=True), K, torch.device("cuda"))
+    # the same steps back to back from a CUDA graph (X stays L2-resident)
     inf.steps(50)
     torch.cuda.synchronize()
-    K = max(args.steps, 100) // 50 * 50
     a, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record()
-    for _ in range(K // 50):
+    for _ in range(4):
         inf.steps(50)
     b2.record()
     b2.synchronize()
-    ms = a.elapsed_time(b2) / K
+    ms_graph = a.elapsed_time(b2) / 200
     st = inf._read_state()
     line = {"metric": "KLqp ELBO-grad evals/s (Bayesian logistic regression, S=5)",
             "value": 1e3 / ms, "unit": "evals/s", "n_gpus": 1, "steps": K,
-            "warmup": 100, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "klqp_logreg_N10000_D50_S5", "launch": "CUDA graph of 50 fused steps",
-                       "l2_flush": "none (X is 2 MB, L2-resident by design; latency-bound)"},
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "klqp_logreg_N10000_D50_S5", "launch": "one fused launch per step",
+                       "l2_flush": "256 MB write before each timed step, outside the events"},
+            "value_graph_l2_resident": 1e3 / ms_graph,
             "gpu_launches": K, "final_loss": float(st.loss), "t": int(st.t)}
     print(json.dumps(line), flush=True)
     return 0
@@ -1180,7 +1222,9 @@ def run_bnn(args):
                                    % (act_bytes / 1e6)},
             "gpu_launches": K * 14,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                         "frac": ach / peak, "traffic": None,
+                         "frac": ach / peak,
+                         "traffic": read_traffic_file("gemm_tc_kernel_bnn_S64_M4096.txt",
+                                                      "dram_bytes_per_step"),
                          "kernel": "whole step (tcgen05 3xTF32 GEMMs + fused head/adjoint + finalize)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
             "final_loss": float(st.loss), "t": int(st.t), "clocks": clk.summary(),
@@ -1236,15 +1280,12 @@ def run_sbn(args):
     for _ in range(max(1, args.warmup // chunk + 1)):
         inf.steps(chunk)
     torch.cuda.synchronize()
-    K = max(args.steps // chunk, 1) * chunk
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    K = args.steps
+    # one step per CUDA graph replay, L2 flushed before each (the step's own
+    # buffers, 117 MB, would otherwise stay in the 129 MB L2)
+    one = graph_of(lambda: inf._step(apply=True))
     with ClockSampler(0) as clk:
-        a.record()
-        for _ in range(K // chunk):
-            inf.steps(chunk)
-        b.record()
-        b.synchronize()
-    ms = a.elapsed_time(b) / K
+        ms = flush_timed(one.replay, K, torch.device("cuda"))
     R = S * B
     flops = 4.0 * R * ((H0 + 1) * H1 + (H1 + 1) * H0 + (H0 + 1) * V) + \
         4.0 * B * (V + 1) * (H0 + BH)
@@ -1344,13 +1385,14 @@ def run_sbn(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "sbn_score_V784_H200_H200_S16_B1024_mlp100",
                        "params": inf._P, "baseline_params": int(inf._bparams.numel()),
-                       "launch": f"CUDA graph of {chunk} steps",
-                       "l2_flush": "inputs larger than L2 (sample-row buffers %.0f MB per step)"
-                                   % (4.0 * R * (V + 3 * H0 + 2 * H1) / 1e6)},
+                       "launch": "one CUDA graph replay per step",
+                       "l2_flush": "256 MB write before each timed step, outside the events"},
             "gpu_launches": K * (1 + launches),
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                         "frac": ach / peak, "traffic": None,
-                         "kernel": "whole step (SIMT bgemm + row kernels + baseline)",
+                         "frac": ach / peak,
+                         "traffic": read_traffic_file("sbn_score_step_B1024_S16.txt",
+                                                      "dram_bytes_per_step"),
+                         "kernel": "whole step (tcgen05 3xTF32 GEMMs, row kernels, baseline MLP)",
                          "peak_source": src, "algorithmic_flops_per_step": flops},
             "q_grad_variance": gvar, "learned_baseline_gain": baseline_gain,
             "target": target, "cpu_baseline": cb,
@@ -1378,13 +1420,8 @@ def run_sgld(args):
     inf.initialize(step_size=1e-4, n_print=0)
     inf.run_iterations(args.warmup)
     torch.cuda.synchronize()
-    a, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
-        a.record()
-        inf.run_iterations(args.steps)
-        b2.record()
-        b2.synchronize()
-    ms = a.elapsed_time(b2) / args.steps
+        ms = flush_timed(lambda: inf.run_iterations(1), args.steps, torch.device("cuda"))
     P = N_FEAT + 1
     flops = 4.0 * N_ROWS * P * C
     line = {"metric": "SGLD chain-iterations/s (Bayesian logistic regression, batched chains)",
@@ -1393,7 +1430,7 @@ def run_sgld(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "sgld_logreg_N10000_D50_C4096", "chains": C,
-                       "l2_flush": "none (X is 2 MB, L2-resident)"},
+                       "l2_flush": "256 MB write before each timed iteration, outside the events"},
             "gpu_launches": 2 * args.steps,
             "roofline": {"bound": "fp32", "achieved": flops / (ms / 1e3) / 1e12,
                          "unit": "TFLOP/s", "traffic": None, "peak": None,

@@ -83,6 +83,7 @@ __global__ void glm_reduce_kernel(GLMDev m, const float* __restrict__ Z, int B, 
 // ============================================================ KLqp step
 struct KlqpArgs {
   int method, S, Spad, nblocks, chunk;
+  double inv_S;  // 1 / S
   float dscale;
   const float* kl_scaling;
   const float* latent_scale;
@@ -111,16 +112,43 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
   float* sig = reinterpret_cast<float*>(rest);  // [PP]
   float* epsS = sig + m.PP;                      // [Spad][PP] this step's draws
+  // The step's per-coordinate inputs, loaded once by every block at the start
+  // (one round trip, overlapping the X tile's copy) so that the last block's
+  // serial tail reads only shared memory: mu, rho, prior loc and scale, KL and
+  // latent scalings, the model-parameter flags and the four optimizer slots.
+  float* s_mu = epsS + (size_t)a.Spad * m.PP;  // [PP]
+  float* s_rho = s_mu + m.PP;
+  float* s_pl = s_rho + m.PP;
+  float* s_ps = s_pl + m.PP;
+  float* s_ks = s_ps + m.PP;
+  float* s_ls = s_ks + m.PP;
+  float* s_sl = s_ls + m.PP;                                  // [4][PP]
+  int* s_pt = reinterpret_cast<int*>(s_sl + 4 * m.PP);        // [PP]
   __shared__ bool s_last;
   const int P = m.P, PP = m.PP;
-  const int64_t t = *(volatile int64_t*)&a.state->t;
-  const uint32_t iter = (uint32_t)t;
   const int rb = blockIdx.x * a.chunk, re = min(m.N, rb + a.chunk);
-  // the first X tile's copy overlaps the draws below
+  // the first X tile's copy overlaps the loads and draws below
   if (re > rb) issue_tile<CT>(m, S.Xs, S.ys, rb, re);
   cp_async_commit();
-  for (int d = threadIdx.x; d < PP; d += kThreads)
-    sig[d] = (d < P && !(a.point && a.point[d])) ? softplusf(a.rho[d]) : 0.0f;
+  const int64_t t = *(volatile int64_t*)&a.state->t;
+  const int64_t gstep = a.state->global_step;
+  const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
+  const uint32_t iter = (uint32_t)t;
+  for (int d = threadIdx.x; d < PP; d += kThreads) {
+    const bool ok = d < P;
+    const int pt = (ok && a.point) ? a.point[d] : 0;
+    const float rho = ok ? a.rho[d] : 0.0f;
+    s_mu[d] = ok ? a.mu[d] : 0.0f;
+    s_rho[d] = rho;
+    s_pl[d] = ok ? m.prior_loc[d] : 0.0f;
+    s_ps[d] = ok ? m.prior_scale[d] : 1.0f;
+    s_ks[d] = (ok && a.kl_scaling) ? a.kl_scaling[d] : 1.0f;
+    s_ls[d] = (ok && a.latent_scale) ? a.latent_scale[d] : 1.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s_sl[j * PP + d] = (ok && a.slots) ? a.slots[j * P + d] : 0.0f;
+    s_pt[d] = pt;
+    sig[d] = (ok && !pt) ? softplusf(rho) : 0.0f;
+  }
   init_x_pad<CT>(m, S);
   __syncthreads();
   // the score method needs d log p / d z only for model parameters
@@ -133,7 +161,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       if (s < a.S && d < P) {
         const float e = eps_value(a, iter, s, d, P);
         epsS[s * PP + d] = e;  // kept for the last block's gradient formula
-        zv = a.mu[d] + sig[d] * e;
+        zv = s_mu[d] + sig[d] * e;
       }
       S.Zt[d * CT + c] = zv;
     }
@@ -158,61 +186,49 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  // per-sample totals (FP64 log-lik; FP32 gradient, summed in block order).
-  // Partials are read from L2 (ld.global.cg) by every thread so the loads of
-  // different blocks are in flight together.
-  double* llS = S.llred;                 // [S]  (reuse; 2 S + 8 <= RT/2*CT)
+  // The tail: every partial load is issued first, the prior terms (KL or
+  // log p(z) - log q(z), which need no partial) are computed while they are
+  // in flight, then the partials are reduced in a fixed order (deterministic).
+  double* llS = S.llred;                 // [S]  (reuse; 2 S + 8 fit, checked at launch)
   double* lsig = llS + a.S;              // [S] log p(z_s) - log q(z_s)
   double* red = lsig + a.S;              // [8] per-warp partial sums
   float* gS = S.Xs;                      // [S][PP] gradient per sample
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // (eight interleaved accumulators per quantity, so that the loads of eight
-  // blocks are in flight together; fixed order, so the sums are deterministic)
-  for (int s = threadIdx.x; s < a.S; s += kThreads) {
-    const double* src = a.ws_ll + s;
-    const size_t st = (size_t)a.Spad;
-    double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    int b = 0;
-    for (; b + 8 <= a.nblocks; b += 8) {
+  constexpr int kBatch = 64;             // partials per thread in flight at once
+  // log-likelihood partials: one warp per sample, lanes over the blocks
+  double llv[2] = {0.0, 0.0};
+  const bool ll_fast = a.nblocks <= 64 && a.S <= kThreads / 32;
+  if (ll_fast && warp < a.S) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] += __ldcg(src + (b + k) * st);
+    for (int k = 0; k < 2; ++k) {
+      const int b = lane + 32 * k;
+      if (b < a.nblocks) llv[k] = __ldcg(a.ws_ll + (size_t)b * a.Spad + warp);
     }
-    for (; b < a.nblocks; ++b) v[0] += __ldcg(src + b * st);
-    llS[s] = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
   }
-  if (need_grad) {
-    // the S x P entries in use (one per thread for small problems; the padding
-    // columns are never read)
-    for (int q = threadIdx.x; q < a.S * P; q += kThreads) {
-      const int sq = q / P, dq = q - sq * P;
-      const float* src = a.ws_g + sq * PP + dq;
-      const size_t st = (size_t)a.Spad * PP;
-      float v[16];
+  // gradient partials: the S x P entries in use, one per thread for small
+  // problems (the padding columns are never read)
+  const int q0 = threadIdx.x;
+  float gv[kBatch];
+  const bool g_fast = need_grad && a.nblocks <= kBatch && a.S * P <= kThreads;
+  if (g_fast && q0 < a.S * P) {
+    const int sq = q0 / P, dq = q0 - sq * P;
+    const float* src = a.ws_g + sq * PP + dq;
+    const size_t st = (size_t)a.Spad * PP;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] = 0.0f;
-      int b = 0;
-      for (; b + 16 <= a.nblocks; b += 16) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) v[k] += __ldcg(src + (b + k) * st);
-      }
-      for (; b < a.nblocks; ++b) v[0] += __ldcg(src + b * st);
-#pragma unroll
-      for (int k = 1; k < 16; ++k) v[0] += v[k];
-      gS[sq * PP + dq] = v[0];
-    }
+    for (int k = 0; k < kBatch; ++k) gv[k] = k < a.nblocks ? __ldcg(src + (size_t)k * st) : 0.0f;
   }
   // score / reparam: per-sample log p(z_s) - log q(z_s), one warp per sample
   if (a.method != EDG_KLQP_REPARAM_KL) {
     for (int s = warp; s < a.S; s += kThreads / 32) {
       double acc = 0.0;
       for (int d = lane; d < P; d += 32) {
-        if (a.point && a.point[d]) continue;
-        const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
+        if (s_pt[d]) continue;
+        const float lsc = s_ls[d];
         const float e = epsS[s * PP + d];
-        const float zv = a.mu[d] + sig[d] * e;
-        const float ps = m.prior_scale[d];
-        const float zp = (zv - m.prior_loc[d]) / ps;
-        const float zq = (zv - a.mu[d]) / sig[d];
+        const float zv = s_mu[d] + sig[d] * e;
+        const float ps = s_ps[d];
+        const float zp = (zv - s_pl[d]) / ps;
+        const float zq = (zv - s_mu[d]) / sig[d];
         const float lp = -0.5f * zp * zp - logf(ps);
         const float lq = -0.5f * zq * zq - logf(sig[d]);
         acc += (double)(lsc * (lp - lq));  // the 0.5 log 2pi terms cancel
@@ -227,23 +243,75 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   if (a.method == EDG_KLQP_REPARAM_KL) {
     double kl = 0.0;
     for (int d = threadIdx.x; d < P; d += kThreads) {
-      if (a.point && a.point[d]) continue;
-      const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
-      const float sp = m.prior_scale[d], sq = sig[d];
-      const float dm = (a.mu[d] - m.prior_loc[d]) / sp;
+      if (s_pt[d]) continue;
+      const float ks = s_ks[d];
+      const float sp = s_ps[d], sq = sig[d];
+      const float dm = (s_mu[d] - s_pl[d]) / sp;
       const float ratio = (sq / sp) * (sq / sp);
-      kl += (double)ks * (0.5 * (double)dm * dm + 0.5 * ((double)ratio - 1.0 - (double)logf(ratio)));
+      // FP32 per coordinate (FP64 runs at a small fraction of the FP32 rate
+      // here), summed in FP64
+      kl += (double)(ks * (0.5f * dm * dm + 0.5f * ((ratio - 1.0f) - logf(ratio))));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) kl += __shfl_xor_sync(0xffffffffu, kl, o);
     if (lane == 0) red[warp] = kl;
   }
+  // reduce the partials
+  if (ll_fast) {
+    if (warp < a.S) {
+      double v = llv[0] + llv[1];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) llS[warp] = v;
+    }
+  } else {
+    for (int s = warp; s < a.S; s += kThreads / 32) {
+      double v = 0.0;
+      for (int b = lane; b < a.nblocks; b += 32) v += __ldcg(a.ws_ll + (size_t)b * a.Spad + s);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) llS[s] = v;
+    }
+  }
+  if (g_fast) {
+    if (q0 < a.S * P) {
+#pragma unroll
+      for (int w = kBatch / 2; w > 0; w >>= 1) {
+#pragma unroll
+        for (int k = 0; k < w; ++k) gv[k] += gv[k + w];
+      }
+      const int sq = q0 / P, dq = q0 - sq * P;
+      gS[sq * PP + dq] = gv[0];
+    }
+  } else if (need_grad) {
+    for (int q = threadIdx.x; q < a.S * P; q += kThreads) {
+      const int sq = q / P, dq = q - sq * P;
+      const float* src = a.ws_g + sq * PP + dq;
+      const size_t st = (size_t)a.Spad * PP;
+      float acc = 0.0f;
+      for (int b0 = 0; b0 < a.nblocks; b0 += kBatch) {
+        float v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k)
+          v[k] = b0 + k < a.nblocks ? __ldcg(src + (size_t)(b0 + k) * st) : 0.0f;
+#pragma unroll
+        for (int w = kBatch / 2; w > 0; w >>= 1) {
+#pragma unroll
+          for (int k = 0; k < w; ++k) v[k] += v[k + w];
+        }
+        acc += v[0];
+      }
+      gS[sq * PP + dq] = acc;
+    }
+  }
   __syncthreads();
-  // ---- loss
-  if (threadIdx.x == 0) {
+  // ---- loss, on the block's last thread (the gradient loop below starts at
+  // thread 0, so both run at once for P < 255)
+  constexpr int kLossThread = kThreads - 1;
+  if (threadIdx.x == kLossThread) {
     double mean_ll = 0.0;
     for (int s = 0; s < a.S; ++s) mean_ll += llS[s];
-    mean_ll /= a.S;
+    mean_ll *= a.inv_S;
     double loss;
     if (a.method == EDG_KLQP_REPARAM_KL) {
       for (int w = 0; w < kThreads / 32; ++w) klsum += red[w];
@@ -253,7 +321,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     } else {
       double ms = 0.0;
       for (int s = 0; s < a.S; ++s) ms += lsig[s];
-      ms /= a.S;
+      ms *= a.inv_S;
       loss = -(mean_ll + ms);
       a.state->aux[0] = mean_ll;
       a.state->aux[1] = ms;
@@ -261,17 +329,17 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     a.state->loss = loss;
     if (!isfinite(loss)) atomicAdd(&a.state->nonfinite, 1u);
   }
-  __syncthreads();  // the loss reads mu/rho before the apply below overwrites them
-  // ---- gradients w.r.t. (mu, rho) and the optimizer apply
-  const float lr = opt_lr(a.opt, a.state->global_step);
-  const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
+  // ---- gradients w.r.t. (mu, rho) and the optimizer apply (they read the
+  // shared-memory copies of mu, rho and the slots, so they need not wait for
+  // the loss above)
+  const float lr = opt_lr(a.opt, gstep);
   const float invS = 1.0f / (float)a.S;
   for (int d = threadIdx.x; d < P; d += kThreads) {
-    const float mu = a.mu[d], rho = a.rho[d], sg = sig[d];
-    const float ps = m.prior_scale[d], pl = m.prior_loc[d];
-    const float lsc = a.latent_scale ? a.latent_scale[d] : 1.0f;
+    const float mu = s_mu[d], rho = s_rho[d], sg = sig[d];
+    const float ps = s_ps[d], pl = s_pl[d];
+    const float lsc = s_ls[d];
     float gmu = 0.0f, gsig = 0.0f;
-    const bool point = a.point && a.point[d];
+    const bool point = s_pt[d] != 0;
     if (point) {
       // model parameter: d loss / d theta = -mean_s d log p(x | z_s) / d theta
       float sg_mu = 0.0f;
@@ -285,7 +353,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
         sg_mu += g;
         sg_sig += g * e;
       }
-      const float ks = a.kl_scaling ? a.kl_scaling[d] : 1.0f;
+      const float ks = s_ks[d];
       gmu = -sg_mu * invS + ks * (mu - pl) / (ps * ps);
       gsig = -sg_sig * invS + ks * (sg / (ps * ps) - 1.0f / sg);
     } else if (a.method == EDG_KLQP_REPARAM) {
@@ -320,22 +388,29 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       a.grad_out[P + d] = grho;
     }
     if (a.apply) {
+      // slots [4][P]: mu's first, rho's first, mu's second, rho's second
       const int n = 2 * P;
-      a.mu[d] = opt_apply(a.opt, mu, gmu, a.slots + d, a.slots + n + d, lr, b1p, b2p);
-      if (!point)
-        a.rho[d] = opt_apply(a.opt, rho, grho, a.slots + P + d, a.slots + n + P + d, lr, b1p, b2p);
+      float m0 = s_sl[d], r0 = s_sl[PP + d], m1 = s_sl[2 * PP + d], r1 = s_sl[3 * PP + d];
+      a.mu[d] = opt_apply(a.opt, mu, gmu, &m0, &m1, lr, b1p, b2p);
+      a.slots[d] = m0;
+      a.slots[n + d] = m1;
+      if (!point) {
+        a.rho[d] = opt_apply(a.opt, rho, grho, &r0, &r1, lr, b1p, b2p);
+        a.slots[P + d] = r0;
+        a.slots[n + P + d] = r1;
+      }
     }
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  // the step counters (no other block reads them any more; the kernel's end
+  // orders these writes before the next step's launch)
+  if (threadIdx.x == kLossThread) {
     if (a.apply) {
       a.state->t = t + 1;
-      a.state->global_step += 1;
+      a.state->global_step = gstep + 1;
       a.state->beta1_power = b1p * a.opt.beta1;
       a.state->beta2_power = b2p * a.opt.beta2;
     }
     a.state->done = 0;
-    __threadfence();
   }
 }
 
@@ -388,7 +463,7 @@ __host__ __device__ constexpr size_t hmc_smem_bytes(int PP) {
 }
 
 template <int CT>
-__global__ void __launch_bounds__(kThreads) hmc_glm_kernel(GLMDev m, HmcArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) hmc_glm_kernel(GLMDev m, HmcArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   GradSmem S;
   unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
@@ -675,8 +750,10 @@ extern "C" size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg
 
 template <int CT>
 static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
-  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4 + (size_t)a.Spad * m.PP * 4;
+  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4 + (size_t)a.Spad * m.PP * 4 +
+                    (size_t)11 * m.PP * 4;
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED, "P=%d too large for KLqp kernel", m.P);
+  // the tail's per-sample sums and per-warp partials reuse the log-lik partials
   EDG_REQUIRE(a.S * 2 + 8 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
   EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,
               "n_samples too large");
@@ -710,6 +787,7 @@ extern "C" int edg_klqp_glm_step(const edg_glm_t* model, const edg_klqp_t* cfg,
   KlqpArgs a;
   a.method = cfg->method;
   a.S = cfg->n_samples;
+  a.inv_S = 1.0 / cfg->n_samples;
   a.Spad = p.Spad;
   a.nblocks = p.nblocks;
   a.chunk = p.chunk;
