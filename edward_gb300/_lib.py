@@ -89,7 +89,8 @@ class EdgMH(ctypes.Structure):
 
 
 class EdgExpFam(ctypes.Structure):
-    _fields_ = [("family", c_int32), ("K", c_int32), ("prior", c_void_p), ("stats", c_void_p)]
+    _fields_ = [("family", c_int32), ("K", c_int32), ("prior", c_void_p), ("stats", c_void_p),
+                ("transform", c_int32)]
 
 
 class EdgHMC(ctypes.Structure):

@@ -551,24 +551,31 @@ def compile_expfam(latents, data):
     from scipy.special import gammaln
     from .models import Beta, Categorical, Dirichlet, Gamma, Poisson
     observed, bindings = _split_data(data)
-    if len(latents) != 1 or len(observed) != 1:
-        raise UnsupportedModel("the constrained-latent family has one latent and one observed "
-                               "variable")
+    if len(latents) != 1 or len(observed) > 1:
+        raise UnsupportedModel("the constrained-latent family has one latent and at most one "
+                               "observed variable")
     z = latents[0]
-    (x, xval), = observed.items()
-    if isinstance(xval, (RandomVariable, Node)):
-        xval = const_value(xval, bindings) if isinstance(xval, Node) else None
-        if xval is None:
-            raise UnsupportedModel("observed values must be bound to an array")
-    xv = np.asarray(xval)
-    if isinstance(z, Beta) and isinstance(x, Bernoulli) and x.probs is z:
+    if observed:
+        (x, xval), = observed.items()
+        if isinstance(xval, (RandomVariable, Node)):
+            xval = const_value(xval, bindings) if isinstance(xval, Node) else None
+            if xval is None:
+                raise UnsupportedModel("observed values must be bound to an array")
+        xv = np.asarray(xval)
+    else:
+        # the latent alone (its prior is the target): no observations
+        x, xv = None, np.zeros(0)
+        if not isinstance(z, (Beta, Gamma, Dirichlet)):
+            raise UnsupportedModel("not a Beta, Gamma or Dirichlet latent")
+    none = x is None
+    if isinstance(z, Beta) and (none or (isinstance(x, Bernoulli) and x.probs is z)):
         if np.any((xv != 0) & (xv != 1)):
             raise ValueError("Bernoulli observations must be 0 or 1")
         a = _const_param(z.concentration1, "Beta concentration1", bindings)
         b = _const_param(z.concentration0, "Beta concentration0", bindings)
         n1 = float((xv == 1).sum())
         fam, K, prior, stats = 0, 1, [float(a), float(b)], [n1, float(xv.size) - n1]
-    elif isinstance(z, Gamma) and isinstance(x, Poisson) and x.rate is z:
+    elif isinstance(z, Gamma) and (none or (isinstance(x, Poisson) and x.rate is z)):
         if np.any(xv < 0) or np.any(xv != np.round(xv)):
             raise ValueError("Poisson observations must be non-negative integers")
         a = _const_param(z.concentration, "Gamma concentration", bindings)
@@ -576,7 +583,7 @@ def compile_expfam(latents, data):
         fam, K = 1, 1
         prior = [float(a), float(r)]
         stats = [float(xv.sum()), float(xv.size), float(gammaln(xv.astype(np.float64) + 1).sum())]
-    elif isinstance(z, Dirichlet) and isinstance(x, Categorical) and x.probs is z:
+    elif isinstance(z, Dirichlet) and (none or (isinstance(x, Categorical) and x.probs is z)):
         alpha = _const_param(z.concentration, "Dirichlet concentration", bindings).reshape(-1)
         Kc = alpha.size
         if Kc < 2 or Kc > 33:

@@ -41,6 +41,25 @@ __device__ __forceinline__ float sigmoid_f(float x) {
 __device__ double log_joint_grad(const edg_expfam_t& m, const float* u, float* g) {
   const double* pr = m.prior;
   const double* st = m.stats;
+  if (!m.transform) {
+    // on the support itself (Beta: (0, 1), Gamma: (0, inf)); NaN outside it,
+    // for the log density and its gradient alike
+    const float z = u[0];
+    const bool in = m.family == EDG_EXPFAM_BETA ? (z > 0.0f && z < 1.0f) : z > 0.0f;
+    if (!in) {
+      g[0] = __int_as_float(0x7fc00000);
+      return __longlong_as_double(0x7ff8000000000000ll);
+    }
+    if (m.family == EDG_EXPFAM_BETA) {
+      const float a1 = (float)pr[0] - 1.0f + (float)st[0], b1 = (float)pr[1] - 1.0f + (float)st[1];
+      g[0] = a1 / z - b1 / (1.0f - z);
+      return (double)(a1 * logf(z)) + (double)(b1 * log1pf(-z)) -
+             (lgamma(pr[0]) + lgamma(pr[1]) - lgamma(pr[0] + pr[1]));
+    }
+    const float a1 = (float)pr[0] - 1.0f + (float)st[0], rn = (float)pr[1] + (float)st[1];
+    g[0] = a1 / z - rn;
+    return pr[0] * log(pr[1]) - lgamma(pr[0]) + (double)(a1 * logf(z)) - (double)(rn * z) - st[2];
+  }
   if (m.family == EDG_EXPFAM_BETA) {
     const float a = (float)pr[0], b = (float)pr[1], n1 = (float)st[0], n0 = (float)st[1];
     const float lz = -softplus_f(-u[0]), l1z = -softplus_f(u[0]);
@@ -251,6 +270,9 @@ static int check_model(const edg_expfam_t* m) {
               EDG_E_VALUE, "unknown family %d", m->family);
   EDG_REQUIRE(m->family == EDG_EXPFAM_DIRICHLET ? (m->K >= 1 && m->K <= kMaxK) : m->K == 1,
               EDG_E_SHAPE, "unconstrained dimension %d not supported", m->K);
+  EDG_REQUIRE(m->transform == 0 || m->transform == 1, EDG_E_VALUE, "transform must be 0 or 1");
+  EDG_REQUIRE(m->transform || m->family != EDG_EXPFAM_DIRICHLET, EDG_E_UNSUPPORTED,
+              "the Dirichlet latent is worked in the unconstrained space only");
   return EDG_OK;
 }
 
@@ -266,6 +288,8 @@ extern "C" int edg_expfam_hmc_run(const edg_expfam_t* model, const edg_hmc_t* cf
                                   const double* u_override, void* stream) {
   int rc = ef::check_model(model);
   if (rc) return rc;
+  EDG_REQUIRE(model->transform == 1, EDG_E_UNSUPPORTED,
+              "HMC samples the constrained latent in its unconstrained space (transform = 1)");
   EDG_REQUIRE(cfg && u && grad && lj && n_accept && state, EDG_E_NULL,
               "pointers must not be NULL");
   EDG_REQUIRE(C > 0 && n_iter >= 0 && cfg->n_steps >= 0, EDG_E_SHAPE, "invalid sizes");

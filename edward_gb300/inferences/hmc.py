@@ -228,6 +228,7 @@ class HMC(MonteCarlo):
         m = _lib.EdgExpFam()
         m.family, m.K = spec.family, K
         m.prior, m.stats = self._ef_prior.data_ptr(), self._ef_stats.data_ptr()
+        m.transform = 1
         self._ef = m
         self._samples = torch.zeros(T, C, K, dtype=torch.float32, device=dev)
         qz = self.latent_vars[spec.z]

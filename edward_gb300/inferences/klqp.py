@@ -118,9 +118,8 @@ class KLqp(VariationalInference):
                 if self._method_id not in (REPARAM,):
                     raise NotImplementedError("the constrained-latent family takes the "
                                               "reparameterisation gradient with Monte Carlo KL")
-                if not self.auto_transform:
-                    raise NotImplementedError("the constrained-latent family needs "
-                                              "auto_transform=True")
+                if not self.auto_transform and self._spec.family == _lib.EXPFAM_DIRICHLET:
+                    raise NotImplementedError("the Dirichlet latent needs auto_transform=True")
                 for blk in self._spec.blocks:
                     parse_normal_q(self.latent_vars[blk.rv])
                 return
@@ -250,6 +249,9 @@ class KLqp(VariationalInference):
         m = _lib.EdgExpFam()
         m.family, m.K = spec.family, K
         m.prior, m.stats = self._ef_prior.data_ptr(), self._ef_stats.data_ptr()
+        # auto_transform=False: q is fitted on the latent's support itself, and
+        # draws outside it give a NaN loss (inference_auto_transform_test.py:46-63)
+        m.transform = 1 if self.auto_transform else 0
         self._ef = m
         self._ef_seed = next_seed()
         self._slots = torch.zeros(4 * K, dtype=torch.float32, device=dev)
@@ -257,7 +259,9 @@ class KLqp(VariationalInference):
         self._opt = self.optimizer.to_c()
         self._grad = torch.zeros(2 * K, dtype=torch.float32, device=dev)
         z = spec.z
-        if spec.family == _lib.EXPFAM_BETA:
+        if not self.auto_transform:
+            self.transformations = {}
+        elif spec.family == _lib.EXPFAM_BETA:
             self.transformations = {z: torch.sigmoid}
         elif spec.family == _lib.EXPFAM_GAMMA:
             self.transformations = {z: torch.nn.functional.softplus}

@@ -404,6 +404,10 @@ typedef struct {
   int32_t K;            /* unconstrained dimension: 1, or categories - 1 (<= 32) */
   const double* prior;  /* device: (a, b) | (a, rate) | alpha[K + 1] */
   const double* stats;  /* device: (n1, n0) | (sum x, N, sum log x!) | counts[K + 1] */
+  int32_t transform;    /* 1: the latent is worked in the unconstrained space above;
+                         * 0: on its support itself (KLqp with auto_transform=False; Beta
+                         * and Gamma only): z = u, no Jacobian, and log p(x, z) and its
+                         * gradient are NaN where u is outside the support */
 } edg_expfam_t;
 /* HMC over C chains (FP32 state u [C, K] and gradient cache, FP64 log joint
  * cache lj [C]; the reference's leapfrog and Metropolis test, with the log

@@ -37,6 +37,43 @@ def constrain(family, U):
     return e / e.sum(axis=-1, keepdims=True)
 
 
+def log_joint_support(family, prior, stats, Z):
+    """log p(x, z) on the support itself (no bijector, ``auto_transform=False``;
+    Beta and Gamma): NaN where z is outside the support, as the reference's
+    densities give for such draws (``inference_auto_transform_test.py:46-63``)."""
+    z = np.asarray(Z, np.float64)[..., 0]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        if family == BETA:
+            a, b = prior
+            n1, n0 = stats
+            inside = (z > 0) & (z < 1)
+            lp = (a - 1 + n1) * np.log(z) + (b - 1 + n0) * np.log1p(-z) - \
+                (gammaln(a) + gammaln(b) - gammaln(a + b))
+        else:
+            a, rate = prior
+            sx, n, slf = stats
+            inside = z > 0
+            lp = a * np.log(rate) - gammaln(a) + (a - 1 + sx) * np.log(z) - (rate + n) * z - slf
+    return np.where(inside, lp, np.nan)
+
+
+def grad_log_joint_support(family, prior, stats, Z):
+    """d log_joint_support / d z (NaN outside the support), same shape as Z."""
+    Z = np.asarray(Z, np.float64)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        if family == BETA:
+            a, b = prior
+            n1, n0 = stats
+            g = (a - 1 + n1) / Z - (b - 1 + n0) / (1 - Z)
+            inside = (Z > 0) & (Z < 1)
+        else:
+            a, rate = prior
+            sx, n, _ = stats
+            g = (a - 1 + sx) / Z - rate - n
+            inside = Z > 0
+    return np.where(inside, g, np.nan)
+
+
 def log_joint(family, prior, stats, U):
     """log p(x, z(u)) + log|det dz/du| for U [..., K'] (K' = 1, or K - 1)."""
     U = np.asarray(U, np.float64)
@@ -96,17 +133,18 @@ def sufficient_stats(family, x, K=None):
     return np.bincount(x.astype(np.int64).reshape(-1), minlength=K).astype(np.float64)
 
 
-def klqp_loss_and_grads(family, prior, stats, mu, rho, eps):
+def klqp_loss_and_grads(family, prior, stats, mu, rho, eps, transform=True):
     """-ELBO of q(u) = N(mu, softplus(rho)) with Monte Carlo KL
-    (``klqp.py:642-704``) and its gradient w.r.t. (mu, rho), for draws eps [S, K]."""
+    (``klqp.py:642-704``) and its gradient w.r.t. (mu, rho), for draws eps [S, K];
+    transform=False: q is on the support itself (``log_joint_support``)."""
     mu = np.asarray(mu, np.float64)
     rho = np.asarray(rho, np.float64)
     eps = np.asarray(eps, np.float64)
     sig = dn.softplus(rho)
     U = mu[None] + sig[None] * eps
-    lj = log_joint(family, prior, stats, U)
+    lj = (log_joint if transform else log_joint_support)(family, prior, stats, U)
     lq = (-0.5 * eps ** 2 - np.log(sig)[None] - dn.HALF_LOG_2PI).sum(-1)
-    g = grad_log_joint(family, prior, stats, U)
+    g = (grad_log_joint if transform else grad_log_joint_support)(family, prior, stats, U)
     loss = -(lj - lq).mean()
     gmu = -g.mean(0)
     gsig = -(g * eps).mean(0) - 1.0 / sig

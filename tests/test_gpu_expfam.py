@@ -152,3 +152,49 @@ def test_hmc_conjugate_posteriors(cuda, family):
     else:
         post = prior + np.bincount(data, minlength=4)
         np.testing.assert_allclose(zs.mean(0).cpu().numpy(), post / post.sum(), atol=0.02)
+
+
+@pytest.mark.parametrize("family", [ef.BETA, ef.GAMMA])
+def test_expfam_klqp_on_support_matches_oracle(cuda, family):
+    """auto_transform=False: q fitted on the latent's support itself (z = u, no
+    Jacobian); with every draw inside the support, loss and gradients agree
+    with the FP64 oracle to 1e-5."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Normal
+    rng = np.random.default_rng(20 + family)
+    z, x, data, prior, K = _model(ed, family, rng)
+    stats = ef.sufficient_stats(family, data, K + 1)
+    mu0 = np.float32(0.4 if family == ef.BETA else 3.0)
+    rho0 = np.float32(-3.0 if family == ef.BETA else -1.0)
+    qz = Normal(loc=ed.Variable(mu0), scale=ed.softplus(ed.Variable(rho0)))
+    inf = ed.KLqp({z: qz}, data={x: data})
+    S = 6
+    inf.initialize(n_samples=S, auto_transform=False)
+    eps = np.clip(rng.standard_normal((S, 1)), -2.0, 2.0).astype(np.float32)
+    loss, gmu, grho = inf.loss_and_gradients(eps)
+    l0, m0, r0 = ef.klqp_loss_and_grads(family, prior, stats, [mu0], [rho0], eps,
+                                        transform=False)
+    assert np.isfinite(l0)
+    assert abs(loss - l0) <= 1e-5 * max(1.0, abs(l0))
+    np.testing.assert_allclose(gmu.cpu().numpy(), m0, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(grho.cpu().numpy(), r0, rtol=1e-5, atol=1e-6)
+
+
+def test_klqp_auto_transform_false_gives_nan(cuda):
+    """tests/inferences/inference_auto_transform_test.py:46-63: a latent with a
+    nonnegative support fitted by a Normal q without auto_transform; q's draws
+    leave the support and the loss becomes NaN (numerical failure is not an
+    error).  With auto_transform the same fit stays finite."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Gamma, Normal
+    for auto, expect_nan in ((False, True), (True, False)):
+        ed.set_seed(42)
+        x = Gamma(2.0, 4.0)
+        rng = np.random.default_rng(0)
+        qx = Normal(loc=ed.Variable(np.float32(rng.standard_normal())),
+                    scale=ed.softplus(ed.Variable(np.float32(rng.standard_normal()))))
+        inference = ed.KLqp({x: qx})
+        inference.initialize(auto_transform=auto, n_samples=5, n_iter=150)
+        for _ in range(inference.n_iter):
+            info_dict = inference.update()
+        assert bool(np.isnan(info_dict["loss"])) == expect_nan, (auto, info_dict)

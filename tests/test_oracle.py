@@ -345,3 +345,54 @@ def test_cpu_baseline_bnn_step_matches_oracle():
     assert abs(loss - loss64) <= 1e-4 * abs(loss64)
     big = np.abs(gmu64) > 1e-3 * np.abs(gmu64).max()
     assert np.all(np.sign(mu0 - mu)[big] == np.sign(gmu64)[big])
+
+
+@pytest.mark.parametrize("transform", [True, False])
+@pytest.mark.parametrize("family", [0, 1, 2])
+def test_expfam_gradients_finite_differences(family, transform):
+    """The constrained-latent log joints' hand-written gradients, in the
+    unconstrained space and on the support itself, against FP64 central
+    differences; on the support, NaN outside it (the reference's densities give
+    NaN for such draws: inference_auto_transform_test.py:46-63)."""
+    from oracle import expfam as ef
+    if family == ef.DIRICHLET and not transform:
+        pytest.skip("the Dirichlet latent is worked in the unconstrained space only")
+    rng = np.random.default_rng(family)
+    if family == ef.BETA:
+        prior, stats = (1.5, 2.0), ef.sufficient_stats(ef.BETA, rng.integers(0, 2, 12))
+        U = rng.uniform(0.1, 0.9, (5, 1)) if not transform else rng.standard_normal((5, 1))
+    elif family == ef.GAMMA:
+        prior, stats = (2.0, 0.5), ef.sufficient_stats(ef.GAMMA, rng.poisson(3.0, 9))
+        U = rng.uniform(0.5, 6.0, (5, 1)) if not transform else rng.standard_normal((5, 1))
+    else:
+        prior = np.array([1.0, 2.0, 0.5, 3.0])
+        stats = ef.sufficient_stats(ef.DIRICHLET, rng.integers(0, 4, 20), 4)
+        U = rng.standard_normal((5, 3))
+    lj = ef.log_joint if transform else ef.log_joint_support
+    glj = ef.grad_log_joint if transform else ef.grad_log_joint_support
+    g = glj(family, prior, stats, U)
+    h = 1e-6
+    for j in range(U.shape[1]):
+        e = np.zeros_like(U)
+        e[:, j] = h
+        fd = (lj(family, prior, stats, U + e) - lj(family, prior, stats, U - e)) / (2 * h)
+        np.testing.assert_allclose(g[:, j], fd, rtol=1e-6, atol=1e-6)
+    if not transform:
+        out = np.array([[-0.5], [1.5]]) if family == ef.BETA else np.array([[-0.5], [0.0]])
+        assert np.all(np.isnan(lj(family, prior, stats, out)))
+        assert np.all(np.isnan(glj(family, prior, stats, out)))
+
+
+def test_expfam_support_and_unconstrained_log_joints_agree():
+    """log p(x, z) on the support equals the unconstrained log joint minus the
+    bijector's log|dz/du| at z = bijector(u)."""
+    from oracle import expfam as ef
+    rng = np.random.default_rng(3)
+    U = rng.standard_normal((7, 1))
+    for family, prior, stats in ((ef.BETA, (1.5, 2.0), (4.0, 6.0)),
+                                 (ef.GAMMA, (2.0, 0.5), (25.0, 9.0, 11.3))):
+        Z = ef.constrain(family, U)
+        ldj = (-dn.softplus(-U) - dn.softplus(U))[:, 0] if family == ef.BETA \
+            else -dn.softplus(-U)[:, 0]
+        np.testing.assert_allclose(ef.log_joint_support(family, prior, stats, Z),
+                                   ef.log_joint(family, prior, stats, U) - ldj, rtol=1e-12)
