@@ -397,9 +397,10 @@ def run_gpu(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic",
-                "config": dict(CONFIG, parallelism=f"replicas{world}",
-                               l2_flush="256 MB write before each step, outside the timed events",
-                               engine=inf.engine, accept_rate=round(acc, 4)),
+                "config": dict(CONFIG,
+                               l2_flush="256 MB write before each step, outside the timed events"),
+                "parallelism": f"replicas{world}", "engine": inf.engine,
+                "accept_rate": round(acc, 4),
                 "e2e": e2e, "gpu_launches": args.steps, "roofline": roof,
                 "cpu_baseline": cb, "clocks": clk.summary(),
                 "wall_s_timed_region": wall}
