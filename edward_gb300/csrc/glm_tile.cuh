@@ -192,6 +192,9 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
     const float4* xr0 = reinterpret_cast<const float4*>(Xb + (2 * rp) * PP);
     const float4* xr1 = reinterpret_cast<const float4*>(Xb + (2 * rp + 1) * PP);
     const float4* zt = reinterpret_cast<const float4*>(S.Zt);
+    // (unrolled so that the next feature quad's loads issue before this
+    // quad's FMAs; likewise the row loop of phase B below)
+#pragma unroll 2
     for (int dq = 0; dq < P4; ++dq) {
       const float4 x0 = xr0[dq], x1 = xr1[dq];
       const float4 z0 = zt[(4 * dq + 0) * CQ + cq];
@@ -236,6 +239,7 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
         if (k >= nu) break;
         const int cqb = u % CQ, dqb = u / CQ;
         float* a = accB[k];
+#pragma unroll 4
         for (int r = hgrp; r < RT; r += H) {
           const float4 rr = reinterpret_cast<const float4*>(S.Rs + r * CT)[cqb];
           const float4 xx = reinterpret_cast<const float4*>(Xb + r * PP)[dqb];
