@@ -81,6 +81,14 @@ __global__ void glm_reduce_kernel(GLMDev m, const float* __restrict__ Z, int B, 
 }
 
 // ============================================================ KLqp step
+// The fused KLqp step runs tiles of one row per thread (RT = 1024 / CT rows)
+// for up to 16 samples: a 10,000-row problem then spreads over 79 blocks
+// instead of 40, which halves each block's share of the latency-bound tile
+// loop.  32-vector tiles keep two rows per thread (the per-sample gradients of
+// the tail live in the tile buffers, 2 RT rows of them).
+template <int CT>
+__host__ __device__ constexpr int klqp_rpt() { return CT == 32 ? 2 : 1; }
+
 struct KlqpArgs {
   int method, S, Spad, nblocks, chunk;
   double inv_S;  // 1 / S
@@ -106,10 +114,10 @@ __device__ __forceinline__ float eps_value(const KlqpArgs& a, uint32_t iter, int
 }
 
 template <int CT>
-__global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   GradSmem S;
-  unsigned char* rest = carve_grad<CT>(smem, m.PP, S);
+  unsigned char* rest = carve_grad<CT, klqp_rpt<CT>()>(smem, m.PP, S);
   float* sig = reinterpret_cast<float*>(rest);  // [PP]
   float* epsS = sig + m.PP;                      // [Spad][PP] this step's draws
   // The step's per-coordinate inputs, loaded once by every block at the start
@@ -128,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   const int P = m.P, PP = m.PP;
   const int rb = blockIdx.x * a.chunk, re = min(m.N, rb + a.chunk);
   // the first X tile's copy overlaps the loads and draws below
-  if (re > rb) issue_tile<CT>(m, S.Xs, S.ys, rb, re);
+  if (re > rb) issue_tile<CT, klqp_rpt<CT>()>(m, S.Xs, S.ys, rb, re);
   cp_async_commit();
   const int64_t t = *(volatile int64_t*)&a.state->t;
   const int64_t gstep = a.state->global_step;
@@ -149,7 +157,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
     s_pt[d] = pt;
     sig[d] = (ok && !pt) ? softplusf(rho) : 0.0f;
   }
-  init_x_pad<CT>(m, S);
+  init_x_pad<CT, klqp_rpt<CT>()>(m, S);
   __syncthreads();
   // the score method needs d log p / d z only for model parameters
   const bool need_grad = a.method != EDG_KLQP_SCORE || a.point != nullptr;
@@ -166,7 +174,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
       S.Zt[d * CT + c] = zv;
     }
     __syncthreads();
-    glm_grad_eval<CT>(m, rb, re, S, true, need_grad, a.dscale, s0 == 0);
+    glm_grad_eval<CT, klqp_rpt<CT>()>(m, rb, re, S, true, need_grad, a.dscale, s0 == 0);
     for (int idx = threadIdx.x; idx < CT * PP; idx += kThreads) {
       const int c = idx / PP;
       if (s0 + c < a.S && need_grad)
@@ -194,13 +202,25 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   double* red = lsig + a.S;              // [8] per-warp partial sums
   float* gS = S.Xs;                      // [S][PP] gradient per sample
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int kBatch = 64;             // partials per thread in flight at once
+  constexpr int kBatch = 96;             // partials per thread in flight at once
+  // fixed-order sum of a batch: [64, 96) folded onto [0, 32), then a tree over 64
+  auto batch_sum = [](float (&v)[kBatch]) {
+    static_assert(kBatch == 96, "fold assumes 96 = 64 + 32");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] += v[k + 64];
+#pragma unroll
+    for (int w = 32; w > 0; w >>= 1) {
+#pragma unroll
+      for (int k = 0; k < w; ++k) v[k] += v[k + w];
+    }
+    return v[0];
+  };
   // log-likelihood partials: one warp per sample, lanes over the blocks
-  double llv[2] = {0.0, 0.0};
-  const bool ll_fast = a.nblocks <= 64 && a.S <= kThreads / 32;
+  double llv[3] = {0.0, 0.0, 0.0};
+  const bool ll_fast = a.nblocks <= 96 && a.S <= kThreads / 32;
   if (ll_fast && warp < a.S) {
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
       const int b = lane + 32 * k;
       if (b < a.nblocks) llv[k] = __ldcg(a.ws_ll + (size_t)b * a.Spad + warp);
     }
@@ -259,7 +279,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   // reduce the partials
   if (ll_fast) {
     if (warp < a.S) {
-      double v = llv[0] + llv[1];
+      double v = (llv[0] + llv[1]) + llv[2];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       if (lane == 0) llS[warp] = v;
@@ -275,13 +295,8 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
   }
   if (g_fast) {
     if (q0 < a.S * P) {
-#pragma unroll
-      for (int w = kBatch / 2; w > 0; w >>= 1) {
-#pragma unroll
-        for (int k = 0; k < w; ++k) gv[k] += gv[k + w];
-      }
       const int sq = q0 / P, dq = q0 - sq * P;
-      gS[sq * PP + dq] = gv[0];
+      gS[sq * PP + dq] = batch_sum(gv);
     }
   } else if (need_grad) {
     for (int q = threadIdx.x; q < a.S * P; q += kThreads) {
@@ -294,12 +309,7 @@ __global__ void __launch_bounds__(kThreads) klqp_glm_kernel(GLMDev m, KlqpArgs a
 #pragma unroll
         for (int k = 0; k < kBatch; ++k)
           v[k] = b0 + k < a.nblocks ? __ldcg(src + (size_t)(b0 + k) * st) : 0.0f;
-#pragma unroll
-        for (int w = kBatch / 2; w > 0; w >>= 1) {
-#pragma unroll
-          for (int k = 0; k < w; ++k) v[k] += v[k + w];
-        }
-        acc += v[0];
+        acc += batch_sum(v);
       }
       gS[sq * PP + dq] = acc;
     }
@@ -640,6 +650,12 @@ static size_t grad_smem_bytes(int PP) {
   return grad_smem_doubles<CT>() * 8 + grad_smem_floats<CT>(PP) * 4;
 }
 
+template <int CT>
+static size_t klqp_grad_smem_bytes(int PP) {
+  constexpr int R = klqp_rpt<CT>();
+  return grad_smem_doubles<CT, R>() * 8 + grad_smem_floats<CT, R>(PP) * 4;
+}
+
 static int pick_ct(int B) { return B <= 8 ? 8 : (B <= 16 ? 16 : 32); }
 
 struct GradPlan {
@@ -730,7 +746,7 @@ static KlqpPlan plan_klqp(const GLMDev& m, int S) {
   KlqpPlan p;
   p.CT = pick_ct(S);
   p.Spad = round_up(S, p.CT);
-  const int RT = 2048 / p.CT;
+  const int RT = 1024 * (p.CT == 32 ? 2 : 1) / p.CT;
   const int ntiles = (m.N + RT - 1) / RT;
   const int sm = sm_count();
   const int tiles_per_block = std::max(1, (ntiles + sm - 1) / sm);
@@ -750,12 +766,13 @@ extern "C" size_t edg_klqp_glm_workspace_bytes(const edg_glm_t* model, const edg
 
 template <int CT>
 static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
-  const size_t sm = grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4 + (size_t)a.Spad * m.PP * 4 +
-                    (size_t)11 * m.PP * 4;
+  constexpr int RT = Tile<CT, klqp_rpt<CT>()>::RT;
+  const size_t sm = klqp_grad_smem_bytes<CT>(m.PP) + (size_t)m.PP * 4 +
+                    (size_t)a.Spad * m.PP * 4 + (size_t)11 * m.PP * 4;
   EDG_REQUIRE((int)sm <= max_smem_optin(), EDG_E_UNSUPPORTED, "P=%d too large for KLqp kernel", m.P);
   // the tail's per-sample sums and per-warp partials reuse the log-lik partials
-  EDG_REQUIRE(a.S * 2 + 8 <= (Tile<CT>::RT / 2) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
-  EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * Tile<CT>::RT * m.PP, EDG_E_UNSUPPORTED,
+  EDG_REQUIRE(a.S * 2 + 8 <= (RT / klqp_rpt<CT>()) * CT, EDG_E_UNSUPPORTED, "n_samples too large");
+  EDG_REQUIRE((size_t)a.S * m.PP <= (size_t)2 * RT * m.PP, EDG_E_UNSUPPORTED,
               "n_samples too large");
   const int rc = set_max_dyn_smem(klqp_glm_kernel<CT>, sm, "klqp_glm_kernel");
   if (rc) return rc;

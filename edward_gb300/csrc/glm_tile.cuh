@@ -10,11 +10,16 @@ namespace edg {
 
 constexpr int kThreads = 256;
 
-template <int CT>
+// A tile is RT rows x CT vectors; each of the 256 threads computes RPT rows x
+// 4 vectors of its eta (RPT = 2: 8 outputs per thread, the default; RPT = 1
+// halves the rows per tile for problems whose row count spreads over too few
+// blocks otherwise).
+template <int CT, int RPT = 2>
 struct Tile {
   static_assert(CT == 8 || CT == 16 || CT == 32, "chains per block must be 8, 16 or 32");
-  static constexpr int RT = 2048 / CT;  // rows per tile: RT * CT = 8 outputs per thread
-  static constexpr int CQ = CT / 4;     // chain quads
+  static_assert(RPT == 1 || RPT == 2, "rows per thread must be 1 or 2");
+  static constexpr int RT = 1024 * RPT / CT;  // rows per tile
+  static constexpr int CQ = CT / 4;           // chain quads
 };
 
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem, int src_bytes) {
@@ -35,33 +40,34 @@ struct GradSmem {
   float* Zt;      // [PP][CT]     parameter vectors, transposed
   float* G;       // [CT][PP]     OUT: likelihood gradient (scaled)
   float* Gpart;   // [4096]       row-group partials of G
-  double* llred;  // [RT/2][CT]   per-thread log-lik partials
+  double* llred;  // [RT/RPT][CT] per-thread log-lik partials
   double* ll;     // [CT]         OUT: log-likelihood (scaled)
 };
 
-template <int CT>
+template <int CT, int RPT = 2>
 __host__ __device__ constexpr size_t grad_smem_floats(int PP) {
-  return (size_t)2 * Tile<CT>::RT * PP + 2 * Tile<CT>::RT + (size_t)Tile<CT>::RT * CT +
-         (size_t)PP * CT + (size_t)CT * PP + 4096;
+  return (size_t)2 * Tile<CT, RPT>::RT * PP + 2 * Tile<CT, RPT>::RT +
+         (size_t)Tile<CT, RPT>::RT * CT + (size_t)PP * CT + (size_t)CT * PP + 4096;
 }
-template <int CT>
+template <int CT, int RPT = 2>
 __host__ __device__ constexpr size_t grad_smem_doubles() {
-  return (size_t)(Tile<CT>::RT / 2) * CT + CT;
+  return (size_t)(Tile<CT, RPT>::RT / RPT) * CT + CT;
 }
 
 // Carves GradSmem from `base` (16-byte aligned); returns the first free byte.
-template <int CT>
+template <int CT, int RPT = 2>
 __device__ unsigned char* carve_grad(unsigned char* base, int PP, GradSmem& S) {
+  constexpr int RT = Tile<CT, RPT>::RT;
   double* d = reinterpret_cast<double*>(base);
   S.llred = d;
-  d += (Tile<CT>::RT / 2) * CT;
+  d += (RT / RPT) * CT;
   S.ll = d;
   d += CT;
   float* f = reinterpret_cast<float*>(d);
   S.Xs = f;
-  f += 2 * Tile<CT>::RT * PP;
+  f += 2 * RT * PP;
   S.Rs = f;
-  f += Tile<CT>::RT * CT;
+  f += RT * CT;
   S.Zt = f;
   f += PP * CT;
   S.G = f;
@@ -69,14 +75,14 @@ __device__ unsigned char* carve_grad(unsigned char* base, int PP, GradSmem& S) {
   S.Gpart = f;
   f += 4096;
   S.ys = f;
-  f += 2 * Tile<CT>::RT;
+  f += 2 * RT;
   return reinterpret_cast<unsigned char*>(f);
 }
 
 // Constant columns of both X buffers: bias column = 1 (if any), padding = 0.
-template <int CT>
+template <int CT, int RPT = 2>
 __device__ void init_x_pad(const GLMDev& m, const GradSmem& S) {
-  constexpr int RT = Tile<CT>::RT;
+  constexpr int RT = Tile<CT, RPT>::RT;
   const int extra = m.PP - m.D;
   for (int i = threadIdx.x; i < 2 * RT * extra; i += kThreads) {
     const int row = i / extra, col = m.D + i % extra;
@@ -84,10 +90,10 @@ __device__ void init_x_pad(const GLMDev& m, const GradSmem& S) {
   }
 }
 
-template <int CT>
+template <int CT, int RPT = 2>
 __device__ __forceinline__ void issue_tile(const GLMDev& m, float* Xdst, float* ydst, int row0,
                                            int row_end) {
-  constexpr int RT = Tile<CT>::RT;
+  constexpr int RT = Tile<CT, RPT>::RT;
   const int nrows = min(RT, row_end - row0);
   const int D = m.D, PP = m.PP;
   const int total = RT * D;
@@ -133,14 +139,15 @@ __device__ __forceinline__ void lik_term(const GLMDev& m, float y, float eta, fl
 // Log-likelihood (and gradient) of CT vectors S.Zt over rows [row_begin, row_end).
 // All threads of the block must call it.  On return S.G / S.ll hold the
 // results (multiplied by dscale) and a __syncthreads() has been done.
-template <int CT>
+template <int CT, int RPT = 2>
 __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const GradSmem& S,
                               bool need_ll, bool need_grad, float dscale,
                               bool first_issued = false) {
-  constexpr int RT = Tile<CT>::RT, CQ = Tile<CT>::CQ;
+  constexpr int RT = Tile<CT, RPT>::RT, CQ = Tile<CT, RPT>::CQ;
   const int tid = threadIdx.x;
   const int PP = m.PP, P4 = PP / 4;
-  const int cq = tid % CQ, rp = tid / CQ;  // phase A: rows 2rp, 2rp+1; chains 4cq..4cq+3
+  // phase A: rows RPT rp .. RPT rp + RPT - 1; chains 4cq..4cq+3
+  const int cq = tid % CQ, rp = tid / CQ;
   // phase B: units of (chain quad, feature quad)
   const int U = CQ * P4;
   int H, nu, unit0, unit1, hgrp;
@@ -168,14 +175,14 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
   // (first_issued: the caller already issued and committed the first tile
   // into buffer 0, so that its copy overlaps the caller's own set-up work)
   if (!first_issued) {
-    if (ntiles > 0) issue_tile<CT>(m, S.Xs, S.ys, row_begin, row_end);
+    if (ntiles > 0) issue_tile<CT, RPT>(m, S.Xs, S.ys, row_begin, row_end);
     cp_async_commit();
   }
   for (int it = 0; it < ntiles; ++it) {
     const int buf = it & 1;
     if (it + 1 < ntiles)
-      issue_tile<CT>(m, S.Xs + (buf ^ 1) * RT * PP, S.ys + (buf ^ 1) * RT, row_begin + (it + 1) * RT,
-                     row_end);
+      issue_tile<CT, RPT>(m, S.Xs + (buf ^ 1) * RT * PP, S.ys + (buf ^ 1) * RT,
+                          row_begin + (it + 1) * RT, row_end);
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
@@ -184,13 +191,13 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
     const int r0 = row_begin + it * RT;
 
     // ---- phase A: eta = X z
-    float acc[2][4];
+    float acc[RPT][4];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < RPT; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
-    const float4* xr0 = reinterpret_cast<const float4*>(Xb + (2 * rp) * PP);
-    const float4* xr1 = reinterpret_cast<const float4*>(Xb + (2 * rp + 1) * PP);
+    const float4* xr0 = reinterpret_cast<const float4*>(Xb + (RPT * rp) * PP);
+    const float4* xr1 = reinterpret_cast<const float4*>(Xb + (RPT * rp + RPT - 1) * PP);
     const float4* zt = reinterpret_cast<const float4*>(S.Zt);
     // (unrolled so that the next feature quad's loads issue before this
     // quad's FMAs; likewise the row loop of phase B below)
@@ -211,13 +218,15 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
   A[0] = fmaf(XV.w, z3.x, A[0]); A[1] = fmaf(XV.w, z3.y, A[1]);            \
   A[2] = fmaf(XV.w, z3.z, A[2]); A[3] = fmaf(XV.w, z3.w, A[3]);
       EDG_ROWFMA(acc[0], x0)
-      EDG_ROWFMA(acc[1], x1)
+      if (RPT == 2) {
+        EDG_ROWFMA(acc[RPT - 1], x1)
+      }
 #undef EDG_ROWFMA
     }
     // ---- epilogue: residuals and log-lik terms
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const int lr = 2 * rp + i;
+    for (int i = 0; i < RPT; ++i) {
+      const int lr = RPT * rp + i;
       const bool valid = r0 + lr < row_end;
       const float yv = yb[lr];
       float res[4];
@@ -290,7 +299,7 @@ __device__ void glm_grad_eval(const GLMDev& m, int row_begin, int row_end, const
     const int warp = tid >> 5, lane = tid & 31;
     for (int c = warp; c < CT; c += kThreads / 32) {
       double s = 0.0;
-      for (int q = lane; q < RT / 2; q += 32) s += S.llred[q * CT + c];
+      for (int q = lane; q < RT / RPT; q += 32) s += S.llred[q * CT + c];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) S.ll[c] = s * (double)dscale;
