@@ -150,7 +150,11 @@ def _klqp(m, cuda, method, n_samples, optimizer=None):
 
 
 @pytest.mark.parametrize("method", [REPARAM_KL, REPARAM, SCORE])
-@pytest.mark.parametrize("N,D,S", [(37, 5, 4), (10000, 50, 5), (2000, 20, 40)])
+# (15000, 10, 3): 118 row blocks, more than one batch of block partials in the
+# step's tail; (3000, 8, 12): 16-vector tiles; (2000, 20, 40): 40 samples, the
+# per-sample sums loop
+@pytest.mark.parametrize("N,D,S", [(37, 5, 4), (10000, 50, 5), (2000, 20, 40), (15000, 10, 3),
+                                   (3000, 8, 12)])
 def test_klqp_loss_and_gradients_parity(cuda, method, N, D, S):
     X, y, _, _ = synthetic_logreg(N, D, seed=N)
     m = f32(GLM(X, y, bias=True, data_scale=1.5, prior_scale=1.2))
