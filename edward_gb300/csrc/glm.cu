@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArg
   // score / reparam: per-sample log p(z_s) - log q(z_s), one warp per sample
   if (a.method != EDG_KLQP_REPARAM_KL) {
     for (int s = warp; s < a.S; s += kThreads / 32) {
-      double acc = 0.0;
+      float acc = 0.0f;  // FP32: a few terms per lane, 32 lanes
       for (int d = lane; d < P; d += 32) {
         if (s_pt[d]) continue;
         const float lsc = s_ls[d];
@@ -251,30 +251,31 @@ __global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArg
         const float zq = (zv - s_mu[d]) / sig[d];
         const float lp = -0.5f * zp * zp - logf(ps);
         const float lq = -0.5f * zq * zq - logf(sig[d]);
-        acc += (double)(lsc * (lp - lq));  // the 0.5 log 2pi terms cancel
+        acc += lsc * (lp - lq);  // the 0.5 log 2pi terms cancel
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) lsig[s] = acc;
+      if (lane == 0) lsig[s] = (double)acc;
     }
   }
-  // analytic KL: one coordinate per thread, block reduction in FP64
+  // analytic KL: one coordinate per thread, FP32 within a warp (FP64 runs at a
+  // small fraction of the FP32 rate here), FP64 across the warps that hold
+  // coordinates
   double klsum = 0.0;
-  if (a.method == EDG_KLQP_REPARAM_KL) {
-    double kl = 0.0;
+  const int kl_warps = min(kThreads / 32, (P + 31) / 32);
+  if (a.method == EDG_KLQP_REPARAM_KL && warp < kl_warps) {
+    float kl = 0.0f;
     for (int d = threadIdx.x; d < P; d += kThreads) {
       if (s_pt[d]) continue;
       const float ks = s_ks[d];
       const float sp = s_ps[d], sq = sig[d];
       const float dm = (s_mu[d] - s_pl[d]) / sp;
       const float ratio = (sq / sp) * (sq / sp);
-      // FP32 per coordinate (FP64 runs at a small fraction of the FP32 rate
-      // here), summed in FP64
-      kl += (double)(ks * (0.5f * dm * dm + 0.5f * ((ratio - 1.0f) - logf(ratio))));
+      kl += ks * (0.5f * dm * dm + 0.5f * ((ratio - 1.0f) - logf(ratio)));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) kl += __shfl_xor_sync(0xffffffffu, kl, o);
-    if (lane == 0) red[warp] = kl;
+    if (lane == 0) red[warp] = (double)kl;
   }
   // reduce the partials
   if (ll_fast) {
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArg
     mean_ll *= a.inv_S;
     double loss;
     if (a.method == EDG_KLQP_REPARAM_KL) {
-      for (int w = 0; w < kThreads / 32; ++w) klsum += red[w];
+      for (int w = 0; w < kl_warps; ++w) klsum += red[w];
       loss = -(mean_ll - klsum);
       a.state->aux[0] = mean_ll;
       a.state->aux[1] = klsum;
