@@ -1029,8 +1029,9 @@ def hier_data(I=2048, seed=0):
 def run_hier(args):
     """All 2,048 instances x 64 chains, 10 leapfrog steps per iteration, one
     launch per iteration (edg_hmc_hier_run), timed for both launch forms (the
-    persistent work-queue grid and one CTA per (instance, chain tile)); the
-    faster form is then replayed from a CUDA graph, which is the value."""
+    persistent work-queue grid and one CTA per (instance, chain tile)) and both
+    tile shapes (32 chains x 64 rows, 16 chains x 128 rows); the fastest pair
+    is then replayed from a CUDA graph, which is the value."""
     import ctypes
     import numpy as np
     import torch
@@ -1065,15 +1066,18 @@ def run_hier(args):
         b.synchronize()
         return a.elapsed_time(b) / k
 
-    forms = {}
-    for launch, name in ((0, "persistent"), (1, "one_cta_per_item")):
-        cfg.launch = launch
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
-        forms[name] = timed(step, args.steps)
+    forms, shape = {}, {}
+    for launch, lname in ((0, "persistent"), (1, "one_cta_per_item")):
+        for ct in (32, 16):
+            name = f"{lname}_{ct}x{2048 // ct}"
+            cfg.launch, cfg.chains_per_block = launch, ct
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            forms[name] = timed(step, args.steps)
+            shape[name] = (launch, ct)
     best = min(forms, key=forms.get)
-    cfg.launch = 0 if best == "persistent" else 1
+    cfg.launch, cfg.chains_per_block = shape[best]
     graph = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -1103,7 +1107,7 @@ def run_hier(args):
                          "frac": ach / peak,
                          "traffic": read_traffic_file("hmc_hier_kernel_ragged_I2048.txt")
                          if hd.I == 2048 else None,
-                         "kernel": "hmc_hier_kernel<32> (SIMT FP32)",
+                         "kernel": "hmc_hier_kernel<%d> (SIMT FP32)" % shape[best][1],
                          "peak_source": src, "algorithmic_flops_per_launch": flops,
                          "x_stream_GBs": 2 * L * work * 4 / (ms / 1e3) / 1e9},
             "accept_rate": float(nacc.sum().item()) / (n * (2 * args.warmup + 3 * args.steps + 1)),

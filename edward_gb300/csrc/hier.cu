@@ -355,6 +355,27 @@ __global__ void __launch_bounds__(kThreads) hmc_hier_kernel(HierArgs a) {
 
 using namespace edg;
 
+template <int CT>
+static int launch_hier(const HierArgs& a, int64_t nitems, int PPmax, int max_D, void* stream) {
+  const size_t sm = hier_smem_bytes<CT>(PPmax);
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  EDG_REQUIRE((int)sm <= optin, EDG_E_UNSUPPORTED,
+              "max_D=%d needs %zu bytes of shared memory with %d chains per block", max_D, sm, CT);
+  const int rc_attr = set_max_dyn_smem(hmc_hier_kernel<CT>, sm, "hmc_hier_kernel");
+  if (rc_attr) return rc_attr;
+  int64_t nblocks = nitems;
+  if (a.persistent) {
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hmc_hier_kernel<CT>, kThreads, sm);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    nblocks = std::min<int64_t>(nitems, (int64_t)std::max(per_sm, 1) * std::max(sms, 1));
+  }
+  hmc_hier_kernel<CT><<<(unsigned)nblocks, kThreads, sm, (cudaStream_t)stream>>>(a);
+  return check_launch("hmc_hier_kernel");
+}
+
 extern "C" int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C,
                                 int32_t n_iter, const int32_t* order, float* z, float* grad,
                                 double* lj, int32_t cache_valid, int32_t* n_accept,
@@ -375,7 +396,11 @@ extern "C" int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, i
   EDG_REQUIRE(cfg->n_steps >= 0, EDG_E_VALUE, "n_steps must be >= 0");
   EDG_REQUIRE(!samples || T_cap > 0, EDG_E_SHAPE, "T_cap must be positive when samples is given");
   if (n_iter == 0 && cache_valid) return EDG_OK;
-  constexpr int CT = 32;
+  // tile shape: 32 chains x 64 rows (default) or 16 chains x 128 rows
+  EDG_REQUIRE(cfg->chains_per_block == 0 || cfg->chains_per_block == 16 ||
+                  cfg->chains_per_block == 32,
+              EDG_E_VALUE, "chains_per_block must be 0, 16 or 32 (got %d)", cfg->chains_per_block);
+  const int CT = cfg->chains_per_block == 16 ? 16 : 32;
   HierArgs a;
   a.X = model->X;
   a.y = model->y;
@@ -407,27 +432,12 @@ extern "C" int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, i
   a.r_ovr = r_override;
   a.u_ovr = u_override;
   a.ratio_out = ratio_out;
-  const int PPmax = round_up(model->max_D, 4);
-  const size_t sm = hier_smem_bytes<CT>(PPmax);
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  EDG_REQUIRE((int)sm <= optin, EDG_E_UNSUPPORTED, "max_D=%d needs %zu bytes of shared memory",
-              model->max_D, sm);
-  const int rc_attr = set_max_dyn_smem(hmc_hier_kernel<CT>, sm, "hmc_hier_kernel");
-  if (rc_attr) return rc_attr;
-  const int64_t nitems = (int64_t)a.I * a.tiles_per_inst;
-  EDG_REQUIRE(nitems < (1ll << 31), EDG_E_SHAPE, "too many instances x chain tiles");
   EDG_REQUIRE(cfg->launch == 0 || cfg->launch == 1, EDG_E_VALUE, "launch must be 0 or 1 (got %d)",
               cfg->launch);
   a.persistent = cfg->launch == 0 ? 1 : 0;
-  int64_t nblocks = nitems;
-  if (a.persistent) {
-    int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hmc_hier_kernel<CT>, kThreads, sm);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    nblocks = std::min<int64_t>(nitems, (int64_t)std::max(per_sm, 1) * std::max(sms, 1));
-  }
-  hmc_hier_kernel<CT><<<(unsigned)nblocks, kThreads, sm, (cudaStream_t)stream>>>(a);
-  return check_launch("hmc_hier_kernel");
+  const int64_t nitems = (int64_t)a.I * a.tiles_per_inst;
+  EDG_REQUIRE(nitems < (1ll << 31), EDG_E_SHAPE, "too many instances x chain tiles");
+  const int PPmax = round_up(model->max_D, 4);
+  return CT == 16 ? launch_hier<16>(a, nitems, PPmax, model->max_D, stream)
+                  : launch_hier<32>(a, nitems, PPmax, model->max_D, stream);
 }

@@ -187,23 +187,26 @@ class HMC(MonteCarlo):
         self._cfg = cfg
         self.engine = "hier"
         self._graphs = {}
-        cfg.launch = self._autotune_hier()
+        best = self._autotune_hier()
+        cfg.launch, cfg.chains_per_block = best & 1, 16 if best & 2 else 32
         self.train = self.update
         return self.train
 
     def _autotune_hier(self):
-        """Launch form of the ragged batch (persistent work-queue grid or one
-        CTA per (instance, chain tile)), timed on scratch copies of the state
-        and cached per model shape."""
+        """Launch form (persistent work-queue grid or one CTA per (instance,
+        chain tile)) and tile shape (32 chains x 64 rows or 16 chains x 128
+        rows) of the ragged batch, timed on scratch copies of the state and
+        cached per model shape.  Candidate c encodes launch = c & 1 and 16
+        chains per block when c & 2."""
         hd, C = self._hier, self.C
         z = self._z.clone()
         g = torch.zeros_like(self._g)
         lj = torch.zeros_like(self._lj)
 
-        def run(launch):
+        def run(c):
             cfg = _lib.EdgHMC()
-            cfg.step_size, cfg.n_steps, cfg.seed, cfg.launch = (self._cfg.step_size,
-                                                                 self._cfg.n_steps, 1, launch)
+            cfg.step_size, cfg.n_steps, cfg.seed = self._cfg.step_size, self._cfg.n_steps, 1
+            cfg.launch, cfg.chains_per_block = c & 1, 16 if c & 2 else 32
             z.copy_(self._z)
             st = _lib.new_state(self._device)
             _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
@@ -212,7 +215,7 @@ class HMC(MonteCarlo):
 
         work = int((hd.Ns.astype(np.int64) * hd.Ds).sum())
         key = f"I{hd.I}_work{work}_maxD{hd.max_D}_C{C}_L{self.n_steps}"
-        return autotune.choose("hmc_hier", key, [0, 1], run)
+        return autotune.choose("hmc_hier_shape", key, [0, 1, 2, 3], run)
 
     def _build_expfam(self):
         """Chains of the unconstrained latent u (FP32, as the reference's

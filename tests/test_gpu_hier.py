@@ -18,11 +18,12 @@ def _instances(seed=3):
     return Xs + X2, ys + y2
 
 
-def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launch=0):
+def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launch=0, ct=32):
     from edward_gb300 import _lib
     cuda = z0.device
     cfg = _lib.EdgHMC()
     cfg.step_size, cfg.n_steps, cfg.seed, cfg.launch = step, L, seed, launch
+    cfg.chains_per_block = ct
     n = hd.I * C
     z = z0.clone()
     g = torch.zeros_like(z)
@@ -38,7 +39,10 @@ def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launc
     return z, g, lj, nacc, ratio, _lib.read_state(st)
 
 
-def test_hier_iteration_parity(cuda):
+@pytest.mark.parametrize("ct", [32, 16])
+def test_hier_iteration_parity(cuda, ct):
+    """One iteration of every instance against the oracle, for both tile
+    shapes (32 chains x 64 rows, 16 chains x 128 rows)."""
     from edward_gb300.ops import HierDevice
     Xs, ys = _instances()
     kw = dict(mu_loc=0.1, mu_scale=1.2, tau_scale=0.8)
@@ -56,7 +60,7 @@ def test_hier_iteration_parity(cuda):
     u = rng.random((1, hd.I * C))
     z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
                                      r=torch.as_tensor(r0, device=cuda),
-                                     u=torch.as_tensor(u, device=cuda))
+                                     u=torch.as_tensor(u, device=cuda), ct=ct)
     assert st.t == 1
     zk, rk, ak = z.cpu().numpy(), ratio.cpu().numpy()[0], nacc.cpu().numpy().astype(bool)
     for i, (X, y) in enumerate(zip(Xs, ys)):
