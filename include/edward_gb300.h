@@ -130,7 +130,9 @@ typedef struct {
   float step_size;
   int32_t n_steps;
   uint64_t seed;
-  int32_t chains_per_block; /* SIMT engine: 0 = library default; else 8, 16 or 32 */
+  int32_t chains_per_block; /* SIMT engine: 0 = library default; else 8, 16 or 32.
+                               hierarchical engine: the tile shape, 32 (or 0) = 32 chains x
+                               64 rows, 16 = 16 chains x 128 rows */
   int32_t cluster_size;     /* tensor-core engine: CTAs per 128 chains (1,2,4,8); 0 = auto */
   int32_t launch;           /* hierarchical engine: 0 = persistent grid of resident CTAs taking
                                (instance, chain tile) items from a work counter, 1 = one CTA
