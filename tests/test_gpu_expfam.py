@@ -198,3 +198,55 @@ def test_klqp_auto_transform_false_gives_nan(cuda):
         for _ in range(inference.n_iter):
             info_dict = inference.update()
         assert bool(np.isnan(info_dict["loss"])) == expect_nan, (auto, info_dict)
+
+
+def test_expfam_dirichlet_largest_supported_size(cuda):
+    """A Dirichlet over 33 categories (the largest unconstrained dimension, 32):
+    one KLqp step's loss and gradients and one HMC iteration against the
+    oracle with the same draws."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Categorical, Dirichlet, Empirical, Normal
+    rng = np.random.default_rng(33)
+    Kc = 33
+    alpha = rng.uniform(0.5, 3.0, Kc).astype(np.float32)
+    data = rng.integers(0, Kc, 200)
+    stats = ef.sufficient_stats(ef.DIRICHLET, data, Kc)
+    K = Kc - 1
+    # KLqp
+    z = Dirichlet(alpha)
+    x = Categorical(probs=z, sample_shape=200)
+    mu0 = (rng.standard_normal(K) * 0.3).astype(np.float32)
+    rho0 = (rng.standard_normal(K) * 0.3 - 1.0).astype(np.float32)
+    qz = Normal(loc=ed.Variable(mu0), scale=ed.softplus(ed.Variable(rho0)))
+    inf = ed.KLqp({z: qz}, data={x: data})
+    S = 9
+    inf.initialize(n_samples=S, auto_transform=True)
+    eps = rng.standard_normal((S, K)).astype(np.float32)
+    loss, gmu, grho = inf.loss_and_gradients(eps)
+    l0, m0, r0 = ef.klqp_loss_and_grads(ef.DIRICHLET, alpha, stats, mu0, rho0, eps)
+    assert abs(loss - l0) <= 1e-5 * max(1.0, abs(l0))
+    np.testing.assert_allclose(gmu.cpu().numpy(), m0, rtol=1e-5, atol=1e-5 * np.abs(m0).max())
+    np.testing.assert_allclose(grho.cpu().numpy(), r0, rtol=1e-5, atol=1e-5 * np.abs(r0).max())
+    # HMC
+    z2 = Dirichlet(alpha)
+    x2 = Categorical(probs=z2, sample_shape=200)
+    C, L, step = 5, 3, 0.05
+    u0 = (rng.standard_normal((C, K)) * 0.3).astype(np.float32)
+    init = np.zeros((4, C, K), np.float32)
+    init[0] = u0
+    qz2 = Empirical(ed.Variable(init), n_chains=C)
+    hmc = ed.HMC({z2: qz2}, data={x2: data}, n_chains=C)
+    hmc.initialize(step_size=step, n_steps=L, n_print=0)
+    r = rng.standard_normal((1, C, K)).astype(np.float32)
+    u = rng.random((1, C))
+    hmc.run_iterations(1, r_override=torch.as_tensor(r, device=cuda),
+                       u_override=torch.as_tensor(u, device=cuda))
+
+    def lj_grad(U):
+        return (ef.log_joint(ef.DIRICHLET, alpha, stats, U),
+                ef.grad_log_joint(ef.DIRICHLET, alpha, stats, U))
+    lj0, g0 = lj_grad(u0)
+    out = ohmc.hmc_step(lj_grad, u0, g0, lj0, r[0], u[0], float(np.float32(step)), L,
+                        dtype=np.float32)
+    got = hmc._samples[0].cpu().numpy()
+    np.testing.assert_allclose(got, out["z"], rtol=1e-5, atol=1e-5 * np.abs(out["z"]).max())

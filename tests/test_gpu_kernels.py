@@ -180,6 +180,42 @@ def test_klqp_loss_and_gradients_parity(cuda, method, N, D, S):
     close(gmu2.cpu().numpy(), e_gmu2, tol)
 
 
+@pytest.mark.parametrize("method", [REPARAM_KL, REPARAM, SCORE])
+def test_klqp_normal_likelihood_with_scalings_parity(cuda, method):
+    """Bayesian linear regression (Normal likelihood, scale 0.7) with a data
+    scale of 2 on y, and for the analytic-KL estimator a KL scaling of 0.5 on w
+    (``kl_scaling``, klqp.py:105-113); loss and gradients against the FP64
+    oracle at the same draws, 1e-5."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Normal
+    N, D, S = 3000, 12, 5
+    rng = np.random.default_rng(40 + method)
+    X = rng.standard_normal((N, D)).astype(np.float32)
+    y = (X @ rng.standard_normal(D) + 0.3 + 0.7 * rng.standard_normal(N)).astype(np.float32)
+    m = f32(GLM(X, y, bias=True, lik=NORMAL, lik_scale=0.7, data_scale=2.0, prior_scale=1.3))
+    w = Normal(loc=ed.zeros(D), scale=ed.ones(D) * 1.3)
+    b = Normal(loc=0.0, scale=1.3)
+    yv = Normal(loc=ed.dot(X, w) + b, scale=0.7)
+    cls = {REPARAM_KL: ed.ReparameterizationKLKLqp, REPARAM: ed.ReparameterizationKLqp,
+           SCORE: ed.ScoreKLqp}[method]
+    inf = cls([w, b], data={yv: y})
+    kls = {w: 0.5} if method == REPARAM_KL else None
+    inf.initialize(n_samples=S, n_iter=10, n_print=0, scale={yv: 2.0}, kl_scaling=kls)
+    P = m.P
+    mu = (rng.standard_normal(P) * 0.3).astype(np.float32)
+    rho = (rng.standard_normal(P) * 0.3 - 1).astype(np.float32)
+    inf._mu.copy_(torch.as_tensor(mu))
+    inf._rho.copy_(torch.as_tensor(rho))
+    eps = rng.standard_normal((S, P)).astype(np.float32)
+    loss, gmu, grho = inf.loss_and_gradients(eps)
+    kl_scaling = np.concatenate([np.full(D, 0.5), [1.0]]) if method == REPARAM_KL else 1.0
+    e_loss, e_gmu, e_grho, _ = klqp_glm_loss_and_grads(m, mu, rho, eps, method,
+                                                       kl_scaling=kl_scaling)
+    assert abs(loss - e_loss) <= RTOL * abs(e_loss)
+    close(gmu.cpu().numpy(), e_gmu, RTOL)
+    close(grho.cpu().numpy(), e_grho, RTOL)
+
+
 def test_klqp_adam_trajectory_golden(cuda):
     """Three fused steps (analytic KL + TF Adam, default staircase lr) match
     the FP64 oracle trajectory in the golden fixture."""
