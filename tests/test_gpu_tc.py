@@ -181,3 +181,28 @@ def test_tc_public_api_engine(cuda):
     acc = inf.n_accept.float().mean().item() / T
     assert 0.3 < acc <= 1.0
     assert torch.isfinite(qw.params).all() and qw.params[-1].abs().sum() > 0
+
+
+def test_tiny_dataset_falls_back_to_the_simt_engine(cuda):
+    """40 rows and P = 51: one row tile cannot be split over the 4-CTA cluster
+    that P = 51 needs, so the tensor-core engine reports EDG_E_UNSUPPORTED
+    (engine='tc' raises) and the automatic choice takes the SIMT engine."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Empirical, Normal
+    X, y, _, _ = synthetic_logreg(40, 50, seed=9)
+
+    def model(engine):
+        w = Normal(loc=ed.zeros(50), scale=ed.ones(50))
+        b = Normal(loc=0.0, scale=1.0)
+        yv = Bernoulli(logits=ed.dot(X, w) + b)
+        T, C = 20, 16
+        qw = Empirical(ed.Variable(np.zeros((T, C, 50), np.float32)), n_chains=C)
+        qb = Empirical(ed.Variable(np.zeros((T, C), np.float32)), n_chains=C)
+        inf = ed.HMC({w: qw, b: qb}, data={yv: y}, n_chains=C)
+        inf.run(step_size=0.05, n_steps=3, engine=engine, n_print=0)
+        return inf, qw
+    with pytest.raises(Exception):
+        model("tc")
+    inf, qw = model("auto")
+    assert inf.engine == "simt" and inf.t == 20
+    assert torch.isfinite(qw.params).all() and qw.params[-1].abs().sum() > 0
