@@ -1408,39 +1408,57 @@ def run_sbn(args):
 
 def run_sgld(args):
     """SGLD (edward/inferences/sgld.py) on the 10,000 x 50 logistic regression with
-    4,096 chains: one batched log-joint gradient + update per iteration."""
+    4,096 chains.  Tensor-core engine: one launch per call of run_iterations,
+    each iteration one 3xTF32 gradient evaluation with the update fused in;
+    SIMT engine: a batched log-joint gradient + update kernel per iteration."""
     import numpy as np
     import torch
     import edward_gb300 as ed
     from edward_gb300.models import Bernoulli, Empirical, Normal
     X, y, _ = make_data()
     C = 4096
+    K = 10   # iterations per launch for the multi-iteration figure
     w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
     b = Normal(loc=0.0, scale=1.0)
     yv = Bernoulli(logits=ed.dot(X, w) + b)
-    T = args.steps + args.warmup
+    T = args.steps * (K + 1) + 2 * args.warmup + 4
     qw = Empirical(ed.Variable(np.zeros((T, C, N_FEAT), np.float32)), n_chains=C)
     qb = Empirical(ed.Variable(np.zeros((T, C), np.float32)), n_chains=C)
     inf = ed.SGLD({w: qw, b: qb}, data={yv: y}, n_chains=C)
-    inf.initialize(step_size=1e-4, n_print=0)
+    inf.initialize(step_size=1e-4, n_print=0, engine=args.engine)
     inf.run_iterations(args.warmup)
     torch.cuda.synchronize()
+    dev = torch.device("cuda")
     with ClockSampler(0) as clk:
-        ms = flush_timed(lambda: inf.run_iterations(1), args.steps, torch.device("cuda"))
+        ms = flush_timed(lambda: inf.run_iterations(1), args.steps, dev)
+        inf.run_iterations(args.warmup * K)
+        ms_k = flush_timed(lambda: inf.run_iterations(K), args.steps, dev) / K
     P = N_FEAT + 1
     flops = 4.0 * N_ROWS * P * C
+    tc = inf.engine == "tc"
+    if tc:
+        peak, src = tensor_peak(None if args.no_extras else measure_tf32_peak(dev))
+        kern = "hmc_glm_tc_kernel<SG> (tcgen05 3xTF32, the SGLD update fused in)"
+        launches = args.steps
+    else:
+        peak, src = None, None
+        kern = "glm_partial_kernel + glm_reduce_kernel + sgmcmc update (SIMT)"
+        launches = 3 * args.steps
+    ach = flops / (ms / 1e3) / 1e12
     line = {"metric": "SGLD chain-iterations/s (Bayesian logistic regression, batched chains)",
             "value": C / (ms / 1e3), "unit": "chain-iterations/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "data": "synthetic", "engine": inf.engine,
             "config": {"workload": "sgld_logreg_N10000_D50_C4096", "chains": C,
-                       "l2_flush": "256 MB write before each timed iteration, outside the events"},
-            "gpu_launches": 2 * args.steps,
-            "roofline": {"bound": "fp32", "achieved": flops / (ms / 1e3) / 1e12,
-                         "unit": "TFLOP/s", "traffic": None, "peak": None,
-                         "kernel": "glm_partial_kernel + glm_reduce_kernel + sgmcmc update (SIMT)",
-                         "algorithmic_flops_per_step": flops},
+                       "l2_flush": "256 MB write before each timed launch, outside the events"},
+            "multi_iteration": {"iterations_per_launch": K, "ms_per_iteration": ms_k,
+                                "value": C / (ms_k / 1e3)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "tensor" if tc else "fp32", "achieved": ach,
+                         "unit": "TFLOP/s", "traffic": None, "peak": peak,
+                         "frac": ach / peak if peak else None, "peak_source": src,
+                         "kernel": kern, "algorithmic_flops_per_step": flops},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0

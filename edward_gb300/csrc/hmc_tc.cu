@@ -113,6 +113,13 @@ struct TcArgs {
   const float* r_ovr;
   const double* u_ovr;
   double* ratio_out;
+  // stochastic-gradient MCMC (the SG instantiation): EDG_SGMCMC_*, SGHMC
+  // friction, the likelihood's data scale, the SGHMC velocity [C, P] and the
+  // noise override [n_iter, C, P]
+  int sg_method;
+  float friction, dscale;
+  float* v;
+  const float* noise;
 };
 
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
@@ -137,10 +144,10 @@ constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
 //     capped at e^40 so that a b stays below 2^116 (sigmoid changes by at most
 //     e^-40 absolute).  Rows beyond N are not masked: their X rows are zero,
 //     so their r only ever multiplies zeros in the backward MMA.
-template <bool LL, bool BERN>
+template <bool LL, bool BERN, bool SCALE = false>
 __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], const float (&y)[8],
                                                int nvalid, float inv_var, float lik_norm,
-                                               Kahan& kl) {
+                                               Kahan& kl, float rscale = 1.0f) {
   float r[8];
   if (LL) {
     float part = 0.0f;
@@ -189,6 +196,10 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
 #pragma unroll
     for (int k = 0; k < 8; ++k) r[k] = (y[k] - v[k]) * inv_var;
   }
+  if (SCALE) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r[k] *= rscale;  // the data scale of SG-MCMC
+  }
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     v[k] = __uint_as_float(__float_as_uint(r[k]) & 0xFFFFE000u);
@@ -196,6 +207,11 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
   }
 }
 
+// SG = false: HMC (leapfrog, Metropolis).  SG = true: SGLD / SGHMC, one
+// gradient evaluation per iteration, each iteration's update made with the
+// cached gradient of the current state in the pre phase and every proposal
+// kept (sgld.py:52-88, sghmc.py:58-102).
+template <bool SG>
 __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int PP = a.PP, P = a.P;
@@ -279,9 +295,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
 #pragma unroll
   for (int i = 0; i < kMaxEPT; ++i) {
     const int d = d0 + i;
-    zr[i] = (cvalid && i < EPT && d < P) ? zg[d] : 0.0f;
-    rr[i] = 0.0f;
-    gr[i] = 0.0f;
+    const bool ok = cvalid && i < EPT && d < P;
+    zr[i] = ok ? zg[d] : 0.0f;
+    rr[i] = (SG && ok && a.v) ? a.v[(size_t)cg * P + d] : 0.0f;  // SGHMC velocity
+    gr[i] = (SG && ok && a.cache_valid) ? gg[d] : 0.0f;
   }
   // prior loc and precision 1/scale^2 per coordinate (zero beyond P), and this
   // thread's share of the log-density normalising constant
@@ -320,13 +337,36 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     const int ee = e - (a.cache_valid ? 0 : 1);
     const int it = cache_eval ? 0 : ee / L;
     const int l = cache_eval ? 0 : ee % L;
-    const bool need_ll = cache_eval || l == L - 1;
+    const bool need_ll = !SG && (cache_eval || l == L - 1);
     const int64_t t = t0 + it;
     const uint32_t iter = (uint32_t)t;
 
     // ================= pre phase: position for this evaluation, broadcast as Z
     if (owner) {
-      if (!cache_eval) {
+      if (SG) {
+        if (!cache_eval) {
+          // the update of iteration t from the cached gradient of the current state
+          const bool sgld = a.sg_method == EDG_SGMCMC_SGLD;
+          const float lr = sgld ? a.step_size / powf((float)(t + 1), 0.55f) : a.step_size * 0.01f;
+          const float sq = sqrtf(sgld ? lr : lr * a.friction);
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) {
+            const int d = d0 + i;
+            const bool ok = cvalid && i < EPT && d < P;
+            float e = 0.0f;
+            if (ok)
+              e = a.noise ? a.noise[((size_t)it * a.C + cg) * P + d]
+                          : philox_normal(a.seed, 5u, iter, (uint32_t)cg, (uint32_t)d);
+            if (sgld) {
+              zr[i] = ok ? zr[i] + 0.5f * lr * gr[i] + sq * e : 0.0f;
+            } else {
+              const float vv = rr[i];
+              zr[i] = ok ? zr[i] + vv : 0.0f;
+              rr[i] = ok ? (1.0f - 0.5f * a.friction) * vv + lr * gr[i] + sq * e : 0.0f;
+            }
+          }
+        }
+      } else if (!cache_eval) {
         if (l == 0) {
           float kf = 0.0f;
 #pragma unroll
@@ -440,7 +480,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     } else if (warp == kBWarp) {
       // backward issuer, concurrent with the forward one: each warp's barrier
       // waits hide behind the other's MMAs in the tensor pipe
-      if (!cache_eval && l == L - 1) {
+      if (!SG && !cache_eval && l == L - 1) {
         // the Metropolis uniforms of this CTA's chains and their FP64 logs,
         // computed here (this warp mostly waits) rather than by the owners
         for (int c = lane; c < CPO; c += 32) {
@@ -567,7 +607,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             const float (&yh)[8] = *reinterpret_cast<const float (*)[8]>(&ye[8 * h]);
             const uint32_t col = 16 * qs + 8 * h;
             const int nv = nvalid - 8 * h;
-            residual_block<LL, BERN>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl);
+            residual_block<LL, BERN, SG>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl, a.dscale);
             tmem_st8(tl + COL_RHI(b) + col, v);
             tmem_st8(tl + COL_RLO(b) + col, lo);
           }
@@ -641,7 +681,27 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
       double lp = plogc + (double)lpf;
       if (need_ll)
         for (int o = TPC >> 1; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
-      if (cache_eval) {
+      if (SG) {
+        // the new state's gradient, cached for the next iteration's update;
+        // the new state itself is kept (every proposal is accepted)
+#pragma unroll
+        for (int i = 0; i < kMaxEPT; ++i) gr[i] = G[i];
+        if (cvalid) {
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) {
+            const int d = d0 + i;
+            if (i < EPT && d < P) {
+              gg[d] = G[i];
+              if (!cache_eval) {
+                if (!isfinite(zr[i])) atomicAdd(&a.state->nonfinite, 1u);
+                zg[d] = zr[i];
+                if (a.samples && t < a.T_cap) a.samples[((size_t)t * a.C + cg) * P + d] = zr[i];
+              }
+            }
+          }
+          if (!cache_eval && part == 0 && a.n_accept) a.n_accept[cg] += 1;
+        }
+      } else if (cache_eval) {
         if (cvalid) {
 #pragma unroll
           for (int i = 0; i < kMaxEPT; ++i)
@@ -703,6 +763,12 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     }
   }
 
+  if (SG && cvalid && a.v) {
+    // the SGHMC velocity for the next launch
+#pragma unroll
+    for (int i = 0; i < kMaxEPT; ++i)
+      if (i < EPT && d0 + i < P) a.v[(size_t)cg * P + d0 + i] = rr[i];
+  }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
@@ -791,6 +857,30 @@ extern "C" int edg_hmc_glm_tc_prepare(const edg_glm_t* model, void* tiles, size_
   return check_launch("prep_tiles_kernel");
 }
 
+// One launch of the tensor-core kernel: a cluster of R CTAs per 128 chains.
+template <bool SG>
+static int launch_tc(const TcArgs& a, int PP, int R, void* stream) {
+  const size_t sm = smem_bytes(PP);
+  int rc = set_max_dyn_smem(hmc_glm_tc_kernel<SG>, sm, "hmc_glm_tc_kernel");
+  if (rc) return rc;
+  const int nclusters = (a.C + kCT - 1) / kCT;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(nclusters * R);
+  lc.blockDim = dim3(kThreads);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = (cudaStream_t)stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = R;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&lc, hmc_glm_tc_kernel<SG>, a);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "hmc_glm_tc_kernel launch: %s", cudaGetErrorString(e));
+  return check_launch("hmc_glm_tc_kernel");
+}
+
 extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C,
                                   int32_t n_iter, const void* tiles, float* z, float* grad,
                                   double* lj, int32_t cache_valid, int32_t* n_accept,
@@ -844,23 +934,68 @@ extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, 
   a.r_ovr = r_override;
   a.u_ovr = u_override;
   a.ratio_out = ratio_out;
-  const size_t sm = smem_bytes(PP);
-  rc = set_max_dyn_smem(hmc_glm_tc_kernel, sm, "hmc_glm_tc_kernel");
+  a.sg_method = -1;
+  a.friction = 0.0f;
+  a.dscale = 1.0f;
+  a.v = nullptr;
+  a.noise = nullptr;
+  return launch_tc<false>(a, PP, R, stream);
+}
+
+extern "C" int edg_sgmcmc_glm_tc_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32_t C,
+                                     int32_t n_iter, const void* tiles, float* z, float* v,
+                                     float* grad, int32_t cache_valid, int32_t* n_accept,
+                                     edg_state_t* state, float* samples, int64_t T_cap,
+                                     const float* noise_override, void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
   if (rc) return rc;
-  const int nclusters = (C + kCT - 1) / kCT;
-  cudaLaunchConfig_t lc = {};
-  lc.gridDim = dim3(nclusters * R);
-  lc.blockDim = dim3(kThreads);
-  lc.dynamicSmemBytes = sm;
-  lc.stream = (cudaStream_t)stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = R;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  lc.attrs = attr;
-  lc.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&lc, hmc_glm_tc_kernel, a);
-  if (e != cudaSuccess) return fail(EDG_E_CUDA, "hmc_glm_tc_kernel launch: %s", cudaGetErrorString(e));
-  return check_launch("hmc_glm_tc_kernel");
+  EDG_REQUIRE(cfg && tiles, EDG_E_NULL, "cfg and tiles must not be NULL");
+  EDG_REQUIRE(z && grad && state, EDG_E_NULL, "z, grad and state must not be NULL");
+  EDG_REQUIRE(cfg->method == EDG_SGMCMC_SGLD || cfg->method == EDG_SGMCMC_SGHMC, EDG_E_VALUE,
+              "unknown SG-MCMC method %d", cfg->method);
+  EDG_REQUIRE(cfg->method != EDG_SGMCMC_SGHMC || v, EDG_E_NULL, "SGHMC needs the velocity v");
+  EDG_REQUIRE(cfg->step_size > 0.0f && cfg->friction >= 0.0f, EDG_E_VALUE,
+              "step_size must be positive and friction >= 0");
+  EDG_REQUIRE(C > 0 && n_iter >= 0, EDG_E_SHAPE, "C must be positive and n_iter >= 0");
+  EDG_REQUIRE(!samples || T_cap > 0, EDG_E_SHAPE, "T_cap must be positive when samples is given");
+  const int PP = padded_P(m.P);
+  EDG_REQUIRE(PP <= 64, EDG_E_UNSUPPORTED, "tensor-core SG-MCMC supports P <= 64 (got %d)", m.P);
+  if (n_iter == 0 && cache_valid) return EDG_OK;
+  const int ntiles = (m.N + kNR - 1) / kNR;
+  const int R = choose_R(PP, C, ntiles, 0);
+  EDG_REQUIRE(R > 0, EDG_E_UNSUPPORTED, "no cluster size fits P=%d with %d row tiles", m.P,
+              ntiles);
+  TcArgs a = {};
+  a.tiles = reinterpret_cast<const unsigned char*>(tiles);
+  a.y = m.y;
+  a.ntiles = ntiles;
+  a.N = m.N;
+  a.P = m.P;
+  a.PP = PP;
+  a.lik = m.lik;
+  a.zscale = m.lik == EDG_LIK_BERNOULLI ? -kLog2e : 1.0f;
+  a.inv_lik_var = m.inv_lik_var;
+  a.lik_norm = m.lik_norm;
+  a.prior_loc = m.prior_loc;
+  a.prior_scale = m.prior_scale;
+  a.C = C;
+  a.n_iter = n_iter;
+  a.n_steps = 1;  // one gradient evaluation per iteration
+  a.cache_valid = cache_valid;
+  a.step_size = cfg->step_size;
+  a.seed = cfg->seed;
+  a.z = z;
+  a.grad = grad;
+  a.lj = nullptr;
+  a.n_accept = n_accept;
+  a.state = state;
+  a.samples = samples;
+  a.T_cap = T_cap;
+  a.sg_method = cfg->method;
+  a.friction = cfg->friction;
+  a.dscale = cfg->data_scale;
+  a.v = cfg->method == EDG_SGMCMC_SGHMC ? v : nullptr;
+  a.noise = noise_override;
+  return launch_tc<true>(a, PP, R, stream);
 }

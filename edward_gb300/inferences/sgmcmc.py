@@ -3,20 +3,33 @@
 
 Same surface as the reference (``Empirical`` stores, ``initialize(step_size)``
 and ``initialize(step_size, friction)``, ``update`` / ``run``, ``n_accept``);
-the log joint uses ``scale`` as the reference's ``_log_joint`` does.  Each
-iteration is one batched log-joint gradient over all C chains plus a fused
-update kernel (``edg_sgmcmc_glm_run``).
+the log joint uses ``scale`` as the reference's ``_log_joint`` does.  Two
+engines: the tensor-core HMC kernel in its SG-MCMC form (one 3xTF32
+gradient evaluation per iteration, the update fused into its owner phase,
+``edg_sgmcmc_glm_tc_run``; P <= 64), and the SIMT form (the batched log-joint
+gradient plus a fused update kernel, ``edg_sgmcmc_glm_run``).  ``engine`` in
+``initialize`` picks one ("tc", "simt"); "auto" times both once per model
+shape.
 """
 import ctypes
 
 import numpy as np
 import torch
 
-from .. import _lib
+from .. import _lib, autotune
 from ..compile import compile_glm
 from ..ops import GLMDevice
 from ..util import next_seed
 from .monte_carlo import MonteCarlo
+
+
+def _check_override(t, numel, dtype, name):
+    """A per-iteration draw / output buffer must hold exactly the elements
+    the launch reads or writes."""
+    if t is None:
+        return
+    if not isinstance(t, torch.Tensor) or t.dtype != dtype or t.numel() != numel:
+        raise ValueError(f"{name} must be a {dtype} tensor of {numel} elements")
 
 
 class _SGMCMC(MonteCarlo):
@@ -56,14 +69,64 @@ class _SGMCMC(MonteCarlo):
         lib = _lib.load()
         self._ws_bytes = lib.edg_sgmcmc_glm_workspace_bytes(self._glm.ref(), C)
         self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
+        # tensor-core form: X re-laid into operand tiles once, and a cache of
+        # the current state's gradient carried between launches
+        self._g = torch.zeros(C, spec.P, dtype=torch.float32, device=dev)
+        self._cache_valid = 0
+        self._tiles = None
+        req = getattr(self, "_engine_req", "auto")
+        if req not in ("auto", "tc", "simt"):
+            raise ValueError("engine must be 'auto', 'tc' or 'simt'")
+        if req != "simt" and spec.P <= 64:
+            nbytes = lib.edg_hmc_glm_tc_tiles_bytes(self._glm.ref())
+            self._tiles = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+            _lib.call("edg_hmc_glm_tc_prepare", self._glm.ref(), _lib.ptr(self._tiles), nbytes,
+                      _lib.stream_ptr())
+        if req == "tc":
+            if self._tiles is None:
+                raise NotImplementedError("the tensor-core engine needs P <= 64")
+            self.engine = "tc"
+        elif req == "simt" or self._tiles is None:
+            self.engine = "simt"
+        else:
+            self.engine = self._autotune()
         self.train = self.update
         return self.train
 
+    def _run_engine(self, engine, n_iter, z, v, g, n_accept, state, samples, noise,
+                    cache_valid):
+        if engine == "tc":
+            _lib.call("edg_sgmcmc_glm_tc_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(self._tiles), _lib.ptr(z), _lib.ptr(v), _lib.ptr(g),
+                      cache_valid, _lib.ptr(n_accept), _lib.ptr(state), _lib.ptr(samples),
+                      samples.shape[0] if samples is not None else 0, _lib.ptr(noise),
+                      _lib.stream_ptr())
+        else:
+            _lib.call("edg_sgmcmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(z), _lib.ptr(v), _lib.ptr(n_accept),
+                      _lib.ptr(state), _lib.ptr(samples),
+                      samples.shape[0] if samples is not None else 0, _lib.ptr(noise),
+                      _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+
+    def _autotune(self):
+        """The faster engine for this model shape, one launch of each on
+        scratch copies of the state (cached per shape and device)."""
+        z, v, g = self._z.clone(), self._v.clone(), torch.zeros_like(self._g)
+        nacc = torch.zeros_like(self._n_accept)
+        st = _lib.new_state(self._device)
+
+        def run(engine):
+            z.copy_(self._z)
+            v.copy_(self._v)
+            self._run_engine(engine, 1, z, v, g, nacc, st, None, None, 0)
+        spec = self._spec
+        key = f"N{spec.N}_P{spec.P}_C{self.C}_m{self._method}"
+        return autotune.choose("sgmcmc_engine", key, ["tc", "simt"], run)
+
     def _launch(self, n_iter, noise=None):
-        _lib.call("edg_sgmcmc_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
-                  int(n_iter), _lib.ptr(self._z), _lib.ptr(self._v), _lib.ptr(self._n_accept),
-                  _lib.ptr(self._state), _lib.ptr(self._samples), self._samples.shape[0],
-                  _lib.ptr(noise), _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+        self._run_engine(self.engine, n_iter, self._z, self._v, self._g, self._n_accept,
+                         self._state, self._samples, noise, self._cache_valid)
+        self._cache_valid = 1
 
     def update(self, feed_dict=None):
         """One iteration for every chain; returns ``{'t', 'accept_rate'}``
@@ -91,6 +154,7 @@ class _SGMCMC(MonteCarlo):
         overrides the Philox draws."""
         if noise is not None:
             noise = torch.as_tensor(noise, dtype=torch.float32, device=self._device).contiguous()
+            _check_override(noise, k * self.C * self._spec.P, torch.float32, "noise")
         self._launch(k, noise)
 
     @property
@@ -104,6 +168,7 @@ class _SGMCMC(MonteCarlo):
         self._n_accept.zero_()
         self._z.copy_(self._samples[0])
         self._v.zero_()
+        self._cache_valid = 0
 
 
 class SGLD(_SGMCMC):
@@ -111,8 +176,9 @@ class SGLD(_SGMCMC):
     lr = step_size / (t + 1)^0.55, z <- z + lr/2 grad log p + N(0, lr)."""
     _method = _lib.SGMCMC_SGLD
 
-    def initialize(self, step_size=0.25, *args, **kwargs):
+    def initialize(self, step_size=0.25, *args, engine="auto", **kwargs):
         self.step_size = step_size
+        self._engine_req = engine
         return super().initialize(*args, **kwargs)
 
 
@@ -122,9 +188,10 @@ class SGHMC(_SGMCMC):
     + N(0, lr * friction)."""
     _method = _lib.SGMCMC_SGHMC
 
-    def initialize(self, step_size=0.25, friction=0.1, *args, **kwargs):
+    def initialize(self, step_size=0.25, friction=0.1, *args, engine="auto", **kwargs):
         self.step_size = step_size
         self.friction = friction
+        self._engine_req = engine
         return super().initialize(*args, **kwargs)
 
 
@@ -208,6 +275,9 @@ class MetropolisHastings(MonteCarlo):
 
     def run_iterations(self, k, e_override=None, u_override=None, ratio_out=None):
         """k iterations without host synchronisation (optional draws / ratios)."""
+        _check_override(e_override, k * self.C * self._spec.P, torch.float32, "e_override")
+        _check_override(u_override, k * self.C, torch.float64, "u_override")
+        _check_override(ratio_out, k * self.C, torch.float64, "ratio_out")
         self._launch(k, e_override, u_override, ratio_out)
 
     def reset(self):

@@ -510,6 +510,23 @@ int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, int32_t C, 
                        double* moments, const float* r_override, const double* u_override,
                        double* ratio_out, void* stream);
 
+/* ---------------------------------------------------------------- SG-MCMC, tensor cores
+ * Same contract as edg_sgmcmc_glm_run, with the per-iteration gradient
+ * computed by the tensor-core kernel above (one 3xTF32 evaluation per
+ * iteration, the SGLD / SGHMC update fused into the kernel's owner phase).
+ * Requires P = D + bias <= 64; `tiles` as for edg_hmc_glm_tc_run.  grad [C, P]
+ * carries the gradient of the current state between calls: with
+ * cache_valid = 0 it is rebuilt by one extra evaluation before the first
+ * iteration; every call leaves it valid for the state it returns.  v [C, P] is
+ * the SGHMC velocity (unused by SGLD).
+ * Replaces the same reference code as edg_sgmcmc_glm_run (sgld.py:52-88,
+ * sghmc.py:58-102). */
+int edg_sgmcmc_glm_tc_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32_t C,
+                          int32_t n_iter, const void* tiles, float* z, float* v, float* grad,
+                          int32_t cache_valid, int32_t* n_accept, edg_state_t* state,
+                          float* samples, int64_t T_cap, const float* noise_override,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,3 +125,98 @@ def test_mh_normal_normal_posterior(cuda, proposal):
     assert inference.t == 2000 and inference.n_accept > 0.1
     inference.reset()
     assert inference.t == 0 and inference.n_accept == 0
+
+
+def _logreg_scaled(ed, C, N, D, seed, dscale, lik="bernoulli"):
+    from edward_gb300.models import Bernoulli, Empirical, Normal
+    if lik == "bernoulli":
+        X, y, _, _ = oglm.synthetic_logreg(N, D, seed=seed)
+    else:
+        rng = np.random.default_rng(seed)
+        X = rng.standard_normal((N, D)).astype(np.float32)
+        y = (X @ rng.standard_normal(D) + 0.3 * rng.standard_normal(N)).astype(np.float32)
+    w = Normal(loc=ed.zeros(D), scale=ed.ones(D))
+    b = Normal(loc=0.0, scale=1.0)
+    eta = ed.dot(X, w) + b
+    yv = Bernoulli(logits=eta) if lik == "bernoulli" else Normal(loc=eta, scale=0.7)
+    rng = np.random.default_rng(seed + 1)
+    w0 = (rng.standard_normal((C, D)) * 0.1).astype(np.float32)
+    qw = Empirical(ed.Variable(np.repeat(w0[None], 20, 0)), n_chains=C)
+    qb = Empirical(ed.Variable(np.zeros((20, C), np.float32)), n_chains=C)
+    kw = {} if lik == "bernoulli" else dict(lik=oglm.NORMAL, lik_scale=0.7)
+    model = oglm.GLM(X, y, bias=True, data_scale=dscale, **kw)
+    return ({w: qw, b: qb}, {yv: y}, {yv: dscale}, model,
+            np.concatenate([w0, np.zeros((C, 1))], 1))
+
+
+@pytest.mark.parametrize("method", ["sgld", "sghmc"])
+@pytest.mark.parametrize("given_noise", [True, False])
+@pytest.mark.parametrize("shape", [(400, 5, 6, 1.0, "bernoulli"), (3000, 20, 200, 2.5, "bernoulli"),
+                                   (1500, 63, 130, 0.5, "normal")])
+def test_sgmcmc_tensor_core_matches_oracle(cuda, method, given_noise, shape):
+    """The tensor-core engine (one 3xTF32 gradient evaluation per iteration,
+    the update fused into the kernel) against the FP64 oracle with the same
+    draws: several clusters of 128 chains (200 and 130 chains: a partial
+    last cluster), P up to 64, the data scale, and the iterations split over
+    two launches so the cached gradient carries over."""
+    import edward_gb300 as ed
+    N, D, C, dscale, lik = shape
+    n1, n2 = 2, 3
+    n = n1 + n2
+    lv, data, scale, model, z0 = _logreg_scaled(ed, C, N, D, 3, dscale, lik)
+    cls = ed.SGLD if method == "sgld" else ed.SGHMC
+    inf = cls(lv, data=data, n_chains=C)
+    kw = dict(step_size=1e-3) if method == "sgld" else dict(step_size=0.05, friction=0.2)
+    inf.initialize(n_print=0, scale=scale, engine="tc", **kw)
+    assert inf.engine == "tc"
+    P = z0.shape[1]
+    noise = np.random.default_rng(1).standard_normal((n, C, P)).astype(np.float32)
+    inf.run_iterations(n1, noise=noise[:n1] if given_noise else None)
+    inf.run_iterations(n2, noise=noise[n1:] if given_noise else None)
+    got = inf._samples[:n].cpu().numpy()
+    noise_fn = (lambda t: noise[t]) if given_noise else None
+    ref, _, _ = sgmcmc.run(model, z0, n, kw["step_size"], method, kw.get("friction", 0.1),
+                           seed=inf._cfg.seed, noise_fn=noise_fn)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+    assert inf.t == n
+    assert np.all(inf.n_accept.cpu().numpy() == n)
+
+
+@pytest.mark.parametrize("method", ["sgld", "sghmc"])
+def test_sgmcmc_engines_agree(cuda, method):
+    """The tensor-core and SIMT engines draw the same Philox noise: the same
+    chains to FP32 rounding over 20 iterations."""
+    import edward_gb300 as ed
+    C, n = 256, 20
+    out = {}
+    for engine in ("tc", "simt"):
+        ed.set_seed(7)
+        lv, data, scale, model, z0 = _logreg_scaled(ed, C, 2000, 12, 5, 1.0)
+        cls = ed.SGLD if method == "sgld" else ed.SGHMC
+        inf = cls(lv, data=data, n_chains=C)
+        kw = dict(step_size=1e-3) if method == "sgld" else dict(step_size=0.05, friction=0.2)
+        inf.initialize(n_print=0, engine=engine, **kw)
+        assert inf.engine == engine
+        inf.run_iterations(n)
+        out[engine] = inf._samples[:n].cpu().numpy()
+    np.testing.assert_allclose(out["tc"], out["simt"], rtol=1e-5,
+                               atol=1e-5 * np.abs(out["simt"]).max())
+
+
+def test_sgmcmc_tensor_core_reset_rebuilds_cache(cuda):
+    """reset() restarts t at 0 from params[0] (the reference keeps the
+    Empirical's values and re-initialises t and n_accept only): the cached
+    gradient belongs to the last state, so it is rebuilt for params[0]."""
+    import edward_gb300 as ed
+    C, n = 64, 4
+    lv, data, scale, model, z0 = _logreg_scaled(ed, C, 800, 8, 2, 1.0)
+    inf = ed.SGLD(lv, data=data, n_chains=C)
+    inf.initialize(n_print=0, step_size=1e-3, engine="tc")
+    inf.run_iterations(n)
+    start = inf._samples[0].cpu().numpy().astype(np.float64)
+    inf.reset()
+    inf.run_iterations(n)
+    got = inf._samples[:n].cpu().numpy()
+    ref, _, _ = sgmcmc.run(model, start, n, 1e-3, "sgld", seed=inf._cfg.seed)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+    assert inf.t == n
