@@ -1028,10 +1028,11 @@ def hier_data(I=2048, seed=0):
 
 def run_hier(args):
     """All 2,048 instances x 64 chains, 10 leapfrog steps per iteration, one
-    launch per iteration (edg_hmc_hier_run), timed for both launch forms (the
-    persistent work-queue grid and one CTA per (instance, chain tile)) and both
-    tile shapes (32 chains x 64 rows, 16 chains x 128 rows); the fastest pair
-    is then replayed from a CUDA graph, which is the value."""
+    launch per iteration, timed for both engines (edg_hmc_hier_tc_run: tcgen05
+    3xTF32, 64 chains x 128 rows per tile; edg_hmc_hier_run: SIMT in two tile
+    shapes, 32 chains x 64 rows and 16 chains x 128 rows) and both launch forms
+    (the persistent work-queue grid and one CTA per (instance, chain tile));
+    the fastest form is then replayed from a CUDA graph, which is the value."""
     import ctypes
     import numpy as np
     import torch
@@ -1049,10 +1050,10 @@ def run_hier(args):
     st = _lib.new_state(dev)
     cfg = _lib.EdgHMC()
     cfg.step_size, cfg.n_steps, cfg.seed = 0.01, L, 1
-    state = {"cache": 0}
+    state = {"cache": 0, "fn": "edg_hmc_hier_run"}
 
     def step():
-        _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
+        _lib.call(state["fn"], hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
                   _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), state["cache"], _lib.ptr(nacc),
                   _lib.ptr(st), None, 0, None, None, None, None, _lib.stream_ptr())
         state["cache"] = 1
@@ -1067,17 +1068,23 @@ def run_hier(args):
         return a.elapsed_time(b) / k
 
     forms, shape = {}, {}
-    for launch, lname in ((0, "persistent"), (1, "one_cta_per_item")):
-        for ct in (32, 16):
-            name = f"{lname}_{ct}x{2048 // ct}"
-            cfg.launch, cfg.chains_per_block = launch, ct
-            for _ in range(args.warmup):
-                step()
-            torch.cuda.synchronize()
-            forms[name] = timed(step, args.steps)
-            shape[name] = (launch, ct)
+    tc_ok = hd.max_D <= 128
+    for engine in (("tc", "simt") if tc_ok else ("simt",)):
+        for launch, lname in ((0, "persistent"), (1, "one_cta_per_item")):
+            for ct in ((64,) if engine == "tc" else (32, 16)):
+                rows = 128 if engine == "tc" else 2048 // ct
+                name = f"{engine}_{lname}_{ct}x{rows}"
+                cfg.launch, cfg.chains_per_block = launch, (ct if engine == "simt" else 0)
+                state["fn"] = "edg_hmc_hier_tc_run" if engine == "tc" else "edg_hmc_hier_run"
+                for _ in range(args.warmup):
+                    step()
+                torch.cuda.synchronize()
+                forms[name] = timed(step, args.steps)
+                shape[name] = (engine, launch, ct)
     best = min(forms, key=forms.get)
-    cfg.launch, cfg.chains_per_block = shape[best]
+    engine, cfg.launch, ct = shape[best]
+    cfg.chains_per_block = ct if engine == "simt" else 0
+    state["fn"] = "edg_hmc_hier_tc_run" if engine == "tc" else "edg_hmc_hier_run"
     graph = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -1087,9 +1094,11 @@ def run_hier(args):
     torch.cuda.current_stream().wait_stream(s)
     graph.replay()
     torch.cuda.synchronize()
+    nacc.zero_()
     with ClockSampler(0) as clk:
         ms = timed(graph.replay, args.steps)
     work = float((hd.Ns.astype(np.int64) * hd.Ds).sum())
+    x_passes = 1 if engine == "tc" else C // ct   # X streams per gradient evaluation
     flops = 4.0 * work * C * L
     peak, src = tensor_peak(measure_tf32_peak(torch.device("cuda")))
     ach = flops / (ms / 1e3) / 1e12
@@ -1105,12 +1114,16 @@ def run_hier(args):
             "gpu_launches": args.steps,
             "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                          "frac": ach / peak,
-                         "traffic": read_traffic_file("hmc_hier_kernel_ragged_I2048.txt")
-                         if hd.I == 2048 else None,
-                         "kernel": "hmc_hier_kernel<%d> (SIMT FP32)" % shape[best][1],
+                         "traffic": read_traffic_file(
+                             "hmc_hier_tc_kernel_ragged_I2048.txt" if engine == "tc"
+                             else "hmc_hier_kernel_ragged_I2048.txt") if hd.I == 2048 else None,
+                         "kernel": ("hmc_hier_tc_kernel (tcgen05 3xTF32, 64 chains x 128 rows)"
+                                    if engine == "tc" else
+                                    "hmc_hier_kernel<%d> (SIMT FP32)" % ct),
                          "peak_source": src, "algorithmic_flops_per_launch": flops,
-                         "x_stream_GBs": 2 * L * work * 4 / (ms / 1e3) / 1e9},
-            "accept_rate": float(nacc.sum().item()) / (n * (2 * args.warmup + 3 * args.steps + 1)),
+                         "x_stream_GBs": x_passes * L * work * 4 / (ms / 1e3) / 1e9},
+            "engine": engine,
+            "accept_rate": float(nacc.sum().item()) / (n * args.steps),
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0

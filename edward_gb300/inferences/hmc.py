@@ -189,16 +189,24 @@ class HMC(MonteCarlo):
         self._graphs = {}
         best = self._autotune_hier()
         cfg.launch, cfg.chains_per_block = best & 1, 16 if best & 2 else 32
+        self.hier_engine = "tc" if best & 4 else "simt"
+        self._hier_fn = "edg_hmc_hier_tc_run" if best & 4 else "edg_hmc_hier_run"
         self.train = self.update
         return self.train
 
     def _autotune_hier(self):
-        """Launch form (persistent work-queue grid or one CTA per (instance,
-        chain tile)) and tile shape (32 chains x 64 rows or 16 chains x 128
-        rows) of the ragged batch, timed on scratch copies of the state and
-        cached per model shape.  Candidate c encodes launch = c & 1 and 16
-        chains per block when c & 2."""
+        """Engine, launch form (persistent work-queue grid or one CTA per
+        (instance, chain tile)) and, for the SIMT engine, the tile shape (32
+        chains x 64 rows or 16 chains x 128 rows) of the ragged batch, timed on
+        scratch copies of the state and cached per model shape.  Candidate c
+        encodes launch = c & 1, 16 chains per block when c & 2, and the
+        tensor-core engine (64 chains x 128 rows, max_D <= 128) when c & 4."""
         hd, C = self._hier, self.C
+        req = self._engine_req
+        tc_ok = hd.max_D <= 128
+        if req == "tc" and not tc_ok:
+            raise NotImplementedError("the tensor-core hierarchical engine needs max_D <= 128")
+        cands = ([0, 1, 2, 3] if req != "tc" else []) + ([4, 5] if tc_ok and req != "simt" else [])
         z = self._z.clone()
         g = torch.zeros_like(self._g)
         lj = torch.zeros_like(self._lj)
@@ -209,13 +217,14 @@ class HMC(MonteCarlo):
             cfg.launch, cfg.chains_per_block = c & 1, 16 if c & 2 else 32
             z.copy_(self._z)
             st = _lib.new_state(self._device)
-            _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
+            fn = "edg_hmc_hier_tc_run" if c & 4 else "edg_hmc_hier_run"
+            _lib.call(fn, hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
                       _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st), None, 0,
                       None, None, None, None, _lib.stream_ptr())
 
         work = int((hd.Ns.astype(np.int64) * hd.Ds).sum())
         key = f"I{hd.I}_work{work}_maxD{hd.max_D}_C{C}_L{self.n_steps}"
-        return autotune.choose("hmc_hier_shape", key, [0, 1, 2, 3], run)
+        return autotune.choose("hmc_hier_engine_shape", key, cands, run)
 
     def _build_expfam(self):
         """Chains of the unconstrained latent u (FP32, as the reference's
@@ -279,7 +288,7 @@ class HMC(MonteCarlo):
             return
         if self.engine == "hier":
             def launch():
-                _lib.call("edg_hmc_hier_run", self._hier.ref(), ctypes.byref(self._cfg), self.C,
+                _lib.call(self._hier_fn, self._hier.ref(), ctypes.byref(self._cfg), self.C,
                           int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),
                           _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
                           _lib.ptr(self._n_accept), _lib.ptr(self._state),

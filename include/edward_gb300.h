@@ -492,6 +492,17 @@ int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, i
                      double* moments, const float* r_override, const double* u_override,
                      double* ratio_out, void* stream);
 
+/* Same contract as edg_hmc_hier_run (same draws, state layout and results to
+ * FP32 rounding), with every gradient evaluation computed as tcgen05 3xTF32
+ * GEMMs: one CTA per (instance, 64 chains), X read once per evaluation for
+ * all 64 chains.  Requires max_D <= 128; cfg->chains_per_block is ignored. */
+int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
+                        const int32_t* order, float* z, float* grad, double* lj,
+                        int32_t cache_valid, int32_t* n_accept, edg_state_t* state,
+                        float* samples, int64_t T_cap, double* moments,
+                        const float* r_override, const double* u_override, double* ratio_out,
+                        void* stream);
+
 /* ---------------------------------------------------------------- HMC, tensor cores
  * Same contract as edg_hmc_glm_run, computed with tcgen05 3xTF32 GEMMs:
  * one thread-block cluster per 128 chains, the cluster's CTAs splitting the

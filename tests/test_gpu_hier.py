@@ -18,7 +18,8 @@ def _instances(seed=3):
     return Xs + X2, ys + y2
 
 
-def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launch=0, ct=32):
+def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launch=0, ct=32,
+         engine="simt"):
     from edward_gb300 import _lib
     cuda = z0.device
     cfg = _lib.EdgHMC()
@@ -31,7 +32,8 @@ def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launc
     nacc = torch.zeros(n, dtype=torch.int32, device=cuda)
     st = _lib.new_state(cuda)
     ratio = torch.zeros(max(n_iter, 1), n, dtype=torch.float64, device=cuda)
-    _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(hd.order),
+    fn = "edg_hmc_hier_tc_run" if engine == "tc" else "edg_hmc_hier_run"
+    _lib.call(fn, hd.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(hd.order),
               _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, _lib.ptr(nacc), _lib.ptr(st),
               _lib.ptr(samples), samples.shape[0] if samples is not None else 0, None,
               _lib.ptr(r), _lib.ptr(u), _lib.ptr(ratio), _lib.stream_ptr())
@@ -39,15 +41,19 @@ def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launc
     return z, g, lj, nacc, ratio, _lib.read_state(st)
 
 
-@pytest.mark.parametrize("ct", [32, 16])
-def test_hier_iteration_parity(cuda, ct):
-    """One iteration of every instance against the oracle, for both tile
-    shapes (32 chains x 64 rows, 16 chains x 128 rows)."""
+@pytest.mark.parametrize("engine,ct,C", [("simt", 32, 40), ("simt", 16, 40), ("tc", 0, 40),
+                                         ("tc", 0, 100)])
+def test_hier_iteration_parity(cuda, engine, ct, C):
+    """One iteration of every instance against the oracle: the SIMT engine in
+    both tile shapes (32 chains x 64 rows, 16 chains x 128 rows) and the
+    tensor-core engine (64 chains x 128 rows; 100 chains = a full and a
+    partial chain tile per instance).  Instances span D = 8..40 and D = 128
+    over 3 row tiles (the last one partial)."""
     from edward_gb300.ops import HierDevice
     Xs, ys = _instances()
     kw = dict(mu_loc=0.1, mu_scale=1.2, tau_scale=0.8)
     hd = HierDevice(Xs, ys, **kw)
-    C, L, step = 40, 3, 0.01
+    L, step = 3, 0.01
     SP = hd.SP
     rng = np.random.default_rng(0)
     z0 = np.zeros((hd.I * C, SP), np.float32)
@@ -60,7 +66,7 @@ def test_hier_iteration_parity(cuda, ct):
     u = rng.random((1, hd.I * C))
     z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
                                      r=torch.as_tensor(r0, device=cuda),
-                                     u=torch.as_tensor(u, device=cuda), ct=ct)
+                                     u=torch.as_tensor(u, device=cuda), ct=ct, engine=engine)
     assert st.t == 1
     zk, rk, ak = z.cpu().numpy(), ratio.cpu().numpy()[0], nacc.cpu().numpy().astype(bool)
     for i, (X, y) in enumerate(zip(Xs, ys)):
@@ -80,7 +86,8 @@ def test_hier_iteration_parity(cuda, ct):
                                    atol=1e-5 * np.abs(exp).max())
 
 
-def test_hier_in_kernel_rng_two_iterations(cuda):
+@pytest.mark.parametrize("engine", ["simt", "tc"])
+def test_hier_in_kernel_rng_two_iterations(cuda, engine):
     from edward_gb300.ops import HierDevice
     Xs, ys = _instances(seed=9)
     hd = HierDevice(Xs, ys)
@@ -93,7 +100,7 @@ def test_hier_in_kernel_rng_two_iterations(cuda):
         z0[i * C:(i + 1) * C, cols(X.shape[1])] = rng.standard_normal((C, X.shape[1] + 2)) * 0.1
     samples = torch.zeros(T, hd.I * C, SP, device=cuda)
     z, _, _, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), T, step, L,
-                                    seed=seed, samples=samples)
+                                    seed=seed, samples=samples, engine=engine)
     assert st.t == T
     sk = samples.cpu().numpy()
     rk = ratio.cpu().numpy()
@@ -145,7 +152,8 @@ def test_hier_public_api_ragged_batch(cuda):
         assert np.all(np.isfinite(wm[i, :D])) and np.all(wm[i, D:] == 0)
 
 
-def test_hier_launch_forms_agree(cuda):
+@pytest.mark.parametrize("engine", ["simt", "tc"])
+def test_hier_launch_forms_agree(cuda, engine):
     """The persistent work-queue grid and the one-CTA-per-item grid run the
     same arithmetic per (instance, chain tile): identical chains, ratios and
     acceptance counts; t advances and the work counter is left at 0."""
@@ -159,7 +167,7 @@ def test_hier_launch_forms_agree(cuda):
     for launch in (0, 1):
         samples = torch.zeros(T, hd.I * C, hd.SP, device=cuda)
         z, g, lj, nacc, ratio, st = _run(hd, C, z0, T, 0.01, 4, seed=5, samples=samples,
-                                         launch=launch)
+                                         launch=launch, engine=engine)
         assert st.t == T and st.done == 0 and st.reserved == 0
         outs.append((samples.cpu().numpy(), lj.cpu().numpy(), nacc.cpu().numpy(),
                      ratio.cpu().numpy()))
@@ -203,3 +211,31 @@ def test_hier_graph_replay_matches_direct_launch(cuda):
                      inf.n_accept.cpu().numpy()))
     for a, b in zip(runs[0], runs[1]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_hier_engines_agree(cuda):
+    """The tensor-core and SIMT engines draw the same Philox momenta and
+    uniforms: over 4 iterations of 100 chains per instance the log acceptance
+    ratios agree to 1e-5 of the log joint, and the kept states agree wherever
+    both engines took the same decisions (all of them, away from ties)."""
+    from edward_gb300.ops import HierDevice
+    Xs, ys = _instances(seed=13)
+    hd = HierDevice(Xs, ys)
+    C, T = 100, 4
+    z0 = torch.as_tensor(np.random.default_rng(4).standard_normal((hd.I * C, hd.SP))
+                         .astype(np.float32) * 0.1, device=cuda)
+    outs = {}
+    for engine in ("simt", "tc"):
+        samples = torch.zeros(T, hd.I * C, hd.SP, device=cuda)
+        z, g, lj, nacc, ratio, st = _run(hd, C, z0, T, 0.01, 4, seed=3, samples=samples,
+                                         engine=engine)
+        assert st.t == T and st.error == 0
+        outs[engine] = (samples.cpu().numpy(), lj.cpu().numpy(), ratio.cpu().numpy(),
+                        nacc.cpu().numpy())
+    s_a, lj_a, r_a, n_a = outs["simt"]
+    s_b, lj_b, r_b, n_b = outs["tc"]
+    scale = max(np.abs(lj_a).max(), 1.0)
+    np.testing.assert_allclose(r_b, r_a, rtol=0, atol=1e-5 * scale)
+    if np.array_equal(n_a, n_b):
+        np.testing.assert_allclose(s_b, s_a, rtol=1e-5, atol=1e-5 * np.abs(s_a).max())
+        np.testing.assert_allclose(lj_b, lj_a, rtol=0, atol=1e-5 * scale)
