@@ -1053,7 +1053,11 @@ def run_hier(args):
     state = {"cache": 0, "fn": "edg_hmc_hier_run"}
 
     def step():
-        _lib.call(state["fn"], hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
+        lead = (_lib.ptr(hd.order),)
+        if state["fn"] == "edg_hmc_hier_tc_run":
+            tiles, toff = hd.tc_tiles()
+            lead = lead + (_lib.ptr(tiles), _lib.ptr(toff))
+        _lib.call(state["fn"], hd.ref(), ctypes.byref(cfg), C, 1, *lead,
                   _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), state["cache"], _lib.ptr(nacc),
                   _lib.ptr(st), None, 0, None, None, None, None, _lib.stream_ptr())
         state["cache"] = 1

@@ -123,10 +123,12 @@ _SIGS = {
                                    c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
                                    c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p]),
+    "edg_hmc_hier_tc_tile_offsets": (c_int64, [c_void_p, c_void_p, c_int32, c_void_p]),
+    "edg_hmc_hier_tc_prepare": (c_int32, [ctypes.POINTER(EdgHier), c_void_p, c_void_p, c_void_p]),
     "edg_hmc_hier_tc_run": (c_int32, [ctypes.POINTER(EdgHier), ctypes.POINTER(EdgHMC), c_int32,
-                                      c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
-                                      c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
-                                      c_void_p, c_void_p, c_void_p]),
+                                      c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_int64,
+                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "edg_gemm_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32]),
     "edg_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32,
                            c_int64, c_void_p, c_int32, c_int64, c_void_p, c_int32, c_int64, c_int32,

@@ -3,7 +3,7 @@
 // (edg_hmc_hier_run); every gradient evaluation is computed as tcgen05
 // 3xTF32 GEMMs (hi*hi + hi*lo + lo*hi, FP32 accumulation in TMEM).
 //
-// One CTA per (instance, 64 chains), 256 threads, all 512 TMEM columns:
+// One CTA per (instance, 64 chains), 512 threads, all 512 TMEM columns:
 //   XF  [lanes = 128 rows of a tile, columns = features]   hi at 0, lo at 128
 //   XT  [lanes = features, columns = 64 rows of a half]     hi at 256, lo at 320
 //   ETA [lanes = rows, columns = 64 chains]                 at 384 (forward accumulator)
@@ -11,25 +11,29 @@
 // tf32 operands must be K-major (a transposed shared-memory operand reads as
 // zeros), so X enters the tensor core in both orientations, and both come
 // from TMEM (the A operand of the TS form).  X is read from HBM as one fp32
-// plane, once per evaluation for all 64 chains: coalesced warp loads (32
-// consecutive features of one row) give XT directly (one lane per feature)
-// and, through a padded shared staging buffer, XF (one lane per row); the
-// hi/lo split is made in registers.  Shared memory holds the B operands only:
-// the positions W [64 chains, K = features] and the residuals R [64 chains,
+// plane, once per evaluation for all 64 chains.  edg_hmc_hier_tc_prepare
+// re-lays each X_i once into 128-row tiles with a row pitch of Dp_i + 1
+// floats (Dp_i = D_i rounded up to 8; zero beyond N_i and D_i), so that each
+// 64-row half of a tile is one contiguous bulk copy (issued by one thread,
+// completed on an mbarrier) into a shared staging half whose odd pitch lets
+// one thread per feature (XT) and one thread per row (XF) read it without
+// bank conflicts; the hi/lo split is made in registers.  The copies of the
+// next tile run under the current tile's MMAs.  Shared memory holds the
+// staging halves and the B operands: the
+// positions W [64 chains, K = features] and the residuals R [64 chains,
 // K = 128 rows], hi and lo planes in the no-swizzle K-major core-matrix layout
 // with 144-byte strides (bank-conflict-free stores from either side).
 //
-// Per 128-row tile:
-//   rows 0-63    -> XT (half 0) and staging -> XF rows 0-63
-//   rows 64-127  -> staging -> XF rows 64-127
+// Per 128-row tile (staging halves A = rows 0-63, B = rows 64-127):
+//   A -> XT (half 0); A, B -> XF; then A takes the next tile's rows 0-63
 //   forward      ETA = XF W^T                      (3 x Dp/8 TS MMAs, M = 128, N = 64)
-//   epilogue     one thread per row and 32 chains: r = y - sigmoid(eta), the
+//   epilogue     one thread per row and 16 chains: r = y - sigmoid(eta), the
 //                per-row log-likelihood; R <- r (hi, lo)
 //   backward     GT += XT R^T over rows 0-63 (24 TS MMAs, M = 128 features)
-//   rows 64-127  -> XT (half 1); backward over rows 64-127
+//   B -> XT (half 1); B takes the next tile's rows 64-127; backward over rows 64-127
 // After the last tile each thread reads the likelihood gradient of one
-// feature for 32 chains from GT, the layout the leapfrog state is kept in
-// (registers: the feature of the thread's TMEM lane, 32 chains).  The
+// feature for 16 chains from GT, the layout the leapfrog state is kept in
+// (registers: the feature of the thread's TMEM lane, 16 chains).  The
 // hierarchical prior, the softplus Jacobian, leapfrog and the FP64 Metropolis
 // test follow hier.cu; per-chain sums over features and rows are warp
 // reduce-scatters plus an FP64 sum over the four lane quadrants.
@@ -42,17 +46,22 @@ namespace edg {
 namespace htc {
 using namespace ptx;
 
-constexpr int kT = 256;
+constexpr int kT = 512;      // 16 warps: four per TMEM lane quadrant
 constexpr int kRows = 128;   // rows per tile (the forward M)
 constexpr int kCh = 64;      // chains per CTA (the MMA N)
 constexpr int kDmax = 128;   // features per instance (the backward M)
+constexpr int kHW = kT / 128;    // warps per lane quadrant (the chain slices)
+constexpr int kCPT = kCh / kHW;  // chains per thread: 16
+constexpr int kRPH = 64 / kHW;   // rows of a 64-row half per thread (XT): 16
+constexpr int kDPT = 128 / kHW;  // features per thread (XF): 32
 constexpr uint32_t kStr = 144;                  // core-matrix stride along K, bytes
 constexpr uint32_t kSBO = (kDmax / 4) * kStr;   // stride between 8-chain groups: 4,608 B
 constexpr uint32_t kPlane = 8 * kSBO;           // one [64 chains, K <= 128] plane: 36,864 B
-constexpr int kStPitch = 129;                   // staging row pitch in floats (odd: no conflicts)
+constexpr int kStPitch = kDmax + 1;             // largest staging row pitch (floats)
 constexpr uint32_t kColXF = 0, kColXT = 256, kColEta = 384, kColGT = 448;
 constexpr size_t kOffR = 2 * kPlane, kOffStage = 4 * kPlane;
-constexpr size_t kOffScal = kOffStage + (size_t)64 * kStPitch * 4;
+constexpr size_t kStageHalf = (size_t)64 * kStPitch;  // floats per staging half
+constexpr size_t kOffScal = kOffStage + 2 * kStageHalf * 4;
 // scalars: 10 x 64 floats, 4 x 64 doubles, 2 x 4 x 64 floats, 4 x 64 doubles, 64 ints
 constexpr size_t kSmemBytes = kOffScal + 640 * 4 + 256 * 8 + 512 * 4 + 256 * 8 + 64 * 4;
 
@@ -64,6 +73,8 @@ struct Args {
   const int32_t* Ns;
   const int32_t* Ds;
   const int32_t* order;
+  const float* tiles;       // X re-laid by edg_hmc_hier_tc_prepare
+  const int64_t* tile_off;  // [I] float offset of each instance's tiles
   int I, SP, C, tiles_per_inst;
   float mu_loc, mu_scale, tau_scale;
   int n_iter, n_steps, cache_valid;
@@ -92,12 +103,17 @@ __device__ __forceinline__ uint32_t bop_off(int c, int k) {
 __device__ __forceinline__ float hi_part(float v) {
   return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
 }
-// Sum over the warp's lanes of v[0..31], scattered: lane i returns the total
-// of index i (31 shuffles instead of 32 x 5).
-__device__ __forceinline__ float reduce_scatter32(float (&v)[32]) {
+// Sum over the warp's lanes of v[0..V-1] (V = 16 or 32), scattered: lane i
+// returns the total of index i % V (31 shuffles instead of V x 5).
+template <int V>
+__device__ __forceinline__ float reduce_scatter(float (&v)[V]) {
   const int lane = threadIdx.x & 31;
+  if (V == 16) {
 #pragma unroll
-  for (int s = 16; s >= 1; s >>= 1) {
+    for (int j = 0; j < V; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], 16);
+  }
+#pragma unroll
+  for (int s = V / 2; s >= 1; s >>= 1) {
     const bool up = (lane & s) != 0;
 #pragma unroll
     for (int j = 0; j < s; ++j) {
@@ -112,19 +128,21 @@ __device__ __forceinline__ float reduce_scatter32(float (&v)[32]) {
 // All n_iter iterations of one work item: chains [ctile*64, ctile*64 + 64)
 // of instance order[item / tiles_per_inst].
 __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint32_t tm,
-                             uint32_t barF, uint32_t barB, uint32_t (&ph)[2], volatile int* err) {
+                             uint32_t barF, uint32_t barB, uint32_t barX0, uint32_t (&ph)[4],
+                             volatile int* err) {
   const int inst = a.order ? a.order[item / a.tiles_per_inst] : item / a.tiles_per_inst;
   const int ctile = item % a.tiles_per_inst;
-  const float* __restrict__ X = a.X + a.x_off[inst];
   const float* __restrict__ Y = a.y + a.y_off[inst];
   const int N = a.Ns[inst], D = a.Ds[inst];
   const int Dp = round_up(D, 8);
+  const int pitch = Dp + 1;  // staging and tile row pitch (floats)
+  const float* __restrict__ Xt = a.tiles + a.tile_off[inst];
   const int ntiles = (N + kRows - 1) / kRows;
   const int SP = a.SP;
   const int cbase = ctile * kCh;
   const int nc = min(kCh, a.C - cbase);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, chain half
+  const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, chain slice
   const int d = 32 * q + lane;            // the feature this thread owns in the state
   const bool dval = d < D;
   const uint32_t lane_base = (uint32_t)(32 * q) << 16;
@@ -144,11 +162,11 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
   const float eps = a.step_size, half = 0.5f * a.step_size;
   auto gchain = [&](int c) -> size_t { return (size_t)inst * a.C + cbase + c; };
 
-  // the accepted state: feature d of chains 32h + i
-  float Z[32], G[32], Rm[32];
+  // the accepted state: feature d of chains kCPT * h + i
+  float Z[kCPT], G[kCPT], Rm[kCPT];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const int c = 32 * h + i;
+  for (int i = 0; i < kCPT; ++i) {
+    const int c = kCPT * h + i;
     const bool ok = c < nc && dval;
     const size_t g = gchain(ok ? c : 0) * SP + (dval ? d : 0);
     Z[i] = ok ? a.z[g] : 0.0f;
@@ -168,39 +186,46 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
   __syncthreads();
 
   // ---- X tile movement
-  auto load_rows = [&](int rbase, float (&x)[32]) {  // rows rbase + 32h + k, feature d
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      const int row = rbase + 32 * h + k;
-      x[k] = (dval && row < N) ? __ldg(X + (size_t)row * D + d) : 0.0f;
+  // rows 128 j + 64 hf .. + 63 (already zero beyond N and D) -> staging half hf
+  auto prefetch = [&](int j, int hf) {
+    if (tid == 0 && j < ntiles) {
+      const uint32_t bytes = 64u * (uint32_t)pitch * 4u;
+      const uint32_t bar = barX0 + 8u * hf;
+      fence_proxy_async();  // the staging half's generic reads come first
+      mbar_expect_tx(bar, bytes);
+      bulk_g2s(smem_u32(stg + hf * kStageHalf), Xt + ((size_t)kRows * j + 64 * hf) * pitch, bytes,
+               bar);
     }
   };
-  auto store_xt = [&](const float (&x)[32]) {  // XT columns 32h + k of lane d
+  auto wait_stage = [&](int hf) {
+    mbar_wait(barX0 + 8u * hf, ph[2 + hf], err);
+    ph[2 + hf] ^= 1u;
+  };
+  auto store_xt = [&](int hf) {  // XT columns kRPH h + k of lane d <- staging half hf
+    const float* sh = stg + hf * kStageHalf;
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < kRPH / 16; ++s) {
       float hv[16], lv[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
-        hv[k] = hi_part(x[16 * s + k]);
-        lv[k] = x[16 * s + k] - hv[k];
+        const float v = sh[(kRPH * h + 16 * s + k) * pitch + d];
+        hv[k] = hi_part(v);
+        lv[k] = v - hv[k];
       }
-      tmem_st16(tm + lane_base + kColXT + 32 * h + 16 * s, hv);
-      tmem_st16(tm + lane_base + kColXT + 64 + 32 * h + 16 * s, lv);
+      tmem_st16(tm + lane_base + kColXT + kRPH * h + 16 * s, hv);
+      tmem_st16(tm + lane_base + kColXT + 64 + kRPH * h + 16 * s, lv);
     }
   };
-  auto stage = [&](const float (&x)[32]) {
+  auto store_xf = [&]() {  // XF lane 32q + lane (tile row) <- staging
+    const float* sr = stg + (q >> 1) * kStageHalf + (32 * (q & 1) + lane) * pitch;
 #pragma unroll
-    for (int k = 0; k < 32; ++k) stg[(32 * h + k) * kStPitch + d] = x[k];
-  };
-  auto store_xf = [&](int srow) {  // XF lane (this warp's quadrant) <- staging row srow
-#pragma unroll
-    for (int ch = 0; ch < 4; ++ch) {
-      const int d0 = 64 * h + 16 * ch;
+    for (int ch = 0; ch < kDPT / 16; ++ch) {
+      const int d0 = kDPT * h + 16 * ch;
       if (d0 >= Dp) break;
       float hv[16], lv[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
-        const float v = stg[srow * kStPitch + d0 + k];
+        const float v = sr[d0 + k];
         hv[k] = hi_part(v);
         lv[k] = v - hv[k];
       }
@@ -234,36 +259,35 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
   auto eval = [&](const float* msrc, const float* usrc, bool need_ll) {
     if (d < Dp) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < kCPT; ++i) {
         const float hv = hi_part(Z[i]);
-        const uint32_t off = bop_off(32 * h + i, d);
+        const uint32_t off = bop_off(kCPT * h + i, d);
         *reinterpret_cast<float*>(Wb + off) = hv;
         *reinterpret_cast<float*>(Wb + kPlane + off) = Z[i] - hv;
       }
     }
     fence_proxy_async();
-    double llacc = 0.0;  // chain 32h + lane over this quadrant's rows
-    float x[32];
+    double llacc = 0.0;  // chain kCPT h + lane % kCPT over this quadrant's rows
+    prefetch(0, 0);
+    prefetch(0, 1);
     for (int j = 0; j < ntiles; ++j) {
       const int row0 = j * kRows;
-      load_rows(row0, x);
+      wait_stage(0);  // both staging halves of tile j have landed
+      wait_stage(1);
       if (j > 0) {  // XT and R are free once the previous tile's backward completes
         mbar_wait(barB, ph[1], err);
         ph[1] ^= 1u;
         tc_fence_after();
       }
-      store_xt(x);
-      stage(x);
-      __syncthreads();
-      if (q < 2) store_xf(32 * q + lane);
-      __syncthreads();
-      load_rows(row0 + 64, x);
-      stage(x);
-      __syncthreads();
-      if (q >= 2) store_xf(32 * (q - 2) + lane);
+      store_xt(0);
+      store_xf();
       tmem_st_wait();
       tc_fence_before();
       __syncthreads();
+      prefetch(j + 1, 0);  // staging half A is free
+      const int row = row0 + 32 * q + lane;  // this thread's row in the epilogue
+      const bool rv = row < N;
+      const float yv = rv ? __ldg(Y + row) : 0.0f;  // loaded under the forward MMAs
       if (warp == 0) {
         tc_fence_after();
         const uint32_t issue = elect_one();
@@ -284,57 +308,68 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       ph[0] ^= 1u;
       tc_fence_after();
       {
-        float v[32];
-        tmem_ld32(tm + lane_base + kColEta + 32 * h, v);
-        const int row = row0 + 32 * q + lane;
-        const bool rv = row < N;
-        const float yv = rv ? __ldg(Y + row) : 0.0f;
-        float llv[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
+        float v[kCPT];
+        tmem_ld16(tm + lane_base + kColEta + kCPT * h, v);
+        // r = y - sigmoid(eta) = y - (eta >= 0 ? 1 : e) / (1 + e), e = exp(-|eta|);
+        // the log-likelihood y eta - softplus(eta) only where the log joint is needed
+        auto resid = [&](int i, float& a1) {
           const float eta = v[i];
           const float e = ex2_approx(-kLog2e * fabsf(eta));
-          const float a1 = 1.0f + e;
+          a1 = 1.0f + e;
           const float s = rcp_approx(a1);
           const float r = rv ? yv - (eta >= 0.0f ? s : e * s) : 0.0f;
-          llv[i] = rv ? -(fmaxf(eta, 0.0f) - eta * yv + kLn2 * lg2_approx(a1)) : 0.0f;
           const float rh = hi_part(r);
-          const uint32_t off = bop_off(32 * h + i, 32 * q + lane);
+          const uint32_t off = bop_off(kCPT * h + i, 32 * q + lane);
           *reinterpret_cast<float*>(Rb + off) = rh;
           *reinterpret_cast<float*>(Rb + kPlane + off) = r - rh;
+        };
+        if (need_ll) {
+          float llv[kCPT];
+#pragma unroll
+          for (int i = 0; i < kCPT; ++i) {
+            float a1;
+            resid(i, a1);
+            llv[i] = rv ? -(fmaxf(v[i], 0.0f) - v[i] * yv + kLn2 * lg2_approx(a1)) : 0.0f;
+          }
+          llacc += (double)reduce_scatter<kCPT>(llv);
+        } else {
+#pragma unroll
+          for (int i = 0; i < kCPT; ++i) {
+            float a1;
+            resid(i, a1);
+          }
         }
-        if (need_ll) llacc += (double)reduce_scatter32(llv);
       }
       fence_proxy_async();
       tc_fence_before();
       __syncthreads();
       issue_bwd(0, j == 0);
-      load_rows(row0 + 64, x);
       mbar_wait(barB, ph[1], err);  // XT is free once the first half's MMAs complete
       ph[1] ^= 1u;
       tc_fence_after();
-      store_xt(x);
+      store_xt(1);
       tmem_st_wait();
       tc_fence_before();
       __syncthreads();
+      prefetch(j + 1, 1);  // staging half B is free
       issue_bwd(1, false);
     }
-    float gl[32];
+    float gl[kCPT];
     if (ntiles > 0) {
       mbar_wait(barB, ph[1], err);
       ph[1] ^= 1u;
       tc_fence_after();
-      tmem_ld32(tm + lane_base + kColGT + 32 * h, gl);
+      tmem_ld16(tm + lane_base + kColGT + kCPT * h, gl);
     } else {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) gl[i] = 0.0f;
+      for (int i = 0; i < kCPT; ++i) gl[i] = 0.0f;
     }
     // hierarchical prior: d/dw = -(w - mu) / tau^2, and the per-chain sums of
     // (w - mu) and (w - mu)^2 over the features
-    float s1v[32], s2v[32];
+    float s1v[kCPT], s2v[kCPT];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int c = 32 * h + i;
+    for (int i = 0; i < kCPT; ++i) {
+      const int c = kCPT * h + i;
       const float tau = softplusf(usrc[c]);
       const float it2 = 1.0f / (tau * tau);
       const float dev = dval ? Z[i] - msrc[c] : 0.0f;
@@ -342,11 +377,13 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       s1v[i] = dev;
       s2v[i] = dev * dev;
     }
-    const float s1p = reduce_scatter32(s1v);
-    const float s2p = reduce_scatter32(s2v);
-    ps1[q * 64 + 32 * h + lane] = s1p;
-    ps2[q * 64 + 32 * h + lane] = s2p;
-    if (need_ll) pd[q * 64 + 32 * h + lane] = llacc;
+    const float s1p = reduce_scatter<kCPT>(s1v);
+    const float s2p = reduce_scatter<kCPT>(s2v);
+    if (lane < kCPT) {
+      ps1[q * 64 + kCPT * h + lane] = s1p;
+      ps2[q * 64 + kCPT * h + lane] = s2p;
+      if (need_ll) pd[q * 64 + kCPT * h + lane] = llacc;
+    }
     __syncthreads();
     if (tid < kCh) {
       const int c = tid;
@@ -378,8 +415,8 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
   if (!a.cache_valid) {
     eval(mu0, u0, true);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int c = 32 * h + i;
+    for (int i = 0; i < kCPT; ++i) {
+      const int c = kCPT * h + i;
       if (c < nc && dval) a.grad[gchain(c) * SP + d] = G[i];
     }
     if (tid < kCh) {
@@ -395,10 +432,10 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
     const int64_t t = t0 + it;
     const uint32_t iter = (uint32_t)t;
     // momenta for (w, mu, u): Philox elements 0..D-1 are w, D is mu, D + 1 is u
-    float kp[32];
+    float kp[kCPT];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int c = 32 * h + i;
+    for (int i = 0; i < kCPT; ++i) {
+      const int c = kCPT * h + i;
       float r = 0.0f;
       if (c < nc && dval)
         r = a.r_ovr ? a.r_ovr[((size_t)it * a.I * a.C + gchain(c)) * SP + d]
@@ -406,7 +443,10 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       Rm[i] = r;
       kp[i] = r * r;
     }
-    pd[q * 64 + 32 * h + lane] = (double)reduce_scatter32(kp);
+    {
+      const float k0 = reduce_scatter<kCPT>(kp);
+      if (lane < kCPT) pd[q * 64 + kCPT * h + lane] = (double)k0;
+    }
     if (tid < kCh) {
       const int c = tid;
       float r1 = 0.0f, r2 = 0.0f;
@@ -436,7 +476,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
     __syncthreads();
     for (int l = 0; l < a.n_steps; ++l) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < kCPT; ++i) {
         Rm[i] += half * G[i];
         Z[i] += eps * Rm[i];
       }
@@ -450,7 +490,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       __syncthreads();
       eval(hmu, hu, l == a.n_steps - 1);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) Rm[i] += half * G[i];
+      for (int i = 0; i < kCPT; ++i) Rm[i] += half * G[i];
       if (tid < kCh) {
         rmu[tid] += half * gmu[tid];
         ru[tid] += half * gu[tid];
@@ -458,8 +498,11 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 32; ++i) kp[i] = Rm[i] * Rm[i];
-    pd[q * 64 + 32 * h + lane] = (double)reduce_scatter32(kp);
+    for (int i = 0; i < kCPT; ++i) kp[i] = Rm[i] * Rm[i];
+    {
+      const float k1 = reduce_scatter<kCPT>(kp);
+      if (lane < kCPT) pd[q * 64 + kCPT * h + lane] = (double)k1;
+    }
     __syncthreads();
     if (tid < kCh) {
       const int c = tid;
@@ -488,8 +531,8 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
     // keep the proposal (written back as the accepted state) or reload the
     // accepted state; then the kept sample and the running moments
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int c = 32 * h + i;
+    for (int i = 0; i < kCPT; ++i) {
+      const int c = kCPT * h + i;
       if (c < nc && dval) {
         const size_t g = gchain(c) * SP + d;
         if (acc[c]) {
@@ -537,7 +580,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
 
 __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) uint64_t bars[4];  // forward, backward, staging halves A and B
   __shared__ uint32_t s_tmem;
   __shared__ int s_item, s_err;
   __shared__ bool s_last;
@@ -546,8 +589,8 @@ __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
   if (threadIdx.x == 0) {
     s_t0 = *(volatile int64_t*)&a.state->t;
     s_err = 0;
-    mbar_init(smem_u32(&bars[0]), 1);
-    mbar_init(smem_u32(&bars[1]), 1);
+#pragma unroll
+    for (int b = 0; b < 4; ++b) mbar_init(smem_u32(&bars[b]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -561,7 +604,8 @@ __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
   tc_fence_after();
   const uint32_t tm = s_tmem;
   const uint32_t barF = smem_u32(&bars[0]), barB = smem_u32(&bars[1]);
-  uint32_t ph[2] = {0u, 0u};
+  const uint32_t barX0 = smem_u32(&bars[2]);  // barX0 + 8 is half B's
+  uint32_t ph[4] = {0u, 0u, 0u, 0u};
   volatile int* err = &s_err;
   if (a.persistent) {
     const int total = a.I * a.tiles_per_inst;
@@ -571,10 +615,10 @@ __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
       __syncthreads();
       const int item = s_item;
       if (item >= total || *err) break;
-      hier_tc_item(a, item, smem, tm, barF, barB, ph, err);
+      hier_tc_item(a, item, smem, tm, barF, barB, barX0, ph, err);
     }
   } else {
-    hier_tc_item(a, blockIdx.x, smem, tm, barF, barB, ph, err);
+    hier_tc_item(a, blockIdx.x, smem, tm, barF, barB, barX0, ph, err);
   }
   tc_fence_before();
   __syncthreads();
@@ -597,13 +641,60 @@ __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
   }
 }
 
+// X_i -> 128-row tiles with row pitch Dp_i + 1 (zero beyond N_i and D_i) at
+// tiles + tile_off[i]; blocks (instance, slice).
+__global__ void __launch_bounds__(256) prep_tiles_kernel(const float* __restrict__ X,
+                                                         const int64_t* __restrict__ x_off,
+                                                         const int32_t* __restrict__ Ns,
+                                                         const int32_t* __restrict__ Ds,
+                                                         const int64_t* __restrict__ tile_off,
+                                                         float* __restrict__ tiles) {
+  const int inst = blockIdx.x;
+  const int N = Ns[inst], D = Ds[inst];
+  const int pitch = round_up(D, 8) + 1;
+  const int64_t n = (int64_t)((N + kRows - 1) / kRows) * kRows * pitch;
+  const float* Xi = X + x_off[inst];
+  float* T = tiles + tile_off[inst];
+  for (int64_t e = threadIdx.x + (int64_t)blockIdx.y * blockDim.x; e < n;
+       e += (int64_t)blockDim.x * gridDim.y) {
+    const int64_t r = e / pitch;
+    const int c = (int)(e - r * pitch);
+    T[e] = (r < N && c < D) ? Xi[r * D + c] : 0.0f;
+  }
+}
+
 }  // namespace htc
 }  // namespace edg
 
 using namespace edg;
 
+extern "C" int64_t edg_hmc_hier_tc_tile_offsets(const int32_t* N, const int32_t* D, int32_t I,
+                                                int64_t* tile_off) {
+  if (!N || !D || I <= 0) return -1;
+  int64_t off = 0;
+  for (int i = 0; i < I; ++i) {
+    if (N[i] < 0 || D[i] <= 0 || D[i] > htc::kDmax) return -1;
+    if (tile_off) tile_off[i] = off;
+    off += (int64_t)((N[i] + htc::kRows - 1) / htc::kRows) * htc::kRows * (round_up(D[i], 8) + 1);
+  }
+  return off;
+}
+
+extern "C" int edg_hmc_hier_tc_prepare(const edg_hier_t* model, const int64_t* tile_off,
+                                       float* tiles, void* stream) {
+  EDG_REQUIRE(model && tile_off && tiles, EDG_E_NULL, "model, tile_off and tiles must not be NULL");
+  EDG_REQUIRE(model->X && model->x_offset && model->N && model->D, EDG_E_NULL,
+              "model arrays must be device pointers");
+  EDG_REQUIRE(model->I > 0, EDG_E_SHAPE, "I must be positive");
+  EDG_REQUIRE(((uintptr_t)tiles & 15u) == 0, EDG_E_VALUE, "tiles must be 16-byte aligned");
+  htc::prep_tiles_kernel<<<dim3((unsigned)model->I, 8), 256, 0, (cudaStream_t)stream>>>(
+      model->X, model->x_offset, model->N, model->D, tile_off, tiles);
+  return check_launch("prep_tiles_kernel");
+}
+
 extern "C" int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C,
-                                   int32_t n_iter, const int32_t* order, float* z, float* grad,
+                                   int32_t n_iter, const int32_t* order, const float* tiles,
+                                   const int64_t* tile_off, float* z, float* grad,
                                    double* lj, int32_t cache_valid, int32_t* n_accept,
                                    edg_state_t* state, float* samples, int64_t T_cap,
                                    double* moments, const float* r_override,
@@ -613,6 +704,9 @@ extern "C" int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg
                   model->D,
               EDG_E_NULL, "model arrays must be device pointers");
   EDG_REQUIRE(z && grad && lj && state, EDG_E_NULL, "z, grad, lj and state must not be NULL");
+  EDG_REQUIRE(tiles && tile_off, EDG_E_NULL,
+              "tiles and tile_off (edg_hmc_hier_tc_prepare) must not be NULL");
+  EDG_REQUIRE(((uintptr_t)tiles & 15u) == 0, EDG_E_VALUE, "tiles must be 16-byte aligned");
   EDG_REQUIRE(model->I > 0 && C > 0 && n_iter >= 0, EDG_E_SHAPE,
               "I and C must be positive and n_iter >= 0");
   EDG_REQUIRE(model->max_D > 0 && model->max_D <= htc::kDmax, EDG_E_UNSUPPORTED,
@@ -633,6 +727,8 @@ extern "C" int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg
   a.Ns = model->N;
   a.Ds = model->D;
   a.order = order;
+  a.tiles = tiles;
+  a.tile_off = tile_off;
   a.I = model->I;
   a.SP = model->max_D + 2;
   a.C = C;

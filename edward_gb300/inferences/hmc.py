@@ -190,7 +190,7 @@ class HMC(MonteCarlo):
         best = self._autotune_hier()
         cfg.launch, cfg.chains_per_block = best & 1, 16 if best & 2 else 32
         self.hier_engine = "tc" if best & 4 else "simt"
-        self._hier_fn = "edg_hmc_hier_tc_run" if best & 4 else "edg_hmc_hier_run"
+        self._hier_tiles = self._hier.tc_tiles() if best & 4 else None
         self.train = self.update
         return self.train
 
@@ -217,10 +217,16 @@ class HMC(MonteCarlo):
             cfg.launch, cfg.chains_per_block = c & 1, 16 if c & 2 else 32
             z.copy_(self._z)
             st = _lib.new_state(self._device)
-            fn = "edg_hmc_hier_tc_run" if c & 4 else "edg_hmc_hier_run"
-            _lib.call(fn, hd.ref(), ctypes.byref(cfg), C, 1, _lib.ptr(hd.order),
-                      _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st), None, 0,
-                      None, None, None, None, _lib.stream_ptr())
+            if c & 4:
+                tiles, toff = hd.tc_tiles()
+                _lib.call("edg_hmc_hier_tc_run", hd.ref(), ctypes.byref(cfg), C, 1,
+                          _lib.ptr(hd.order), _lib.ptr(tiles), _lib.ptr(toff), _lib.ptr(z),
+                          _lib.ptr(g), _lib.ptr(lj), 0, None, _lib.ptr(st), None, 0, None, None,
+                          None, None, _lib.stream_ptr())
+            else:
+                _lib.call("edg_hmc_hier_run", hd.ref(), ctypes.byref(cfg), C, 1,
+                          _lib.ptr(hd.order), _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, None,
+                          _lib.ptr(st), None, 0, None, None, None, None, _lib.stream_ptr())
 
         work = int((hd.Ns.astype(np.int64) * hd.Ds).sum())
         key = f"I{hd.I}_work{work}_maxD{hd.max_D}_C{C}_L{self.n_steps}"
@@ -288,8 +294,14 @@ class HMC(MonteCarlo):
             return
         if self.engine == "hier":
             def launch():
-                _lib.call(self._hier_fn, self._hier.ref(), ctypes.byref(self._cfg), self.C,
-                          int(n_iter), _lib.ptr(self._hier.order), _lib.ptr(self._z),
+                if self._hier_tiles is not None:
+                    fn = "edg_hmc_hier_tc_run"
+                    lead = (_lib.ptr(self._hier.order), _lib.ptr(self._hier_tiles[0]),
+                            _lib.ptr(self._hier_tiles[1]))
+                else:
+                    fn, lead = "edg_hmc_hier_run", (_lib.ptr(self._hier.order),)
+                _lib.call(fn, self._hier.ref(), ctypes.byref(self._cfg), self.C,
+                          int(n_iter), *lead, _lib.ptr(self._z),
                           _lib.ptr(self._g), _lib.ptr(self._lj), self._cache_valid,
                           _lib.ptr(self._n_accept), _lib.ptr(self._state),
                           _lib.ptr(self._samples), self._samples.shape[0], None,

@@ -147,6 +147,23 @@ class HierDevice:
     def ref(self):
         return ctypes.byref(self.c)
 
+    def tc_tiles(self):
+        """(tiles, tile_off) for edg_hmc_hier_tc_run: X re-laid once into
+        128-row tiles (edg_hmc_hier_tc_prepare), cached."""
+        if getattr(self, "_tc", None) is None:
+            lib = _lib.load()
+            off = np.zeros(self.I, np.int64)
+            total = lib.edg_hmc_hier_tc_tile_offsets(self.Ns.ctypes.data, self.Ds.ctypes.data,
+                                                     self.I, off.ctypes.data)
+            if total < 0:
+                raise NotImplementedError("the tensor-core hierarchical engine needs D_i <= 128")
+            tiles = torch.empty(max(int(total), 4), dtype=torch.float32, device=self.device)
+            off_t = torch.as_tensor(off, device=self.device)
+            _lib.call("edg_hmc_hier_tc_prepare", self.ref(), _lib.ptr(off_t), _lib.ptr(tiles),
+                      _lib.stream_ptr())
+            self._tc = (tiles, off_t)
+        return self._tc
+
 
 class BNNDevice:
     """Device data of a compiled Bayesian NN (``compile.MLPSpec``) and where

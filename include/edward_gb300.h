@@ -495,13 +495,22 @@ int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, i
 /* Same contract as edg_hmc_hier_run (same draws, state layout and results to
  * FP32 rounding), with every gradient evaluation computed as tcgen05 3xTF32
  * GEMMs: one CTA per (instance, 64 chains), X read once per evaluation for
- * all 64 chains.  Requires max_D <= 128; cfg->chains_per_block is ignored. */
+ * all 64 chains.  Requires max_D <= 128; cfg->chains_per_block is ignored.
+ * `tiles` is X re-laid once by edg_hmc_hier_tc_prepare: instance i at float
+ * offset tile_off[i], in 128-row tiles with row pitch round_up(D_i, 8) + 1,
+ * zero beyond N_i and D_i.  edg_hmc_hier_tc_tile_offsets fills tile_off
+ * (host arrays N, D) and returns the total size in floats (-1 on bad
+ * input); tile_off is then copied to the device for the two calls below. */
+int64_t edg_hmc_hier_tc_tile_offsets(const int32_t* N, const int32_t* D, int32_t I,
+                                     int64_t* tile_off);
+int edg_hmc_hier_tc_prepare(const edg_hier_t* model, const int64_t* tile_off, float* tiles,
+                            void* stream);
 int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, int32_t n_iter,
-                        const int32_t* order, float* z, float* grad, double* lj,
-                        int32_t cache_valid, int32_t* n_accept, edg_state_t* state,
-                        float* samples, int64_t T_cap, double* moments,
-                        const float* r_override, const double* u_override, double* ratio_out,
-                        void* stream);
+                        const int32_t* order, const float* tiles, const int64_t* tile_off,
+                        float* z, float* grad, double* lj, int32_t cache_valid,
+                        int32_t* n_accept, edg_state_t* state, float* samples, int64_t T_cap,
+                        double* moments, const float* r_override, const double* u_override,
+                        double* ratio_out, void* stream);
 
 /* ---------------------------------------------------------------- HMC, tensor cores
  * Same contract as edg_hmc_glm_run, computed with tcgen05 3xTF32 GEMMs:

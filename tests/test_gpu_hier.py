@@ -32,8 +32,12 @@ def _run(hd, C, z0, n_iter, step, L, r=None, u=None, seed=7, samples=None, launc
     nacc = torch.zeros(n, dtype=torch.int32, device=cuda)
     st = _lib.new_state(cuda)
     ratio = torch.zeros(max(n_iter, 1), n, dtype=torch.float64, device=cuda)
-    fn = "edg_hmc_hier_tc_run" if engine == "tc" else "edg_hmc_hier_run"
-    _lib.call(fn, hd.ref(), ctypes.byref(cfg), C, n_iter, _lib.ptr(hd.order),
+    if engine == "tc":
+        tiles, toff = hd.tc_tiles()
+        fn, lead = "edg_hmc_hier_tc_run", (_lib.ptr(hd.order), _lib.ptr(tiles), _lib.ptr(toff))
+    else:
+        fn, lead = "edg_hmc_hier_run", (_lib.ptr(hd.order),)
+    _lib.call(fn, hd.ref(), ctypes.byref(cfg), C, n_iter, *lead,
               _lib.ptr(z), _lib.ptr(g), _lib.ptr(lj), 0, _lib.ptr(nacc), _lib.ptr(st),
               _lib.ptr(samples), samples.shape[0] if samples is not None else 0, None,
               _lib.ptr(r), _lib.ptr(u), _lib.ptr(ratio), _lib.stream_ptr())
