@@ -25,8 +25,9 @@
 // with 144-byte strides (bank-conflict-free stores from either side).
 //
 // Per 128-row tile (staging halves A = rows 0-63, B = rows 64-127):
-//   A -> XT (half 0); A, B -> XF; then A takes the next tile's rows 0-63
+//   A, B -> XF (under the previous tile's last backward MMAs)
 //   forward      ETA = XF W^T                      (3 x Dp/8 TS MMAs, M = 128, N = 64)
+//   A -> XT (half 0), under the forward MMAs; then A takes the next tile's rows 0-63
 //   epilogue     one thread per row and 16 chains: r = y - sigmoid(eta), the
 //                per-row log-likelihood; R <- r (hi, lo)
 //   backward     GT += XT R^T over rows 0-63 (24 TS MMAs, M = 128 features)
@@ -274,17 +275,12 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       const int row0 = j * kRows;
       wait_stage(0);  // both staging halves of tile j have landed
       wait_stage(1);
-      if (j > 0) {  // XT and R are free once the previous tile's backward completes
-        mbar_wait(barB, ph[1], err);
-        ph[1] ^= 1u;
-        tc_fence_after();
-      }
-      store_xt(0);
+      // XF is free (the previous forward completed): built while the previous
+      // tile's second backward half still runs
       store_xf();
       tmem_st_wait();
       tc_fence_before();
       __syncthreads();
-      prefetch(j + 1, 0);  // staging half A is free
       const int row = row0 + 32 * q + lane;  // this thread's row in the epilogue
       const bool rv = row < N;
       const float yv = rv ? __ldg(Y + row) : 0.0f;  // loaded under the forward MMAs
@@ -304,6 +300,12 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         mma_commit_if(issue, barF);
         __syncwarp();
       }
+      if (j > 0) {  // XT and R are free once the previous tile's backward completes
+        mbar_wait(barB, ph[1], err);
+        ph[1] ^= 1u;
+        tc_fence_after();
+      }
+      store_xt(0);  // under the forward MMAs
       mbar_wait(barF, ph[0], err);
       ph[0] ^= 1u;
       tc_fence_after();
@@ -340,9 +342,11 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
           }
         }
       }
+      tmem_st_wait();
       fence_proxy_async();
       tc_fence_before();
       __syncthreads();
+      prefetch(j + 1, 0);  // staging half A is free
       issue_bwd(0, j == 0);
       mbar_wait(barB, ph[1], err);  // XT is free once the first half's MMAs complete
       ph[1] ^= 1u;
