@@ -13,7 +13,8 @@
 // from TMEM (the A operand of the TS form).  X is read from HBM as one fp32
 // plane, once per evaluation for all 64 chains.  edg_hmc_hier_tc_prepare
 // re-lays each X_i once into 128-row tiles with a row pitch of Dp_i + 1
-// floats (Dp_i = D_i rounded up to 8; zero beyond N_i and D_i), so that each
+// floats (Dp_i = D_i rounded up to 8; y_i in the pad column Dp_i, zero
+// elsewhere beyond D_i and beyond N_i), so that each
 // 64-row half of a tile is one contiguous bulk copy (issued by one thread,
 // completed on an mbarrier) into a shared staging half whose odd pitch lets
 // one thread per feature (XT) and one thread per row (XF) read it without
@@ -96,6 +97,10 @@ struct Args {
 };
 
 // Byte offset of element (chain c, k) in a W or R plane.
+// Orders this thread's shared-memory writes before later tensor-core reads.
+__device__ __forceinline__ void fence_shared_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ uint32_t bop_off(int c, int k) {
   return (uint32_t)(c >> 3) * kSBO + (uint32_t)(k >> 2) * kStr + (uint32_t)(c & 7) * 16u +
          (uint32_t)(k & 3) * 4u;
@@ -133,7 +138,6 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
                              volatile int* err) {
   const int inst = a.order ? a.order[item / a.tiles_per_inst] : item / a.tiles_per_inst;
   const int ctile = item % a.tiles_per_inst;
-  const float* __restrict__ Y = a.y + a.y_off[inst];
   const int N = a.Ns[inst], D = a.Ds[inst];
   const int Dp = round_up(D, 8);
   const int pitch = Dp + 1;  // staging and tile row pitch (floats)
@@ -192,7 +196,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
     if (tid == 0 && j < ntiles) {
       const uint32_t bytes = 64u * (uint32_t)pitch * 4u;
       const uint32_t bar = barX0 + 8u * hf;
-      fence_proxy_async();  // the staging half's generic reads come first
+      fence_shared_async();  // the staging half's generic reads come first
       mbar_expect_tx(bar, bytes);
       bulk_g2s(smem_u32(stg + hf * kStageHalf), Xt + ((size_t)kRows * j + 64 * hf) * pitch, bytes,
                bar);
@@ -267,7 +271,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         *reinterpret_cast<float*>(Wb + kPlane + off) = Z[i] - hv;
       }
     }
-    fence_proxy_async();
+    fence_shared_async();
     double llacc = 0.0;  // chain kCPT h + lane % kCPT over this quadrant's rows
     prefetch(0, 0);
     prefetch(0, 1);
@@ -283,7 +287,8 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       __syncthreads();
       const int row = row0 + 32 * q + lane;  // this thread's row in the epilogue
       const bool rv = row < N;
-      const float yv = rv ? __ldg(Y + row) : 0.0f;  // loaded under the forward MMAs
+      // y rides in the tile's pad column (index Dp) of the staged row
+      const float yv = stg[(q >> 1) * kStageHalf + (32 * (q & 1) + lane) * pitch + Dp];
       if (warp == 0) {
         tc_fence_after();
         const uint32_t issue = elect_one();
@@ -343,7 +348,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         }
       }
       tmem_st_wait();
-      fence_proxy_async();
+      fence_shared_async();
       tc_fence_before();
       __syncthreads();
       prefetch(j + 1, 0);  // staging half A is free
@@ -645,10 +650,13 @@ __global__ void __launch_bounds__(kT, 1) hmc_hier_tc_kernel(const Args a) {
   }
 }
 
-// X_i -> 128-row tiles with row pitch Dp_i + 1 (zero beyond N_i and D_i) at
-// tiles + tile_off[i]; blocks (instance, slice).
+// X_i -> 128-row tiles with row pitch Dp_i + 1 at tiles + tile_off[i]:
+// columns [0, D_i) hold the row of X_i, column Dp_i holds y_i, the rest and
+// the rows beyond N_i are zero; blocks (instance, slice).
 __global__ void __launch_bounds__(256) prep_tiles_kernel(const float* __restrict__ X,
+                                                         const float* __restrict__ y,
                                                          const int64_t* __restrict__ x_off,
+                                                         const int64_t* __restrict__ y_off,
                                                          const int32_t* __restrict__ Ns,
                                                          const int32_t* __restrict__ Ds,
                                                          const int64_t* __restrict__ tile_off,
@@ -658,12 +666,14 @@ __global__ void __launch_bounds__(256) prep_tiles_kernel(const float* __restrict
   const int pitch = round_up(D, 8) + 1;
   const int64_t n = (int64_t)((N + kRows - 1) / kRows) * kRows * pitch;
   const float* Xi = X + x_off[inst];
+  const float* yi = y + y_off[inst];
   float* T = tiles + tile_off[inst];
+  const int Dp = pitch - 1;
   for (int64_t e = threadIdx.x + (int64_t)blockIdx.y * blockDim.x; e < n;
        e += (int64_t)blockDim.x * gridDim.y) {
     const int64_t r = e / pitch;
     const int c = (int)(e - r * pitch);
-    T[e] = (r < N && c < D) ? Xi[r * D + c] : 0.0f;
+    T[e] = r < N ? (c < D ? Xi[r * D + c] : (c == Dp ? yi[r] : 0.0f)) : 0.0f;
   }
 }
 
@@ -687,12 +697,12 @@ extern "C" int64_t edg_hmc_hier_tc_tile_offsets(const int32_t* N, const int32_t*
 extern "C" int edg_hmc_hier_tc_prepare(const edg_hier_t* model, const int64_t* tile_off,
                                        float* tiles, void* stream) {
   EDG_REQUIRE(model && tile_off && tiles, EDG_E_NULL, "model, tile_off and tiles must not be NULL");
-  EDG_REQUIRE(model->X && model->x_offset && model->N && model->D, EDG_E_NULL,
-              "model arrays must be device pointers");
+  EDG_REQUIRE(model->X && model->y && model->x_offset && model->y_offset && model->N && model->D,
+              EDG_E_NULL, "model arrays must be device pointers");
   EDG_REQUIRE(model->I > 0, EDG_E_SHAPE, "I must be positive");
   EDG_REQUIRE(((uintptr_t)tiles & 15u) == 0, EDG_E_VALUE, "tiles must be 16-byte aligned");
   htc::prep_tiles_kernel<<<dim3((unsigned)model->I, 8), 256, 0, (cudaStream_t)stream>>>(
-      model->X, model->x_offset, model->N, model->D, tile_off, tiles);
+      model->X, model->y, model->x_offset, model->y_offset, model->N, model->D, tile_off, tiles);
   return check_launch("prep_tiles_kernel");
 }
 

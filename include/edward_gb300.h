@@ -496,9 +496,10 @@ int edg_hmc_hier_run(const edg_hier_t* model, const edg_hmc_t* cfg, int32_t C, i
  * FP32 rounding), with every gradient evaluation computed as tcgen05 3xTF32
  * GEMMs: one CTA per (instance, 64 chains), X read once per evaluation for
  * all 64 chains.  Requires max_D <= 128; cfg->chains_per_block is ignored.
- * `tiles` is X re-laid once by edg_hmc_hier_tc_prepare: instance i at float
- * offset tile_off[i], in 128-row tiles with row pitch round_up(D_i, 8) + 1,
- * zero beyond N_i and D_i.  edg_hmc_hier_tc_tile_offsets fills tile_off
+ * `tiles` is X and y re-laid once by edg_hmc_hier_tc_prepare: instance i at
+ * float offset tile_off[i], in 128-row tiles with row pitch
+ * Dp_i + 1 (Dp_i = round_up(D_i, 8)): X_i in columns [0, D_i), y_i in column
+ * Dp_i, zero elsewhere and beyond N_i.  edg_hmc_hier_tc_tile_offsets fills tile_off
  * (host arrays N, D) and returns the total size in floats (-1 on bad
  * input); tile_off is then copied to the device for the two calls below. */
 int64_t edg_hmc_hier_tc_tile_offsets(const int32_t* N, const int32_t* D, int32_t I,
