@@ -319,32 +319,32 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         tmem_ld16(tm + lane_base + kColEta + kCPT * h, v);
         // r = y - sigmoid(eta) = y - (eta >= 0 ? 1 : e) / (1 + e), e = exp(-|eta|);
         // the log-likelihood y eta - softplus(eta) only where the log joint is needed
-        auto resid = [&](int i, float& a1) {
-          const float eta = v[i];
-          const float e = ex2_approx(-kLog2e * fabsf(eta));
-          a1 = 1.0f + e;
-          const float s = rcp_approx(a1);
-          const float r = rv ? yv - (eta >= 0.0f ? s : e * s) : 0.0f;
+        auto put = [&](int i, float r) {  // R <- r (hi, lo) for chain kCPT h + i, this row
           const float rh = hi_part(r);
           const uint32_t off = bop_off(kCPT * h + i, 32 * q + lane);
           *reinterpret_cast<float*>(Rb + off) = rh;
           *reinterpret_cast<float*>(Rb + kPlane + off) = r - rh;
         };
         if (need_ll) {
+          // with the log-likelihood y eta - softplus(eta): e = exp(-|eta|),
+          // sigmoid = (eta >= 0 ? 1 : e) / (1 + e), softplus = max(eta, 0) + log(1 + e)
           float llv[kCPT];
 #pragma unroll
           for (int i = 0; i < kCPT; ++i) {
-            float a1;
-            resid(i, a1);
-            llv[i] = rv ? -(fmaxf(v[i], 0.0f) - v[i] * yv + kLn2 * lg2_approx(a1)) : 0.0f;
+            const float eta = v[i];
+            const float e = ex2_approx(-kLog2e * fabsf(eta));
+            const float a1 = 1.0f + e;
+            const float s = rcp_approx(a1);
+            put(i, yv - (eta >= 0.0f ? s : e * s));
+            llv[i] = rv ? -(fmaxf(eta, 0.0f) - eta * yv + kLn2 * lg2_approx(a1)) : 0.0f;
           }
           llacc += (double)reduce_scatter<kCPT>(llv);
         } else {
+          // r = y - 1 / (1 + exp(-eta)) (exp overflows to inf for eta << 0,
+          // giving 0).  Rows beyond N are not masked: their XT columns are zero.
 #pragma unroll
-          for (int i = 0; i < kCPT; ++i) {
-            float a1;
-            resid(i, a1);
-          }
+          for (int i = 0; i < kCPT; ++i)
+            put(i, yv - rcp_approx(1.0f + ex2_approx(-kLog2e * v[i])));
         }
       }
       tmem_st_wait();
