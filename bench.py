@@ -690,7 +690,7 @@ def run_klqp_record(args, dev, X, y, cpu_klqp, flush, tf32):
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "traffic": read_traffic_file(
                             "klqp_glm_kernel_logreg_S5.txt"),
-                        "kernel": "klqp_glm_kernel<8> (fused step, 40 blocks)",
+                        "kernel": "klqp_glm_kernel<8> (fused step, 79 blocks of 128 rows)",
                         "peak_source": hsrc, "algorithmic_bytes_per_launch": alg_bytes,
                         "note": "2 MB of X per step: launch- and latency-bound by construction"},
            "final_elbo_per_datum": final_elbo, "run_wall_s_1000_steps": run_wall,
