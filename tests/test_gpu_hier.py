@@ -243,3 +243,56 @@ def test_hier_engines_agree(cuda):
     if np.array_equal(n_a, n_b):
         np.testing.assert_allclose(s_b, s_a, rtol=1e-5, atol=1e-5 * np.abs(s_a).max())
         np.testing.assert_allclose(lj_b, lj_a, rtol=0, atol=1e-5 * scale)
+
+
+@pytest.mark.parametrize("C", [1, 65])
+def test_hier_tensor_core_edge_shapes(cuda, C):
+    """The tensor-core engine on edge shapes against the oracle: D = 1, 3
+    (one 8-wide K step), 64 / 65 (the K-step and XF chunk boundaries), 127 and
+    128 (the feature limit); N = 1, 128 and 129 rows (exact and one-over tiles),
+    300; a single chain and 65 chains (a second chain tile of one chain)."""
+    from edward_gb300.ops import HierDevice
+    rng = np.random.default_rng(17)
+    shapes = [(1, 5), (128, 1), (129, 3), (300, 64), (200, 65), (129, 127), (257, 128)]
+    Xs, ys = [], []
+    for N, D in shapes:
+        X = rng.standard_normal((N, D)).astype(np.float32)
+        w = rng.standard_normal(D) * 0.5
+        p = 1.0 / (1.0 + np.exp(-(X.astype(np.float64) @ w)))
+        Xs.append(X)
+        ys.append((rng.random(N) < p).astype(np.float32))
+    kw = dict(mu_loc=-0.2, mu_scale=0.9, tau_scale=1.3)
+    hd = HierDevice(Xs, ys, **kw)
+    L, step = 3, 0.02
+    SP = hd.SP
+    z0 = np.zeros((hd.I * C, SP), np.float32)
+    r0 = np.zeros((1, hd.I * C, SP), np.float32)
+    cols = lambda D: list(range(D)) + [SP - 2, SP - 1]   # noqa: E731
+    for i, X in enumerate(Xs):
+        D = X.shape[1]
+        z0[i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2)) * 0.2
+        r0[0][i * C:(i + 1) * C, cols(D)] = rng.standard_normal((C, D + 2))
+    u = rng.random((1, hd.I * C))
+    z, g, lj, nacc, ratio, st = _run(hd, C, torch.as_tensor(z0, device=cuda), 1, step, L,
+                                     r=torch.as_tensor(r0, device=cuda),
+                                     u=torch.as_tensor(u, device=cuda), engine="tc")
+    assert st.t == 1 and st.error == 0
+    zk, gk, rk = z.cpu().numpy(), g.cpu().numpy(), ratio.cpu().numpy()[0]
+    ak = nacc.cpu().numpy().astype(bool)
+    for i, (X, y) in enumerate(zip(Xs, ys)):
+        D = X.shape[1]
+        sl = slice(i * C, (i + 1) * C)
+        f = hier.lj_grad_fn(X, y, **kw)
+        zi = z0[sl][:, cols(D)].astype(np.float64)
+        lj0, g0 = f(zi)
+        res = hmc_step(f, zi, g0, lj0, r0[0][sl][:, cols(D)], u[0, sl], step, L)
+        scale = max(np.abs(lj0).max(), np.abs(res["lj"]).max(), 1.0)
+        np.testing.assert_allclose(rk[sl], res["ratio"], rtol=0, atol=1e-5 * scale)
+        same = ak[sl] == res["accept"]
+        exp = res["z"][same]
+        np.testing.assert_allclose(zk[sl][:, cols(D)][same], exp, rtol=1e-5,
+                                   atol=1e-5 * max(np.abs(exp).max(), 1.0))
+        # the cached gradient belongs to the kept state
+        _, gkept = f(zk[sl][:, cols(D)].astype(np.float64))
+        np.testing.assert_allclose(gk[sl][:, cols(D)], gkept, rtol=1e-5,
+                                   atol=1e-5 * max(np.abs(gkept).max(), 1.0))

@@ -220,3 +220,29 @@ def test_sgmcmc_tensor_core_reset_rebuilds_cache(cuda):
     ref, _, _ = sgmcmc.run(model, start, n, 1e-3, "sgld", seed=inf._cfg.seed)
     np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
     assert inf.t == n
+
+
+@pytest.mark.parametrize("method", ["sgld", "sghmc"])
+def test_sgmcmc_tensor_core_single_chain_bias_only(cuda, method):
+    """The tensor-core engine with one chain of a bias-only Normal model
+    (P = 1: x ~ N(mu, 1), the reference tests' Normal-Normal shape) against the
+    oracle, 6 iterations with Philox noise."""
+    import edward_gb300 as ed
+    from edward_gb300.models import Empirical, Normal
+    x_data = np.random.default_rng(3).standard_normal(50).astype(np.float32) * 0.3
+    mu = Normal(loc=0.0, scale=1.0)
+    x = Normal(loc=mu, scale=1.0, sample_shape=50)
+    qmu = Empirical(params=ed.Variable(np.full(10, 0.5, np.float32)))
+    cls = ed.SGLD if method == "sgld" else ed.SGHMC
+    inf = cls({mu: qmu}, data={x: x_data})
+    kw = dict(step_size=0.01) if method == "sgld" else dict(step_size=0.05, friction=0.2)
+    inf.initialize(n_print=0, engine="tc", **kw)
+    assert inf.engine == "tc"
+    n = 6
+    inf.run_iterations(n)
+    got = inf._samples[:n].cpu().numpy().reshape(n, 1, -1)
+    model = oglm.GLM(np.zeros((50, 0)), x_data, bias=True, lik=oglm.NORMAL)
+    ref, _, _ = sgmcmc.run(model, np.array([[0.5]]), n, kw["step_size"], method,
+                           kw.get("friction", 0.1), seed=inf._cfg.seed)
+    np.testing.assert_allclose(got.reshape(ref.shape), ref, rtol=1e-5,
+                               atol=1e-5 * np.abs(ref).max())
