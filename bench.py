@@ -1481,6 +1481,71 @@ def run_sgld(args):
     return 0
 
 
+def run_mh(args):
+    """MetropolisHastings (edward/inferences/metropolis_hastings.py) with Normal
+    random-walk proposals (scale 0.01) on the 10,000 x 50 logistic regression
+    with 4,096 chains.  Tensor-core engine: one launch per call of
+    run_iterations, each iteration the proposal, one 3xTF32 log-joint
+    evaluation (its gradient included) and the FP64 test; SIMT engine: propose,
+    batched log joint and accept kernels per iteration."""
+    import numpy as np
+    import torch
+    import edward_gb300 as ed
+    from edward_gb300.models import Bernoulli, Empirical, Normal
+    X, y, _ = make_data()
+    C = 4096
+    K = 10
+    w = Normal(loc=ed.zeros(N_FEAT), scale=ed.ones(N_FEAT))
+    b = Normal(loc=0.0, scale=1.0)
+    yv = Bernoulli(logits=ed.dot(X, w) + b)
+    T = args.steps * (K + 1) + 2 * args.warmup + 4
+    qw = Empirical(ed.Variable(np.zeros((T, C, N_FEAT), np.float32)), n_chains=C)
+    qb = Empirical(ed.Variable(np.zeros((T, C), np.float32)), n_chains=C)
+    props = {w: Normal(loc=w, scale=0.01 * ed.ones(N_FEAT)), b: Normal(loc=b, scale=0.01)}
+    inf = ed.MetropolisHastings({w: qw, b: qb}, props, data={yv: y}, n_chains=C)
+    inf.initialize(n_print=0, engine=args.engine)
+    inf.run_iterations(args.warmup)
+    torch.cuda.synchronize()
+    dev = torch.device("cuda")
+    with ClockSampler(0) as clk:
+        ms = flush_timed(lambda: inf.run_iterations(1), args.steps, dev)
+        inf.run_iterations(args.warmup * K)
+        ms_k = flush_timed(lambda: inf.run_iterations(K), args.steps, dev) / K
+    P = N_FEAT + 1
+    tc = inf.engine == "tc"
+    flops = (4.0 if tc else 2.0) * N_ROWS * P * C  # executed: the tensor-core form adds the adjoint
+    alg = 2.0 * N_ROWS * P * C                    # algorithmic: the log joint alone
+    if tc:
+        peak, src = tensor_peak(None if args.no_extras else measure_tf32_peak(dev))
+        kern = "hmc_glm_tc_kernel<2> (tcgen05 3xTF32, proposal and FP64 test fused in)"
+        launches = args.steps
+    else:
+        peak, src = None, None
+        kern = "mh propose + glm_partial_kernel + glm_reduce_kernel + mh accept (SIMT)"
+        launches = 4 * args.steps
+    ach = alg / (ms / 1e3) / 1e12
+    line = {"metric": "Metropolis-Hastings chain-iterations/s (Bayesian logistic regression, "
+                      "batched chains)",
+            "value": C / (ms / 1e3), "unit": "chain-iterations/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "engine": inf.engine,
+            "config": {"workload": "mh_logreg_N10000_D50_C4096_walk0.01", "chains": C,
+                       "l2_flush": "256 MB write before each timed launch, outside the events"},
+            "multi_iteration": {"iterations_per_launch": K, "ms_per_iteration": ms_k,
+                                "value": C / (ms_k / 1e3)},
+            "accept_rate": float(inf.n_accept.sum().item()) / (C * max(inf.t, 1)),
+            "gpu_launches": launches,
+            "roofline": {"bound": "tensor" if tc else "fp32", "achieved": ach,
+                         "unit": "TFLOP/s", "traffic": None, "peak": peak,
+                         "frac": ach / peak if peak else None, "peak_source": src,
+                         "kernel": kern, "algorithmic_flops_per_step": alg,
+                         "executed_flops_per_step": flops},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1499,7 +1564,7 @@ def main():
     ap.add_argument("--hier-instances", type=int, default=2048)
     ap.add_argument("--sbn-compare-steps", type=int, default=1000)
     ap.add_argument("--sbn-seeds", type=int, default=5)
-    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn", "sgld"],
+    ap.add_argument("--workload", default="hmc_logreg", choices=["hmc_logreg", "hier", "klqp", "bnn", "sbn", "sgld", "mh"],
                     help="hmc_logreg is the headline; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -1516,6 +1581,8 @@ def main():
         return run_sbn(args)
     if args.workload == "sgld":
         return run_sgld(args)
+    if args.workload == "mh":
+        return run_mh(args)
     return run_gpu(args)
 
 

@@ -178,6 +178,10 @@ _SIGS = {
                                      c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
                                      c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                      c_void_p, c_void_p, c_void_p]),
+    "edg_mh_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgMH), c_int32,
+                                    c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
+                                    c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
     "edg_sgmcmc_glm_tc_run": (c_int32, [ctypes.POINTER(EdgGLM), ctypes.POINTER(EdgSGMCMC),
                                         c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                         c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,

@@ -120,6 +120,10 @@ struct TcArgs {
   float friction, dscale;
   float* v;
   const float* noise;
+  // Metropolis-Hastings (the MH instantiation): proposal location [P] (NULL =
+  // random walk) and scale [P]; `noise` then overrides the proposal draws
+  const float* mh_loc;
+  const float* mh_scale;
 };
 
 constexpr int kMaxEPT = 4;  // chain-state elements per owner thread
@@ -207,12 +211,15 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
   }
 }
 
-// SG = false: HMC (leapfrog, Metropolis).  SG = true: SGLD / SGHMC, one
-// gradient evaluation per iteration, each iteration's update made with the
-// cached gradient of the current state in the pre phase and every proposal
-// kept (sgld.py:52-88, sghmc.py:58-102).
-template <bool SG>
+// MODE 0: HMC (leapfrog, Metropolis).  MODE 1: SGLD / SGHMC, one gradient
+// evaluation per iteration, each iteration's update made with the cached
+// gradient of the current state in the pre phase and every proposal kept
+// (sgld.py:52-88, sghmc.py:58-102).  MODE 2: Metropolis-Hastings with Normal
+// proposals, one log-joint evaluation per iteration (its gradient is
+// computed and unused) and the FP64 test of metropolis_hastings.py:64-156.
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
+  constexpr bool SG = MODE == 1, MH = MODE == 2;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int PP = a.PP, P = a.P;
   const uint32_t SB = stage_bytes(PP);
@@ -337,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
     const int ee = e - (a.cache_valid ? 0 : 1);
     const int it = cache_eval ? 0 : ee / L;
     const int l = cache_eval ? 0 : ee % L;
-    const bool need_ll = !SG && (cache_eval || l == L - 1);
+    const bool need_ll = MH || (!SG && (cache_eval || l == L - 1));
     const int64_t t = t0 + it;
     const uint32_t iter = (uint32_t)t;
 
@@ -365,6 +372,32 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
               rr[i] = ok ? (1.0f - 0.5f * a.friction) * vv + lr * gr[i] + sq * e : 0.0f;
             }
           }
+        }
+      } else if (MH) {
+        if (!cache_eval) {
+          // the proposal z' = (random walk ? z : loc) + scale e (Philox stream 6)
+          // from the accepted state, and log g(z | z') - log g(z' | z) in FP64
+          // (zero for the random walk), kept in kin0
+          double lq = 0.0;
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) {
+            const int d = d0 + i;
+            const bool ok = cvalid && i < EPT && d < P;
+            float zn = 0.0f;
+            if (ok) {
+              const float e = a.noise ? a.noise[((size_t)it * a.C + cg) * P + d]
+                                      : philox_normal(a.seed, 6u, iter, (uint32_t)cg, (uint32_t)d);
+              const float s = a.mh_scale[d], zc = zg[d];
+              zn = (a.mh_loc ? a.mh_loc[d] : zc) + s * e;
+              if (a.mh_loc) {
+                const double u0 = ((double)zc - a.mh_loc[d]) / s, u1 = ((double)zn - a.mh_loc[d]) / s;
+                lq += -0.5 * u0 * u0 + 0.5 * u1 * u1;
+              }
+            }
+            zr[i] = zn;
+          }
+          for (int o = TPC >> 1; o > 0; o >>= 1) lq += __shfl_xor_sync(0xffffffffu, lq, o);
+          kin0 = lq;
         }
       } else if (!cache_eval) {
         if (l == 0) {
@@ -488,7 +521,7 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
           double lu = 0.0;
           if (cgl < a.C)
             lu = log(a.u_ovr ? a.u_ovr[(size_t)it * a.C + cgl]
-                             : u01d(philox_at(a.seed, 2u, iter, (uint32_t)cgl, 0u).x));
+                             : u01d(philox_at(a.seed, MH ? 7u : 2u, iter, (uint32_t)cgl, 0u).x));
           s_logu[c] = lu;
         }
       }
@@ -708,6 +741,33 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             if (i < EPT && d0 + i < P) gg[d0 + i] = G[i];
           if (part == 0) a.lj[cg] = llsum + lp;
         }
+      } else if (MH) {
+        // ratio = log p(x, z') - log p(x, z) + log g(z | z') - log g(z' | z),
+        // accept if log u < ratio (Philox stream 7), on the chain's first thread
+        const double lj_new = llsum + lp;
+        double ratio = 0.0;
+        int acc_lead = 0;
+        if (part == 0 && cvalid) {
+          ratio = lj_new - a.lj[cg] + kin0;
+          acc_lead = s_logu[chain_local] < ratio ? 1 : 0;
+        }
+        const bool accept = __shfl_sync(0xffffffffu, acc_lead, lane & ~(TPC - 1)) != 0;
+        if (cvalid) {
+          if (part == 0) {
+            if (accept) a.lj[cg] = lj_new;
+            if (a.n_accept) a.n_accept[cg] += accept ? 1 : 0;
+            if (a.ratio_out) a.ratio_out[(size_t)it * a.C + cg] = ratio;
+          }
+#pragma unroll
+          for (int i = 0; i < kMaxEPT; ++i) {
+            const int d = d0 + i;
+            if (i < EPT && d < P) {
+              const float kept = accept ? zr[i] : zg[d];
+              if (accept) zg[d] = zr[i];
+              if (a.samples && t < a.T_cap) a.samples[((size_t)t * a.C + cg) * P + d] = kept;
+            }
+          }
+        }
       } else {
 #pragma unroll
         for (int i = 0; i < kMaxEPT; ++i) {
@@ -858,10 +918,10 @@ extern "C" int edg_hmc_glm_tc_prepare(const edg_glm_t* model, void* tiles, size_
 }
 
 // One launch of the tensor-core kernel: a cluster of R CTAs per 128 chains.
-template <bool SG>
+template <int MODE>
 static int launch_tc(const TcArgs& a, int PP, int R, void* stream) {
   const size_t sm = smem_bytes(PP);
-  int rc = set_max_dyn_smem(hmc_glm_tc_kernel<SG>, sm, "hmc_glm_tc_kernel");
+  int rc = set_max_dyn_smem(hmc_glm_tc_kernel<MODE>, sm, "hmc_glm_tc_kernel");
   if (rc) return rc;
   const int nclusters = (a.C + kCT - 1) / kCT;
   cudaLaunchConfig_t lc = {};
@@ -876,7 +936,7 @@ static int launch_tc(const TcArgs& a, int PP, int R, void* stream) {
   attr[0].val.clusterDim.z = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&lc, hmc_glm_tc_kernel<SG>, a);
+  const cudaError_t e = cudaLaunchKernelEx(&lc, hmc_glm_tc_kernel<MODE>, a);
   if (e != cudaSuccess) return fail(EDG_E_CUDA, "hmc_glm_tc_kernel launch: %s", cudaGetErrorString(e));
   return check_launch("hmc_glm_tc_kernel");
 }
@@ -939,7 +999,9 @@ extern "C" int edg_hmc_glm_tc_run(const edg_glm_t* model, const edg_hmc_t* cfg, 
   a.dscale = 1.0f;
   a.v = nullptr;
   a.noise = nullptr;
-  return launch_tc<false>(a, PP, R, stream);
+  a.mh_loc = nullptr;
+  a.mh_scale = nullptr;
+  return launch_tc<0>(a, PP, R, stream);
 }
 
 extern "C" int edg_sgmcmc_glm_tc_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32_t C,
@@ -997,5 +1059,64 @@ extern "C" int edg_sgmcmc_glm_tc_run(const edg_glm_t* model, const edg_sgmcmc_t*
   a.dscale = cfg->data_scale;
   a.v = cfg->method == EDG_SGMCMC_SGHMC ? v : nullptr;
   a.noise = noise_override;
-  return launch_tc<true>(a, PP, R, stream);
+  a.mh_loc = nullptr;
+  a.mh_scale = nullptr;
+  return launch_tc<1>(a, PP, R, stream);
+}
+
+extern "C" int edg_mh_glm_tc_run(const edg_glm_t* model, const edg_mh_t* cfg, int32_t C,
+                                 int32_t n_iter, const void* tiles, float* z, float* grad,
+                                 double* lj, int32_t cache_valid, int32_t* n_accept,
+                                 edg_state_t* state, float* samples, int64_t T_cap,
+                                 const float* e_override, const double* u_override,
+                                 double* ratio_out, void* stream) {
+  GLMDev m;
+  int rc = make_glm(model, &m);
+  if (rc) return rc;
+  EDG_REQUIRE(cfg && tiles && cfg->proposal_scale, EDG_E_NULL,
+              "cfg, tiles and cfg->proposal_scale must not be NULL");
+  EDG_REQUIRE(z && grad && lj && state, EDG_E_NULL, "z, grad, lj and state must not be NULL");
+  EDG_REQUIRE(C > 0 && n_iter >= 0, EDG_E_SHAPE, "C must be positive and n_iter >= 0");
+  EDG_REQUIRE(!samples || T_cap > 0, EDG_E_SHAPE, "T_cap must be positive when samples is given");
+  const int PP = padded_P(m.P);
+  EDG_REQUIRE(PP <= 64, EDG_E_UNSUPPORTED, "tensor-core Metropolis-Hastings supports P <= 64 (got %d)",
+              m.P);
+  if (n_iter == 0 && cache_valid) return EDG_OK;
+  const int ntiles = (m.N + kNR - 1) / kNR;
+  const int R = choose_R(PP, C, ntiles, 0);
+  EDG_REQUIRE(R > 0, EDG_E_UNSUPPORTED, "no cluster size fits P=%d with %d row tiles", m.P,
+              ntiles);
+  TcArgs a = {};
+  a.tiles = reinterpret_cast<const unsigned char*>(tiles);
+  a.y = m.y;
+  a.ntiles = ntiles;
+  a.N = m.N;
+  a.P = m.P;
+  a.PP = PP;
+  a.lik = m.lik;
+  a.zscale = m.lik == EDG_LIK_BERNOULLI ? -kLog2e : 1.0f;
+  a.inv_lik_var = m.inv_lik_var;
+  a.lik_norm = m.lik_norm;
+  a.prior_loc = m.prior_loc;
+  a.prior_scale = m.prior_scale;
+  a.C = C;
+  a.n_iter = n_iter;
+  a.n_steps = 1;  // one log-joint evaluation per iteration
+  a.cache_valid = cache_valid;
+  a.seed = cfg->seed;
+  a.z = z;
+  a.grad = grad;
+  a.lj = lj;
+  a.n_accept = n_accept;
+  a.state = state;
+  a.samples = samples;
+  a.T_cap = T_cap;
+  a.u_ovr = u_override;
+  a.ratio_out = ratio_out;
+  a.sg_method = -1;
+  a.dscale = 1.0f;
+  a.noise = e_override;
+  a.mh_loc = cfg->proposal_loc;
+  a.mh_scale = cfg->proposal_scale;
+  return launch_tc<2>(a, PP, R, stream);
 }

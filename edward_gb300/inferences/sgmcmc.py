@@ -200,7 +200,10 @@ class MetropolisHastings(MonteCarlo):
     with the reference's surface: ``MetropolisHastings(latent_vars,
     proposal_vars, data)``.  Proposals for the GLM family are Normal random
     walks ``Normal(loc=z, scale=s)`` or independence proposals
-    ``Normal(loc=m, scale=s)`` (constant m, s), per latent."""
+    ``Normal(loc=m, scale=s)`` (constant m, s), per latent.  Two engines, as
+    for SG-MCMC: the tensor-core HMC kernel in its Metropolis-Hastings form
+    (``edg_mh_glm_tc_run``, P <= 64) and the SIMT form (``edg_mh_glm_run``);
+    ``initialize(engine=...)`` picks one, "auto" times both once per shape."""
 
     def __init__(self, latent_vars, proposal_vars, data=None, n_chains=None):
         from ..inferences.inference import check_latent_vars
@@ -258,15 +261,67 @@ class MetropolisHastings(MonteCarlo):
         lib = _lib.load()
         self._ws_bytes = lib.edg_mh_glm_workspace_bytes(self._glm.ref(), C)
         self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
+        # tensor-core form: X re-laid into operand tiles once; the kernel also
+        # computes the proposal's gradient, into a scratch buffer
+        self._g = torch.zeros(C, spec.P, dtype=torch.float32, device=dev)
+        self._tiles = None
+        req = getattr(self, "_engine_req", "auto")
+        if req not in ("auto", "tc", "simt"):
+            raise ValueError("engine must be 'auto', 'tc' or 'simt'")
+        if req != "simt" and spec.P <= 64:
+            nbytes = lib.edg_hmc_glm_tc_tiles_bytes(self._glm.ref())
+            self._tiles = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+            _lib.call("edg_hmc_glm_tc_prepare", self._glm.ref(), _lib.ptr(self._tiles), nbytes,
+                      _lib.stream_ptr())
+        if req == "tc":
+            if self._tiles is None:
+                raise NotImplementedError("the tensor-core engine needs P <= 64")
+            self.engine = "tc"
+        elif req == "simt" or self._tiles is None:
+            self.engine = "simt"
+        else:
+            self.engine = self._autotune()
         self.train = self.update
         return self.train
 
+    def initialize(self, *args, engine="auto", **kwargs):
+        self._engine_req = engine
+        return super().initialize(*args, **kwargs)
+
+    def _run_engine(self, engine, n_iter, z, lj, cache_valid, n_accept, state, samples,
+                    e_override=None, u_override=None, ratio_out=None):
+        T_cap = samples.shape[0] if samples is not None else 0
+        if engine == "tc":
+            _lib.call("edg_mh_glm_tc_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(self._tiles), _lib.ptr(z), _lib.ptr(self._g),
+                      _lib.ptr(lj), cache_valid, _lib.ptr(n_accept), _lib.ptr(state),
+                      _lib.ptr(samples), T_cap, _lib.ptr(e_override), _lib.ptr(u_override),
+                      _lib.ptr(ratio_out), _lib.stream_ptr())
+        else:
+            _lib.call("edg_mh_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
+                      int(n_iter), _lib.ptr(z), _lib.ptr(lj), cache_valid, _lib.ptr(n_accept),
+                      _lib.ptr(state), _lib.ptr(samples), T_cap, _lib.ptr(e_override),
+                      _lib.ptr(u_override), _lib.ptr(ratio_out), _lib.ptr(self._ws),
+                      self._ws_bytes, _lib.stream_ptr())
+
+    def _autotune(self):
+        """The faster engine for this model shape, one launch of each on
+        scratch copies of the state (cached per shape and device)."""
+        z, lj = self._z.clone(), torch.zeros_like(self._lj)
+        nacc = torch.zeros_like(self._n_accept)
+        st = _lib.new_state(self._device)
+
+        def run(engine):
+            z.copy_(self._z)
+            self._run_engine(engine, 1, z, lj, 0, nacc, st, None)
+        spec = self._spec
+        key = f"N{spec.N}_P{spec.P}_C{self.C}_walk{int(bool(self._walk))}"
+        return autotune.choose("mh_engine", key, ["tc", "simt"], run)
+
     def _launch(self, n_iter, e_override=None, u_override=None, ratio_out=None):
-        _lib.call("edg_mh_glm_run", self._glm.ref(), ctypes.byref(self._cfg), self.C,
-                  int(n_iter), _lib.ptr(self._z), _lib.ptr(self._lj), self._cache_valid,
-                  _lib.ptr(self._n_accept), _lib.ptr(self._state), _lib.ptr(self._samples),
-                  self._samples.shape[0], _lib.ptr(e_override), _lib.ptr(u_override),
-                  _lib.ptr(ratio_out), _lib.ptr(self._ws), self._ws_bytes, _lib.stream_ptr())
+        self._run_engine(self.engine, n_iter, self._z, self._lj, self._cache_valid,
+                         self._n_accept, self._state, self._samples, e_override, u_override,
+                         ratio_out)
         self._cache_valid = 1
 
     update = _SGMCMC.update
