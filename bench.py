@@ -1473,7 +1473,10 @@ def run_sgld(args):
                                 "value": C / (ms_k / 1e3)},
             "gpu_launches": launches,
             "roofline": {"bound": "tensor" if tc else "fp32", "achieved": ach,
-                         "unit": "TFLOP/s", "traffic": None, "peak": peak,
+                         "unit": "TFLOP/s",
+                         "traffic": read_traffic_file(
+                             "hmc_glm_tc_kernel_sgmcmc_mh_logreg_C4096.txt") if tc else None,
+                         "peak": peak,
                          "frac": ach / peak if peak else None, "peak_source": src,
                          "kernel": kern, "algorithmic_flops_per_step": flops},
             "clocks": clk.summary()}
