@@ -33,6 +33,9 @@
 //                per-row log-likelihood; R <- r (hi, lo)
 //   backward     GT += XT R^T over rows 0-63 (24 TS MMAs, M = 128 features)
 //   B -> XT (half 1); B takes the next tile's rows 64-127; backward over rows 64-127
+// (where Dp <= 64 the second XT half is kept in XF's unused columns instead:
+// both halves are written under the forward, both staging halves refill at
+// once, and the backward is one run of 48 MMAs)
 // After the last tile each thread reads the likelihood gradient of one
 // feature for 16 chains from GT, the layout the leapfrog state is kept in
 // (registers: the feature of the thread's TMEM lane, 16 chains).  The
@@ -206,7 +209,8 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
     mbar_wait(barX0 + 8u * hf, ph[2 + hf], err);
     ph[2 + hf] ^= 1u;
   };
-  auto store_xt = [&](int hf) {  // XT columns kRPH h + k of lane d <- staging half hf
+  // XT columns (hi at chi, lo at clo) + kRPH h + k of lane d <- staging half hf
+  auto store_xt = [&](int hf, uint32_t chi, uint32_t clo) {
     const float* sh = stg + hf * kStageHalf;
 #pragma unroll
     for (int s = 0; s < kRPH / 16; ++s) {
@@ -217,8 +221,8 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         hv[k] = hi_part(v);
         lv[k] = v - hv[k];
       }
-      tmem_st16(tm + lane_base + kColXT + kRPH * h + 16 * s, hv);
-      tmem_st16(tm + lane_base + kColXT + 64 + kRPH * h + 16 * s, lv);
+      tmem_st16(tm + lane_base + chi + kRPH * h + 16 * s, hv);
+      tmem_st16(tm + lane_base + clo + kRPH * h + 16 * s, lv);
     }
   };
   auto store_xf = [&]() {  // XF lane 32q + lane (tile row) <- staging
@@ -238,7 +242,7 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       tmem_st16(tm + lane_base + kColXF + 128 + d0, lv);
     }
   };
-  auto issue_bwd = [&](int hf, bool first) {
+  auto issue_bwd = [&](int hf, bool first, uint32_t chi, uint32_t clo, bool commit) {
     if (warp == 0) {
       tc_fence_after();
       const uint32_t issue = elect_one();
@@ -248,15 +252,19 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       for (int k = 0; k < 8; ++k) {
         const uint32_t ko = (uint32_t)(16 * hf + 2 * k) * kStr;  // rows 64 hf + 8k
         const uint64_t bh = sdesc(rb + ko, kStr, kSBO), bl = sdesc(rb + kPlane + ko, kStr, kSBO);
-        const uint32_t ahi = tm + kColXT + 8 * k, alo = tm + kColXT + 64 + 8 * k;
+        const uint32_t ahi = tm + chi + 8 * k, alo = tm + clo + 8 * k;
         mma_ts_if(issue, tm + kColGT, ahi, bh, id, (first && k == 0) ? 0u : 1u);
         mma_ts_if(issue, tm + kColGT, ahi, bl, id, 1u);
         mma_ts_if(issue, tm + kColGT, alo, bh, id, 1u);
       }
-      mma_commit_if(issue, barB);
+      if (commit) mma_commit_if(issue, barB);
       __syncwarp();
     }
   };
+  // Dp <= 64: XF uses only columns [0, 64) and [128, 192), so XT's second half
+  // goes to [64, 128) and [192, 256); both halves are then built under the
+  // forward and the whole backward is issued at once
+  const bool xt1f = Dp <= 64;
 
   // gradient of the log joint at Z (registers) and (msrc, usrc): likelihood
   // by the tile loop into G, then the hierarchical prior; with need_ll the
@@ -310,7 +318,14 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
         ph[1] ^= 1u;
         tc_fence_after();
       }
-      store_xt(0);  // under the forward MMAs
+      store_xt(0, kColXT, kColXT + 64);  // under the forward MMAs
+      if (xt1f) {
+        store_xt(1, kColXF + 64, kColXF + 192);
+        tmem_st_wait();
+        __syncthreads();     // both staging halves consumed
+        prefetch(j + 1, 0);  // the next tile's copies run under this tile's MMAs
+        prefetch(j + 1, 1);
+      }
       mbar_wait(barF, ph[0], err);
       ph[0] ^= 1u;
       tc_fence_after();
@@ -351,17 +366,22 @@ __device__ void hier_tc_item(const Args& a, int item, unsigned char* smem, uint3
       fence_shared_async();
       tc_fence_before();
       __syncthreads();
-      prefetch(j + 1, 0);  // staging half A is free
-      issue_bwd(0, j == 0);
-      mbar_wait(barB, ph[1], err);  // XT is free once the first half's MMAs complete
-      ph[1] ^= 1u;
-      tc_fence_after();
-      store_xt(1);
-      tmem_st_wait();
-      tc_fence_before();
-      __syncthreads();
-      prefetch(j + 1, 1);  // staging half B is free
-      issue_bwd(1, false);
+      if (xt1f) {
+        issue_bwd(0, j == 0, kColXT, kColXT + 64, false);
+        issue_bwd(1, false, kColXF + 64, kColXF + 192, true);
+      } else {
+        prefetch(j + 1, 0);  // staging half A is free
+        issue_bwd(0, j == 0, kColXT, kColXT + 64, true);
+        mbar_wait(barB, ph[1], err);  // XT is free once the first half's MMAs complete
+        ph[1] ^= 1u;
+        tc_fence_after();
+        store_xt(1, kColXT, kColXT + 64);
+        tmem_st_wait();
+        tc_fence_before();
+        __syncthreads();
+        prefetch(j + 1, 1);  // staging half B is free
+        issue_bwd(1, false, kColXT, kColXT + 64, true);
+      }
     }
     float gl[kCPT];
     if (ntiles > 0) {
