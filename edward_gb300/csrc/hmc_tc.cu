@@ -215,8 +215,9 @@ __device__ __forceinline__ void residual_block(float (&v)[8], float (&lo)[8], co
 // evaluation per iteration, each iteration's update made with the cached
 // gradient of the current state in the pre phase and every proposal kept
 // (sgld.py:52-88, sghmc.py:58-102).  MODE 2: Metropolis-Hastings with Normal
-// proposals, one log-joint evaluation per iteration (its gradient is
-// computed and unused) and the FP64 test of metropolis_hastings.py:64-156.
+// proposals, one log-joint evaluation per iteration and the FP64 test of
+// metropolis_hastings.py:64-156; the backward side keeps its barriers and
+// does no work (no X^T copies, residual stores or backward MMAs).
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a) {
   constexpr bool SG = MODE == 1, MH = MODE == 2;
@@ -462,9 +463,13 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         for (int i = 0; i < nt; ++i) {
           const uint32_t g = gt + i, s = g & 1u;
           if (g >= 2) mbar_wait(empty + 8 * s, ((g >> 1) - 1) & 1u, err);
-          mbar_expect_tx(full + 8 * s, bytes);
-          bulk_g2s(smem_u32((s ? stage1 : stage0) + part_off),
-                   a.tiles + (size_t)(t_begin + i) * SB + part_off, bytes, full + 8 * s);
+          if (MH && lane == 1) {
+            mbar_arrive(full + 8 * s);  // Metropolis-Hastings reads no X^T
+          } else {
+            mbar_expect_tx(full + 8 * s, bytes);
+            bulk_g2s(smem_u32((s ? stage1 : stage0) + part_off),
+                     a.tiles + (size_t)(t_begin + i) * SB + part_off, bytes, full + 8 * s);
+          }
         }
       }
       __syncwarp();
@@ -542,16 +547,19 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         // the partial buffer b is free
         mbar_wait(b_r + 8 * b, (g >> 1) & 1u, err);
         tc_fence_after();
-        const uint32_t dg = tbase + COL_GP(b);
-        const uint32_t rh = tbase + COL_RHI(b), rl = tbase + COL_RLO(b);
-        const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
+        if (!MH) {  // Metropolis-Hastings needs no gradient: the commits alone
+          const uint32_t dg = tbase + COL_GP(b);
+          const uint32_t rh = tbase + COL_RHI(b), rl = tbase + COL_RLO(b);
+          const uint64_t th = s ? dt_hi[1] : dt_hi[0], tlo = s ? dt_lo[1] : dt_lo[0];
 #pragma unroll
-        for (int kk = 0; kk < kNR / 8; ++kk) {
-          mma_ts_if(issue, dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
-          mma_ts_if(issue, dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
+          for (int kk = 0; kk < kNR / 8; ++kk) {
+            mma_ts_if(issue, dg, rh + 8u * kk, tlo + 16 * kk, id_b, kk > 0 ? 1u : 0u);
+            mma_ts_if(issue, dg, rl + 8u * kk, th + 16 * kk, id_b, 1u);
+          }
+#pragma unroll
+          for (int kk = 0; kk < kNR / 8; ++kk)
+            mma_ts_if(issue, dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
         }
-#pragma unroll
-        for (int kk = 0; kk < kNR / 8; ++kk) mma_ts_if(issue, dg, rh + 8u * kk, th + 16 * kk, id_b, 1u);
         mma_commit_if(issue, b_emptyt + 8 * s);
         mma_commit_if(issue, b_gfull + 8 * b);
       }
@@ -576,7 +584,9 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
         mbar_wait(b_gfull + 8 * b, (g >> 1) & 1u, err);
         tc_fence_after();
         const uint32_t ga = tl + COL_GP(b) + gc0;
-        if (gcols == 16) {
+        if (MH) {
+          // no gradient partial was computed
+        } else if (gcols == 16) {
           float v[16];
           tmem_ld16(ga, v);
 #pragma unroll
@@ -641,8 +651,10 @@ __global__ void __launch_bounds__(kThreads, 1) hmc_glm_tc_kernel(const TcArgs a)
             const uint32_t col = 16 * qs + 8 * h;
             const int nv = nvalid - 8 * h;
             residual_block<LL, BERN, SG>(v, lo, yh, nv, a.inv_lik_var, a.lik_norm, kl, a.dscale);
-            tmem_st8(tl + COL_RHI(b) + col, v);
-            tmem_st8(tl + COL_RLO(b) + col, lo);
+            if (!MH) {  // Metropolis-Hastings keeps only the log-likelihood
+              tmem_st8(tl + COL_RHI(b) + col, v);
+              tmem_st8(tl + COL_RLO(b) + col, lo);
+            }
           }
           tmem_st_wait();
           tc_fence_before();

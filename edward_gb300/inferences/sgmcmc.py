@@ -261,8 +261,8 @@ class MetropolisHastings(MonteCarlo):
         lib = _lib.load()
         self._ws_bytes = lib.edg_mh_glm_workspace_bytes(self._glm.ref(), C)
         self._ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=dev)
-        # tensor-core form: X re-laid into operand tiles once; the kernel also
-        # computes the proposal's gradient, into a scratch buffer
+        # tensor-core form: X re-laid into operand tiles once; `_g` is the
+        # kernel's gradient scratch
         self._g = torch.zeros(C, spec.P, dtype=torch.float32, device=dev)
         self._tiles = None
         req = getattr(self, "_engine_req", "auto")

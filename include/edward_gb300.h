@@ -551,8 +551,8 @@ int edg_sgmcmc_glm_tc_run(const edg_glm_t* model, const edg_sgmcmc_t* cfg, int32
 /* ---------------------------------------------------------------- Metropolis-Hastings, tensor cores
  * Same contract as edg_mh_glm_run, with each iteration's log joint of the
  * proposals computed by the tensor-core kernel above (the proposal, the FP64
- * ratio and the accept / reject fused around it; the kernel also computes the
- * proposals' gradient, into `grad` [C, P], which is scratch here).  Requires
+ * ratio and the accept / reject fused around it).  `grad` [C, P] is scratch
+ * (the kernel writes the prior's gradient there).  Requires
  * P = D + bias <= 64; `tiles` as for edg_hmc_glm_tc_run.  Replaces the same
  * reference code as edg_mh_glm_run (metropolis_hastings.py:64-156). */
 int edg_mh_glm_tc_run(const edg_glm_t* model, const edg_mh_t* cfg, int32_t C, int32_t n_iter,
