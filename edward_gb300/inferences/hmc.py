@@ -190,7 +190,11 @@ class HMC(MonteCarlo):
         best = self._autotune_hier()
         cfg.launch, cfg.chains_per_block = best & 1, 16 if best & 2 else 32
         self.hier_engine = "tc" if best & 4 else "simt"
-        self._hier_tiles = self._hier.tc_tiles() if best & 4 else None
+        if best & 4:
+            self._hier_tiles = self._hier.tc_tiles()
+        else:
+            self._hier_tiles = None
+            self._hier._tc = None  # the re-laid copy of X is only the tensor-core engine's
         self.train = self.update
         return self.train
 
