@@ -71,10 +71,6 @@ constexpr size_t kOffScal = kOffStage + 2 * kStageHalf * 4;
 constexpr size_t kSmemBytes = kOffScal + 640 * 4 + 256 * 8 + 512 * 4 + 256 * 8 + 64 * 4;
 
 struct Args {
-  const float* X;
-  const float* y;
-  const int64_t* x_off;
-  const int64_t* y_off;
   const int32_t* Ns;
   const int32_t* Ds;
   const int32_t* order;
@@ -754,10 +750,6 @@ extern "C" int edg_hmc_hier_tc_run(const edg_hier_t* model, const edg_hmc_t* cfg
               cfg->launch);
   if (n_iter == 0 && cache_valid) return EDG_OK;
   htc::Args a;
-  a.X = model->X;
-  a.y = model->y;
-  a.x_off = model->x_offset;
-  a.y_off = model->y_offset;
   a.Ns = model->N;
   a.Ds = model->D;
   a.order = order;
