@@ -12,7 +12,8 @@ HEADER = os.path.join(ROOT, "include", "edward_gb300.h")
 
 def declared():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(edg_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|size_t|const char\*)\s+(edg_\w+)\s*\(",
+                                 src, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -75,3 +76,29 @@ def test_workspace_sizes_beyond_2gib(lib):
     assert need % 8 == 0
     small = f(ctypes.byref(g), 64)
     assert 0 < small < need
+
+
+def test_hier_tc_tile_offsets(lib):
+    """The host-side layout of the re-laid ragged batch: instance i starts at
+    the sum over earlier instances of ceil(N/128) * 128 * (round_up(D, 8) + 1)
+    floats; D outside [1, 128] or a negative N is rejected with -1."""
+    import numpy as np
+    f = lib.edg_hmc_hier_tc_tile_offsets
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+    N = np.array([1, 128, 129, 0, 20000], np.int32)
+    D = np.array([1, 8, 9, 64, 128], np.int32)
+    off = np.zeros(5, np.int64)
+    total = f(N.ctypes.data, D.ctypes.data, 5, off.ctypes.data)
+    sizes = [((n + 127) // 128) * 128 * (((d + 7) // 8) * 8 + 1) for n, d in zip(N, D)]
+    assert total == sum(sizes)
+    assert list(off) == list(np.concatenate([[0], np.cumsum(sizes)[:-1]]))
+    assert all(o % 4 == 0 for o in off)          # 16-byte aligned float offsets
+    assert f(N.ctypes.data, D.ctypes.data, 5, None) == total
+    for bad_d in (0, 129):
+        Db = D.copy()
+        Db[2] = bad_d
+        assert f(N.ctypes.data, Db.ctypes.data, 5, off.ctypes.data) == -1
+    Nb = N.copy()
+    Nb[0] = -1
+    assert f(Nb.ctypes.data, D.ctypes.data, 5, off.ctypes.data) == -1
