@@ -87,6 +87,91 @@ def cpu_baseline(budget_s=10.0, procs=None):
                       f"NumPy FP32, BLAS 1 thread/process), {wall:.1f} s wall"}
 
 
+def _cpu_mc_worker(args):
+    """Reference-structured SGLD or random-walk MH chains of the 10,000 x 50
+    logistic regression (one chain at a time); returns the seconds taken."""
+    kind, chains, n_iter, seed = args
+    import numpy as np
+    from oracle.cpu_baseline import mh_logreg_chain, sgld_logreg_chain
+    X, y, z0 = make_data()
+    P = N_FEAT + 1
+    loc, sc = np.zeros(P, np.float32), np.ones(P, np.float32)
+    t0 = time.perf_counter()
+    for c in chains:
+        if kind == "sgld":
+            sgld_logreg_chain(X, y, z0[c], n_iter, 1e-4, seed, c, loc, sc)
+        else:
+            mh_logreg_chain(X, y, z0[c], n_iter, 0.01 * np.ones(P, np.float32), seed, c, loc, sc)
+    return time.perf_counter() - t0
+
+
+def cpu_mc_baseline(kind, budget_s=10.0):
+    """SGLD / MH chains on all host cores (one process per core, chains split
+    across processes, NumPy FP32, BLAS one thread per process); a
+    cpu_baseline dict in chain-iterations/s."""
+    import multiprocessing as mp
+    procs = len(os.sched_getaffinity(0))
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    t = _cpu_mc_worker((kind, [0], 4, 1))
+    per = max(t / 4, 1e-5)  # seconds per chain-iteration
+    chains_per_proc = max(1, N_CHAINS // procs)
+    n_iter = int(min(max(budget_s / (per * chains_per_proc), 4), 200))
+    work = [(kind, list(range(p * chains_per_proc, (p + 1) * chains_per_proc)), n_iter, 1)
+            for p in range(procs)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        t0 = time.perf_counter()
+        pool.map(_cpu_mc_worker, work)
+        wall = time.perf_counter() - t0
+    total = procs * chains_per_proc * n_iter
+    what = "gradient (2 GEMVs)" if kind == "sgld" else "two log joints (1 GEMV each)"
+    return {"value": total / wall, "unit": "chain-iterations/s", "cores": procs, "kind": "port",
+            "sample": f"{procs * chains_per_proc} chains x {n_iter} iterations, one chain at a "
+                      f"time per process ({what} per iteration, NumPy FP32, BLAS 1 thread/"
+                      f"process), {wall:.1f} s wall"}
+
+
+def _cpu_hier_worker(units):
+    """Reference-structured HMC iterations (one chain each) on hierarchical
+    instances given as (X_i, y_i, global chain row); returns the seconds taken."""
+    import numpy as np
+    from oracle.cpu_baseline import hier_chain
+    t0 = time.perf_counter()
+    for X, y, row in units:
+        hier_chain(X, y, np.zeros(X.shape[1] + 2, np.float32), 1, 0.01, 10, 1, row)
+    return time.perf_counter() - t0
+
+
+def cpu_hier_baseline(Xs, ys, C, L, budget_s=10.0):
+    """One HMC iteration of single chains on instances drawn at random
+    (seeded) from the ragged batch, on all host cores; projected to the whole
+    batch by its work (sum of N_i * D_i per chain), in chain-steps/s."""
+    import multiprocessing as mp
+    import numpy as np
+    procs = len(os.sched_getaffinity(0))
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    work = np.array([x.shape[0] * x.shape[1] for x in Xs], np.float64)
+    rng = np.random.default_rng(5)
+    # calibrate on a few instances
+    probe = rng.integers(0, len(Xs), 4)
+    t = _cpu_hier_worker([(Xs[i], ys[i], int(i) * C) for i in probe])
+    per_work = max(t / work[probe].sum(), 1e-12)
+    n_units = max(procs, int(procs * budget_s / (per_work * work.mean())))
+    pick = rng.integers(0, len(Xs), n_units)
+    groups = [[(Xs[i], ys[i], int(i) * C) for i in pick[p::procs]] for p in range(procs)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        t0 = time.perf_counter()
+        pool.map(_cpu_hier_worker, groups)
+        wall = time.perf_counter() - t0
+    t_full = wall * C * work.sum() / work[pick].sum()
+    return {"value": float(len(Xs) * C * L / t_full), "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{n_units} (instance, chain) pairs drawn at random, one HMC iteration "
+                      f"of {L} leapfrog steps each (GEMV pair per gradient, NumPy FP32, BLAS 1 "
+                      f"thread/process), {wall:.1f} s wall, projected to the whole batch by "
+                      f"sum(N_i D_i)"}
+
+
 # ------------------------------------------------------------------ KLqp workload (the ELBO-gradient half)
 
 KLQP_S, KLQP_ITERS, KLQP_SEED = 5, 1000, 1
@@ -1127,6 +1212,8 @@ def run_hier(args):
                          "peak_source": src, "algorithmic_flops_per_launch": flops,
                          "x_stream_GBs": x_passes * L * work * 4 / (ms / 1e3) / 1e9},
             "engine": engine,
+            "cpu_baseline": None if args.no_cpu_baseline else cpu_hier_baseline(
+                Xs, ys, C, L, budget_s=args.cpu_budget),
             "accept_rate": float(nacc.sum().item()) / (n * args.steps),
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
@@ -1467,6 +1554,8 @@ def run_sgld(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "engine": inf.engine,
+            "cpu_baseline": None if args.no_cpu_baseline else cpu_mc_baseline(
+                "sgld", args.cpu_budget),
             "config": {"workload": "sgld_logreg_N10000_D50_C4096", "chains": C,
                        "l2_flush": "256 MB write before each timed launch, outside the events"},
             "multi_iteration": {"iterations_per_launch": K, "ms_per_iteration": ms_k,
@@ -1533,6 +1622,8 @@ def run_mh(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "engine": inf.engine,
+            "cpu_baseline": None if args.no_cpu_baseline else cpu_mc_baseline(
+                "mh", args.cpu_budget),
             "config": {"workload": "mh_logreg_N10000_D50_C4096_walk0.01", "chains": C,
                        "l2_flush": "256 MB write before each timed launch, outside the events"},
             "multi_iteration": {"iterations_per_launch": K, "ms_per_iteration": ms_k,

@@ -16,6 +16,15 @@ module reproduces the reference's execution structure in NumPy FP32:
 * KLqp (``klqp.py:707-769``): one model copy per Monte Carlo sample (GEMV
   forward + GEMV backward each), the analytic KL, then an unfused Adam apply
   (``variational_inference.py:97,120-121``).
+* SGLD (``sgld.py:63-88``): one log-joint gradient graph per iteration (two
+  GEMVs), the Langevin update with the Philox stream-5 noise.
+* MetropolisHastings (``metropolis_hastings.py:64-156``): per iteration the
+  proposal and two log-joint graphs, of the proposal and of the current
+  state (one GEMV each), then the ratio and the test.
+* HMC on one hierarchical instance (``hmc.py`` with the softplus transform
+  of ``util/random_variables.py:903-904``): as the HMC chain above, with the
+  Normal(mu, tau) prior of w, the priors of mu and tau and the log-det
+  Jacobian added to every log joint and gradient.
 
 BLAS threads are whatever NumPy's BLAS is configured with (the caller sets
 them to the number of host cores).
@@ -23,6 +32,8 @@ them to the number of host cores).
 import numpy as np
 
 from .philox import KIND_EPS, KIND_MOMENTUM, KIND_UNIFORM, normals, uniforms64
+
+KIND_SGMCMC, KIND_MH_PROPOSAL, KIND_MH_UNIFORM = 5, 6, 7
 
 
 def _softplus(x):
@@ -79,6 +90,102 @@ def hmc_logreg_chain(X, y, z0, n_iter, step_size, n_steps, seed, chain, prior_lo
             r = r + np.float32(0.5) * eps * g
         lj_new = _log_joint(X, y, zn[:D], zn[D], prior_loc, prior_scale)
         lj_old = _log_joint(X, y, z[:D], z[D], prior_loc, prior_scale)
+        ratio = 0.5 * (r0 * r0).sum() - 0.5 * (r * r).sum() + lj_new - lj_old
+        if np.log(u) < ratio:
+            z = zn
+            n_acc += 1
+    return z, n_acc
+
+
+def sgld_logreg_chain(X, y, z0, n_iter, step_size, seed, chain, prior_loc, prior_scale):
+    """n_iter reference-structured SGLD iterations of one chain (full data,
+    scale 1); returns the final state."""
+    X = np.asarray(X, np.float32)
+    y = np.asarray(y, np.float32)
+    D = X.shape[1]
+    z = np.asarray(z0, np.float32).copy()
+    for t in range(n_iter):
+        _, g = _log_joint_and_grad(X, y, z[:D], z[D], prior_loc, prior_scale)
+        e = normals(seed, KIND_SGMCMC, t, 1, D + 1, row0=chain)[0].astype(np.float32)
+        lr = np.float32(step_size / (t + 1.0) ** 0.55)
+        z = z + np.float32(0.5) * lr * g + np.sqrt(lr) * e
+    return z
+
+
+def mh_logreg_chain(X, y, z0, n_iter, scale, seed, chain, prior_loc, prior_scale):
+    """n_iter reference-structured random-walk Metropolis-Hastings iterations
+    of one chain; returns (final state, n_accept)."""
+    X = np.asarray(X, np.float32)
+    y = np.asarray(y, np.float32)
+    D = X.shape[1]
+    z = np.asarray(z0, np.float32).copy()
+    n_acc = 0
+    for t in range(n_iter):
+        e = normals(seed, KIND_MH_PROPOSAL, t, 1, D + 1, row0=chain)[0].astype(np.float32)
+        zn = z + np.asarray(scale, np.float32) * e
+        lj_new = _log_joint(X, y, zn[:D], zn[D], prior_loc, prior_scale)
+        lj_old = _log_joint(X, y, z[:D], z[D], prior_loc, prior_scale)
+        u = uniforms64(seed, KIND_MH_UNIFORM, t, 1, row0=chain)[0]
+        if np.log(u) < float(lj_new) - float(lj_old):
+            z = zn
+            n_acc += 1
+    return z, n_acc
+
+
+def _hier_log_joint(X, y, w, mu, u, mu_loc, mu_scale, tau_scale, grad):
+    """One hierarchical log-joint graph (one GEMV over X_i, plus its
+    transposed GEMV with ``grad``): Bernoulli likelihood, w ~ N(mu, tau),
+    mu ~ N(mu_loc, mu_scale), tau ~ HalfNormal(tau_scale) with tau =
+    softplus(u) and log|d tau / d u| = log sigmoid(u)."""
+    eta = X @ w                                                   # ed.dot
+    ll = -(np.maximum(eta, 0) - eta * y + np.log1p(np.exp(-np.abs(eta)))).sum(dtype=np.float32)
+    tau = np.float32(_softplus(u))
+    dev = w - mu
+    D = w.shape[0]
+    s2 = np.float32((dev * dev).sum(dtype=np.float32))
+    lw = -0.5 * s2 / (tau * tau) - D * np.log(tau) - D * np.float32(0.9189385)
+    zm = (mu - mu_loc) / mu_scale
+    lmu = -0.5 * zm * zm - np.log(mu_scale) - np.float32(0.9189385)
+    zt = tau / tau_scale
+    ltau = np.float32(0.5 * np.log(2.0 / np.pi)) - np.log(tau_scale) - 0.5 * zt * zt
+    ldj = -_softplus(-u)
+    lj = np.float32(ll + lw + lmu + ltau + ldj)
+    if not grad:
+        return lj, None
+    r = y - _sigmoid(eta)
+    gw = (X.T @ r - dev / (tau * tau)).astype(np.float32)         # tf.gradients
+    gmu = np.float32(dev.sum(dtype=np.float32) / (tau * tau) - (mu - mu_loc) / mu_scale ** 2)
+    dtau = -D / tau + s2 / tau ** 3 - tau / tau_scale ** 2
+    sg = np.float32(_sigmoid(u))
+    gu = np.float32(dtau * sg + (1.0 - sg))
+    return lj, np.concatenate([gw, [gmu, gu]]).astype(np.float32)
+
+
+def hier_chain(X, y, z0, n_iter, step_size, n_steps, seed, chain, mu_loc=0.0, mu_scale=1.0,
+               tau_scale=1.0):
+    """n_iter reference-structured HMC iterations of one chain of one
+    hierarchical instance, state (w [D], mu, u); returns (final state,
+    n_accept).  Momenta and uniforms use Philox streams 1 and 2 at global
+    chain row ``chain``, as the kernels do."""
+    X = np.asarray(X, np.float32)
+    y = np.asarray(y, np.float32)
+    D = X.shape[1]
+    z = np.asarray(z0, np.float32).copy()
+    eps = np.float32(step_size)
+    args = (np.float32(mu_loc), np.float32(mu_scale), np.float32(tau_scale))
+    n_acc = 0
+    for t in range(n_iter):
+        r0 = normals(seed, KIND_MOMENTUM, t, 1, D + 2, row0=chain)[0].astype(np.float32)
+        u = uniforms64(seed, KIND_UNIFORM, t, 1, row0=chain)[0]
+        zn, r = z.copy(), r0.copy()
+        _, g = _hier_log_joint(X, y, zn[:D], zn[D], zn[D + 1], *args, True)
+        for _ in range(n_steps):
+            r = r + np.float32(0.5) * eps * g
+            zn = zn + eps * r
+            _, g = _hier_log_joint(X, y, zn[:D], zn[D], zn[D + 1], *args, True)
+            r = r + np.float32(0.5) * eps * g
+        lj_new, _ = _hier_log_joint(X, y, zn[:D], zn[D], zn[D + 1], *args, False)
+        lj_old, _ = _hier_log_joint(X, y, z[:D], z[D], z[D + 1], *args, False)
         ratio = 0.5 * (r0 * r0).sum() - 0.5 * (r * r).sum() + lj_new - lj_old
         if np.log(u) < ratio:
             z = zn

@@ -396,3 +396,37 @@ def test_expfam_support_and_unconstrained_log_joints_agree():
             else -dn.softplus(-U)[:, 0]
         np.testing.assert_allclose(ef.log_joint_support(family, prior, stats, Z),
                                    ef.log_joint(family, prior, stats, U) - ldj, rtol=1e-12)
+
+
+def test_cpu_baseline_sgld_mh_hier_follow_the_oracle():
+    """The timed CPU restatements of SGLD, Metropolis-Hastings and
+    hierarchical HMC (FP32, one chain at a time, as the reference runs) track
+    the FP64 oracle with the same Philox draws."""
+    import numpy as np
+    from oracle import cpu_baseline as cb, glm as oglm, hier, mh, sgmcmc
+    from oracle.hmc import hmc_step
+    from oracle.philox import normals, uniforms64
+    X, y, _, _ = oglm.synthetic_logreg(300, 5, seed=1)
+    m = oglm.GLM(X, y, bias=True)
+    z0 = (np.random.default_rng(0).standard_normal(6) * 0.1).astype(np.float32)
+    loc, sc = np.zeros(6, np.float32), np.ones(6, np.float32)
+    zc = cb.sgld_logreg_chain(X, y, z0, 4, 1e-3, 9, 2, loc, sc)
+    Z0 = np.zeros((3, 6))
+    Z0[2] = z0
+    _, zr, _ = sgmcmc.run(m, Z0, 4, 1e-3, "sgld", seed=9)
+    np.testing.assert_allclose(zc, zr[2], rtol=1e-5, atol=1e-5 * np.abs(zr[2]).max())
+    s = 0.02 * np.ones(6, np.float32)
+    zc2, _ = cb.mh_logreg_chain(X, y, z0, 5, s, 9, 0, loc, sc)
+    zz = z0[None].astype(np.float64)
+    for t in range(5):
+        zz, _, _ = mh.step(m, zz, t, s.astype(np.float64), None, seed=9)
+    np.testing.assert_allclose(zc2, zz[0], rtol=1e-5, atol=1e-6)
+    Xs, ys = hier.synthetic_instances(1, seed=3, n_range=(200, 200), d_range=(7, 7))
+    f = hier.lj_grad_fn(Xs[0], ys[0])
+    zh = (np.random.default_rng(1).standard_normal(9) * 0.2).astype(np.float32)
+    zc3, _ = cb.hier_chain(Xs[0], ys[0], zh, 1, 0.02, 4, 5, 3)
+    zi = zh[None].astype(np.float64)
+    lj, g = f(zi)
+    res = hmc_step(f, zi, g, lj, normals(5, 1, 0, 1, 9, row0=3), uniforms64(5, 2, 0, 1, row0=3),
+                   0.02, 4)
+    np.testing.assert_allclose(zc3, res["z"][0], rtol=1e-5, atol=1e-5)
