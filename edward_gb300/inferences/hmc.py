@@ -25,8 +25,9 @@ class HMC(MonteCarlo):
                    cluster_size=0, *args, **kwargs):
         """``step_size`` / ``n_steps`` as in ``hmc.py:45-59``.
 
-        engine: "tc" (tcgen05 tensor cores, P <= 64), "simt" (CUDA cores) or
-        "auto" (autotuned between them); ``chains_per_block`` (SIMT) and
+        engine: "tc" (tcgen05 tensor cores: P <= 64 for a single GLM, max D_i
+        <= 128 for a ragged hierarchical batch), "simt" (CUDA cores) or "auto"
+        (autotuned between them); ``chains_per_block`` (SIMT) and
         ``cluster_size`` (tensor cores) pin a launch shape, 0 = autotuned."""
         if engine not in ("auto", "tc", "simt"):
             raise ValueError("engine must be 'auto', 'tc' or 'simt'")
