@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArg
   // the first X tile's copy overlaps the loads and draws below
   if (re > rb) issue_tile<CT, klqp_rpt<CT>()>(m, S.Xs, S.ys, rb, re);
   cp_async_commit();
+  // Launched as a programmatic dependent of the previous step: everything
+  // above (the X tile's copy) may run under the previous step's tail; the
+  // step's inputs are read only once that grid has completed.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int64_t t = *(volatile int64_t*)&a.state->t;
   const int64_t gstep = a.state->global_step;
   const float b1p = a.state->beta1_power, b2p = a.state->beta2_power;
@@ -184,7 +188,9 @@ __global__ void __launch_bounds__(kThreads, 1) klqp_glm_kernel(GLMDev m, KlqpArg
       a.ws_ll[(size_t)blockIdx.x * a.Spad + s0 + threadIdx.x] = S.ll[threadIdx.x];
     __syncthreads();
   }
-  // ---- last block finishes the step
+  // ---- last block finishes the step; the next step's grid may start its
+  // prologue once every block is here
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -777,7 +783,18 @@ static int launch_klqp(const GLMDev& m, const KlqpArgs& a, cudaStream_t st) {
               "n_samples too large");
   const int rc = set_max_dyn_smem(klqp_glm_kernel<CT>, sm, "klqp_glm_kernel");
   if (rc) return rc;
-  klqp_glm_kernel<CT><<<a.nblocks, kThreads, sm, st>>>(m, a);
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)a.nblocks);
+  lc.blockDim = dim3(kThreads);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&lc, klqp_glm_kernel<CT>, m, a);
+  if (e != cudaSuccess) return fail(EDG_E_CUDA, "klqp_glm_kernel launch: %s", cudaGetErrorString(e));
   return check_launch("klqp_glm_kernel");
 }
 
