@@ -102,3 +102,53 @@ def test_hier_tc_tile_offsets(lib):
     Nb = N.copy()
     Nb[0] = -1
     assert f(Nb.ctypes.data, D.ctypes.data, 5, off.ctypes.data) == -1
+
+
+def test_tensor_core_entry_points_validate_before_any_cuda_call():
+    """The SG-MCMC, Metropolis-Hastings and hierarchical tensor-core entry
+    points reject bad arguments on the host, with the documented codes, before
+    they touch the GPU (fake non-NULL device pointers; nothing is launched)."""
+    import ctypes as ct
+    from edward_gb300 import _lib
+    lib = _lib.load()
+    fake = ct.c_void_p(0x1000)
+    g = _lib.EdgGLM()
+    g.X = g.y = g.prior_loc = g.prior_scale = 0x1000
+    g.N, g.D, g.bias, g.lik, g.lik_scale = 100, 3, 1, 0, 1.0
+    sg = _lib.EdgSGMCMC()
+    sg.method, sg.step_size, sg.friction, sg.data_scale, sg.seed = 7, 0.1, 0.0, 1.0, 1
+    rc = lib.edg_sgmcmc_glm_tc_run(ct.byref(g), ct.byref(sg), 4, 1, fake, fake, fake, fake, 0,
+                                   fake, fake, None, 0, None, None)
+    assert rc == _lib.EDG_E_VALUE
+    sg.method = _lib.SGMCMC_SGHMC
+    rc = lib.edg_sgmcmc_glm_tc_run(ct.byref(g), ct.byref(sg), 4, 1, fake, fake, None, fake, 0,
+                                   fake, fake, None, 0, None, None)
+    assert rc == _lib.EDG_E_NULL  # SGHMC needs the velocity
+    sg.method, sg.step_size = _lib.SGMCMC_SGLD, 0.0
+    rc = lib.edg_sgmcmc_glm_tc_run(ct.byref(g), ct.byref(sg), 4, 1, fake, fake, None, fake, 0,
+                                   fake, fake, None, 0, None, None)
+    assert rc == _lib.EDG_E_VALUE
+    mhc = _lib.EdgMH()
+    mhc.proposal_loc, mhc.proposal_scale, mhc.seed = None, None, 1
+    rc = lib.edg_mh_glm_tc_run(ct.byref(g), ct.byref(mhc), 4, 1, fake, fake, fake, fake, 0, fake,
+                               fake, None, 0, None, None, None, None)
+    assert rc == _lib.EDG_E_NULL
+    g.D = 70  # P = 71 > 64
+    mhc.proposal_scale = 0x1000
+    rc = lib.edg_mh_glm_tc_run(ct.byref(g), ct.byref(mhc), 4, 1, fake, fake, fake, fake, 0, fake,
+                               fake, None, 0, None, None, None, None)
+    assert rc == _lib.EDG_E_UNSUPPORTED
+    hm = _lib.EdgHier()
+    hm.X = hm.y = hm.x_offset = hm.y_offset = hm.N = hm.D = 0x1000
+    hm.I, hm.max_D, hm.mu_loc, hm.mu_scale, hm.tau_scale = 2, 16, 0.0, 1.0, 1.0
+    cfg = _lib.EdgHMC()
+    cfg.step_size, cfg.n_steps, cfg.seed = 0.01, 3, 1
+    args = lambda tiles, toff: (ct.byref(hm), ct.byref(cfg), 4, 1, None, tiles, toff,  # noqa: E731
+                                fake, fake, fake, 0, None, fake, None, 0, None, None, None,
+                                None, None)
+    assert lib.edg_hmc_hier_tc_run(*args(None, fake)) == _lib.EDG_E_NULL
+    assert lib.edg_hmc_hier_tc_run(*args(ct.c_void_p(0x1004), fake)) == _lib.EDG_E_VALUE
+    hm.max_D = 129
+    assert lib.edg_hmc_hier_tc_run(*args(fake, fake)) == _lib.EDG_E_UNSUPPORTED
+    for code in (_lib.EDG_E_NULL, _lib.EDG_E_VALUE, _lib.EDG_E_UNSUPPORTED):
+        assert code < 0
